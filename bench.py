@@ -1,0 +1,353 @@
+#!/usr/bin/env python
+"""Throughput of the fused fluidLB D2Q9 step on GB300.
+
+Workload (default): flow past a cylinder, 8192 x 2048 nodes, BGK, populations
+stored as FP32 shifted deviations (f - w_i), anti-bounce-back pressure
+inlet/outlet, bounce-back walls and cylinder, seeded +-1e-4 velocity
+perturbation.  A "step" is one time step of the whole grid (one fused kernel
+launch).  Inputs (two 604 MB population buffers) are larger than L2.
+
+Prints one JSON line.  ``--impl reference`` times the CPU restatement of the
+reference's Numba-parallel CPU kernels (oracle/lbm_oracle.c, OpenMP over all
+host cores) on the same case.  With torchrun (N > 1) every rank advances its own
+replica of the case (the path has no exchange step on one GPU); value is the
+aggregate over ranks, time the max over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+B_LU = {"fp64": 144.0, "fp32_shifted": 72.0, "fp16_shifted": 36.0}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nx", type=int, default=8192)
+    ap.add_argument("--ny", type=int, default=2048)
+    ap.add_argument("--collision", default="BGK", choices=["BGK", "MRT"])
+    ap.add_argument("--storage", default="fp32_shifted", choices=list(B_LU))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the FP64 / FP16 / error side measurements")
+    return ap.parse_args()
+
+
+def workload_case(args, storage):
+    from pylabolt_gb300 import workloads
+    scale = args.nx / 8192.0
+    return workloads.cylinder(nx=args.nx, ny=args.ny, model=args.collision, storage=storage,
+                              radius=128.0 * scale,
+                              center=(int(2048 * scale), int(args.ny // 2 + 3)))
+
+
+def workload_name(args):
+    return f"cylinder_{args.nx}x{args.ny}_{args.collision.lower()}_{args.storage}"
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_measure(case_dict, steps_budget_s=20.0, max_steps=None, warmup=1):
+    """Times the C restatement of the reference CPU kernels on `case_dict`."""
+    from oracle.setup import build_state
+    from oracle.clib import COracle
+    st = build_state(case_dict)
+    co = COracle(st)
+    co.initialize()
+    co.run(warmup)
+    t0 = time.perf_counter()
+    co.run(1)
+    one = time.perf_counter() - t0
+    n = max(1, int(steps_budget_s / max(one, 1e-6)))
+    if max_steps is not None:
+        n = min(n, max_steps)
+    t0 = time.perf_counter()
+    co.run(n)
+    dt = time.perf_counter() - t0
+    nodes = st.Nx * st.Ny
+    return nodes * n / dt / 1e6, n, dt
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from pylabolt_gb300 import workloads  # noqa: F401
+    from oracle.clib import build
+    build()
+    cores = os.cpu_count()
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    case = workload_case(args, "fp64")
+    from oracle.setup import build_state
+    from oracle.clib import COracle
+    st = build_state(case)
+    co = COracle(st)
+    co.initialize()
+    co.run(args.warmup)
+    # bounded sample: time as many of the K steps as fit in ~90 s
+    t0 = time.perf_counter()
+    co.run(1)
+    one = time.perf_counter() - t0
+    k = max(1, min(args.steps - 1, int(90.0 / max(one, 1e-6)))) + 1
+    t0 = time.perf_counter()
+    co.run(k - 1)
+    dt = time.perf_counter() - t0 + one
+    nodes = args.nx * args.ny
+    mlups = nodes * k / dt / 1e6
+    sample = (f"{k} of {args.steps} time steps of the full {args.nx}x{args.ny} grid "
+              f"(FP64, 5 unfused sweeps + boundary kernels, OpenMP {cores} threads)")
+    line = {
+        "impl": "reference", "metric": "D2Q9 MLUPS", "value": mlups, "unit": "MLUPS",
+        "n_gpus": args.gpus, "steps": k, "warmup": args.warmup,
+        "ms_per_step": dt / k * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(args), "nx": args.nx, "ny": args.ny,
+                   "collision": args.collision},
+        "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": mlups, "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, world, rank, local):
+    import torch
+    from pylabolt_gb300.config import Case
+    from pylabolt_gb300.lbm import FluidLBM
+    from pylabolt_gb300 import capi
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = local if world > 1 else 0
+    torch.cuda.set_device(device)
+
+    nodes = args.nx * args.ny
+    case_d = workload_case(args, args.storage)
+    case = Case(case_d)
+    sim = FluidLBM(case, device=device)
+    sim.initialize()
+    sim.step(args.warmup)
+    sim.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(device)
+
+    clocks = ClockSampler(device)
+    launches0 = sim.kernel_launches
+    barrier()
+    clocks.start()
+    ms = sim.time_steps(args.steps)       # CUDA events on the handle's stream
+    barrier()
+    clk = clocks.stop()
+    launches = sim.kernel_launches - launches0
+    if dist is not None:
+        t = torch.tensor([ms], device=f"cuda:{device}", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    mlups = world * nodes * args.steps / (ms / 1e3) / 1e6
+    per_launch_ms = ms / args.steps
+    peak, peak_kind = measured_peak()
+    achieved = B_LU[args.storage] * nodes / (per_launch_ms / 1e3) / 1e9
+
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "step_kernel_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tr = json.load(f)
+        key = f"{args.collision.lower()}_{args.storage}"
+        if key in tr and tr[key].get("nodes"):
+            traffic = tr[key]["dram_bytes_per_launch"] * nodes / tr[key]["nodes"]
+
+    # ---- end to end through the Python API, host buffers ------------------
+    e2e_steps = min(args.steps, 100)
+    rho_h = np.ascontiguousarray(case.density)
+    u_h = np.ascontiguousarray(case.velocity)
+    barrier()
+    t0 = time.perf_counter()
+    sim.initialize(rho_h, u_h)                      # H2D of the initial fields
+    for _ in range(e2e_steps):
+        sim.step(1, residual=True)
+        sim.residual()                              # D2H of the step's residual
+    rho_o, u_o = sim.moments()                      # D2H of the final fields
+    t_e2e = time.perf_counter() - t0
+    e2e = {"value": world * nodes * e2e_steps / t_e2e / 1e6, "unit": "MLUPS",
+           "h2d_bytes_per_step": int((rho_h.nbytes + u_h.nbytes) / e2e_steps),
+           "d2h_bytes_per_step": int(8 * 8 + (rho_o.nbytes + u_o.nbytes) / e2e_steps),
+           "steps": e2e_steps,
+           "what": "FluidLBM.initialize(host rho,u) + per step lbm_step_ex(RESIDUAL) + "
+                   "lbm_residual readback + final lbm_get_moments readback"}
+
+    extra = {}
+    if not args.no_extra and rank == 0:
+        extra = side_measurements(args, case_d, sim, nodes, peak)
+    sim.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            from oracle.clib import build
+            build()
+            cpu_case = workload_case(args, "fp64")
+            mlups_cpu, n_cpu, dt_cpu = cpu_measure(cpu_case, steps_budget_s=15.0, max_steps=200)
+            cpu = {"value": mlups_cpu, "unit": "MLUPS", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"{n_cpu} full time steps of the same {args.nx}x{args.ny} case "
+                             f"in {dt_cpu:.1f} s (C restatement of the reference CPU kernels, "
+                             f"FP64, OpenMP)"}
+        except Exception as e:  # reported, never substituted
+            cpu = {"value": None, "unit": "MLUPS", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {e}"}
+
+    if rank == 0:
+        line = {
+            "metric": "D2Q9 MLUPS", "value": mlups, "unit": "MLUPS", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_launch_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if args.storage != "fp64" else "f64", "data": "synthetic",
+            "config": {"workload": workload_name(args), "nx": args.nx, "ny": args.ny,
+                       "collision": args.collision, "storage": args.storage,
+                       "bytes_per_lattice_update": B_LU[args.storage],
+                       "l2": "inputs larger than L2 (two population buffers of "
+                             f"{9 * nodes * B_LU[args.storage] / 18 / 1e6:.0f} MB)",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": traffic},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": int(launches),
+            "clocks": clk,
+        }
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def side_measurements(args, case_d, sim32, nodes, peak):
+    """FP64 and FP16 throughput of the same step and the FP32/FP16 error
+    against FP64 after a short run from the same initial state."""
+    from pylabolt_gb300.config import Case
+    from pylabolt_gb300.lbm import FluidLBM
+    out = {}
+    case = Case(case_d)
+    res = {}
+    for storage, steps in (("fp64", max(5, args.steps // 10)), ("fp16_shifted", args.steps)):
+        with FluidLBM(case, storage=storage) as s:
+            s.initialize()
+            s.step(3)
+            s.synchronize()
+            ms = s.time_steps(steps)
+            mlups = nodes * steps / (ms / 1e3) / 1e6
+            res[storage] = {"mlups": mlups,
+                            "roofline_frac": B_LU[storage] * nodes / (ms / steps / 1e3) / 1e9 / peak}
+    out["fp64"] = res["fp64"]
+    out["fp16_shifted"] = res["fp16_shifted"]
+    err_steps = 200
+    us = {}
+    for storage in ("fp64", "fp32_shifted", "fp16_shifted"):
+        with FluidLBM(case, storage=storage) as s:
+            s.initialize()
+            s.step(err_steps, moments=True)
+            us[storage] = s.moments()[1]
+    ref = us["fp64"]
+    fluid = ~case.solid
+    for storage in ("fp32_shifted", "fp16_shifted"):
+        d = us[storage][fluid] - ref[fluid]
+        out.setdefault("error_vs_fp64", {})[storage] = {
+            "steps": err_steps,
+            "u_rel_l2": float(np.linalg.norm(d) / np.linalg.norm(ref[fluid])),
+            "u_max_abs_over_max": float(np.abs(d).max() / np.abs(ref[fluid]).max())}
+    return out
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    run_gb300(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,185 @@
+/*
+ * lbm_gb300.h -- C-ABI of the GB300 fluidLB D2Q9 step (liblbm_gb300.so).
+ *
+ * The reference (Malyadeep/pylabolt) is pure Python: its hot path is a set of
+ * Numba kernels selected by name inside the operator layer.  These entry points
+ * replace that layer for one case on one GPU.  Each declaration names the
+ * reference code it stands in for.
+ *
+ * Conventions
+ *  - Every call returns an int status (LBM_OK == 0).  lbm_last_error() gives a
+ *    message for the last failing call of the calling thread.
+ *  - Host arrays are borrowed for the duration of the call only.  The library
+ *    owns all device memory of a handle.
+ *  - Node arrays on the host use the reference's inner-node order
+ *    ind = x * ny + y (x-major, y fastest), i.e. the padded index
+ *    (x+1)*(ny+2)+(y+1) of pylabolt/base/fields.py with the ghost ring removed,
+ *    unless a `layout` argument selects the padded form.
+ *  - One CUDA stream per handle; a handle is not thread-safe.  Calls that
+ *    return data to the host synchronise that stream with a bounded wait
+ *    (LBM_ERR_TIMEOUT when it expires).
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct LbmHandle LbmHandle;
+
+/* status codes */
+#define LBM_OK 0
+#define LBM_ERR_ARG 1        /* invalid argument or configuration           */
+#define LBM_ERR_CUDA 2       /* a CUDA runtime call failed                   */
+#define LBM_ERR_NONFINITE 3  /* the residual pass met a non-finite moment    */
+#define LBM_ERR_TIMEOUT 4    /* a bounded device wait expired                */
+#define LBM_ERR_STATE 5      /* call out of order (e.g. step before init)    */
+#define LBM_ERR_ALLOC 6      /* device allocation failed                     */
+
+/* storage / arithmetic of the populations */
+#define LBM_FP64 0           /* f in FP64, reference operation order         */
+#define LBM_FP32_SHIFTED 1   /* f - w_i stored in FP32, FP32 arithmetic      */
+#define LBM_FP16_SHIFTED 2   /* (f - w_i)*scale stored in FP16, FP32 arithmetic */
+
+/* collision model -- pylabolt/solvers/fluidLB.py:35-40 names */
+#define LBM_BGK 0
+#define LBM_MRT 1
+
+/* forcing model -- pylabolt/solvers/fluidLB.py:27-33 names */
+#define LBM_FORCING_NONE 0
+#define LBM_GUO_LINEAR 1
+#define LBM_GUO_SECOND_ORDER 2
+
+/* per-direction link kinds of a boundary ("special") node */
+#define LBM_LINK_PULL 0   /* f_i(x) <- f*_i(src): plain or periodic-wrapped pull,
+                             also the zero_gradient source                      */
+#define LBM_LINK_ZERO 1   /* f_i(x) <- 0: pull from a ghost node nobody fills   */
+#define LBM_LINK_BB 2     /* f_i(x) <- f*_ibar(x): halfway bounce-back          */
+#define LBM_LINK_MBB 3    /* f_i(x) <- f*_ibar(x) - 2 w rho(x) inv_cs_2 param:
+                             moving wall / moving solid, param = c_ibar . u_w   */
+#define LBM_LINK_ABB 4    /* f_i(x) <- -f*_ibar(x) + 2 w rho_w (1 + ...):
+                             anti-bounce-back, param = rho_w, aux = node x+n    */
+
+/* moment layouts for lbm_get_moments / lbm_init_fields */
+#define LBM_LAYOUT_INNER 0   /* [nx*ny], ind = x*ny + y                    */
+#define LBM_LAYOUT_PADDED 1  /* [(nx+2)*(ny+2)], ind = x*(ny+2) + y, ghosts 0 */
+
+/* flags of lbm_step_ex: what the last step of the call records */
+#define LBM_STEP_MOMENTS 1   /* keep rho/u of that step for lbm_get_moments */
+#define LBM_STEP_RESIDUAL 2  /* evaluate the residual for lbm_residual      */
+
+typedef struct {
+  int32_t nx, ny;          /* inner grid (mesh_dict["grid"])                   */
+  int32_t precision;       /* LBM_FP64 / LBM_FP32_SHIFTED / LBM_FP16_SHIFTED   */
+  int32_t collision;       /* LBM_BGK / LBM_MRT                                */
+  int32_t forcing;         /* LBM_FORCING_NONE / LBM_GUO_*                     */
+  int32_t body_force_field;/* 1: per-node force field replaces rho*g           */
+  int32_t device;          /* CUDA device ordinal                              */
+  int32_t reserved;
+  double omega;            /* 1/tau, tau = kin_visc*inv_cs_2 + 0.5             */
+  double inv_cs_2, inv_cs_4; /* pylabolt/base/lattice.py:41-44 values           */
+  double eps;              /* control.float_min (FP64 eps)                     */
+  double gravity[2];       /* forcing_dict["gravity"]; zero for forcing None   */
+  double mrt_s[4];         /* s_e, s_eps, s_q, s_nu (MRT only)                 */
+  double fp16_scale;       /* storage scale of LBM_FP16_SHIFTED (power of 2)   */
+} LbmConfig;
+
+/* Links of one boundary node: every node whose nine incoming populations are
+ * not all plain in-domain pulls (domain edges, periodic edges, solid
+ * neighbours) and every node whose moments an anti-bounce-back link reads. */
+typedef struct {
+  int64_t node;            /* inner index x*ny + y                          */
+  int64_t src[9];          /* PULL: source node (inner index)               */
+  int64_t aux[9];          /* ABB: node x+n (inner index; must be listed)   */
+  double param[9];         /* MBB: c_ibar . u ; ABB: rho_w                  */
+  int8_t type[9];          /* LBM_LINK_*                                    */
+  int8_t reserved[7];
+} LbmNodeLinks;
+
+/* Creates a case on the GPU: geometry, link table and parameters.  Replaces
+ * the operator set-up of Solver.__init__/set_backend
+ * (pylabolt/solvers/fluidLB.py:109-204: State, CollisionOperator,
+ * ForceOperator, StreamingOperator, BoundaryOperator kernel binding).
+ * node_solid: [nx*ny] bytes, 1 = solid (pylabolt/base/fields.py `solid`). */
+int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
+               const LbmNodeLinks* links, int64_t nlinks, LbmHandle** out);
+
+/* Sets rho/u and the populations entering the next step to f_eq(rho, u) on
+ * fluid nodes; solid nodes keep rho/u as given (reported by lbm_get_moments).
+ * Replaces initialize_pop_density_based_second_order
+ * (pylabolt/parallel/cpu/equilibrium_kernels.py:38-78) and the initial
+ * fields of pylabolt/base/init_fields.py.  rho: [n], u: [n][2] in `layout`. */
+int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout);
+
+/* Sets a per-node body force field F[n][2] (inner layout) used instead of
+ * rho*g when cfg.body_force_field == 1 (extension: no reference key). */
+int lbm_set_body_force(LbmHandle* h, const double* force);
+
+/* Advances nsteps time steps, each one Solver.single_time_step
+ * (pylabolt/solvers/fluidLB.py:206-253: density, force, velocity, collide,
+ * periodic wrap, stream, boundaries) as one fused kernel launch.  Long runs
+ * are replayed from a captured CUDA graph (the reference captures one step,
+ * fluidLB.py:270-287). */
+int lbm_step(LbmHandle* h, int64_t nsteps);
+
+/* As lbm_step; the last step also records what `flags` asks for
+ * (LBM_STEP_MOMENTS / LBM_STEP_RESIDUAL).  The host loop of Solver.run
+ * (fluidLB.py:352-384) calls this on std_out_interval / save_interval steps. */
+int lbm_step_ex(LbmHandle* h, int64_t nsteps, int flags);
+
+/* rho/u of the last step recorded with LBM_STEP_MOMENTS: the fields the
+ * reference holds in state.fields.density/velocity after that step and writes
+ * with InputOutputOperator.write_fields (pylabolt/utils/io_operator.py:158-190).
+ * rho: [n], u: [n][2] in `layout`. */
+int lbm_get_moments(LbmHandle* h, double* rho, double* u, int layout);
+
+/* Residuals {res_rho, res_ux, res_uy} of the last LBM_STEP_RESIDUAL step:
+ * sqrt(sum (phi-phi_old)^2 / (sum phi_old^2 + eps)) over fluid nodes, phi_old
+ * from the previous residual step (zeros at first) -- ResidueOperator,
+ * pylabolt/utils/residues.py:171-222.  Returns LBM_ERR_NONFINITE when that
+ * pass met a non-finite rho or u. */
+int lbm_residual(LbmHandle* h, double out[3]);
+
+/* FP64 sums over fluid nodes of the stored post-collision populations:
+ * {sum f, sum cx f, sum cy f} (mass and momentum diagnostics; extension). */
+int lbm_conservation(LbmHandle* h, double out[3]);
+
+/* Post-collision populations of the last step (the reference's pop_fluid),
+ * FP64 in the padded AoS layout [(nx+2)*(ny+2)][9] of
+ * pylabolt/base/fields.py:83-92; ghost and solid nodes are 0. */
+int lbm_get_populations(LbmHandle* h, double* pop);
+
+/* Sets the populations entering the next step (the reference's pop_fluid_new)
+ * from the padded AoS layout; the next step starts from them directly. */
+int lbm_set_populations(LbmHandle* h, const double* pop_new);
+
+/* Number of completed steps since the last init. */
+int lbm_time(LbmHandle* h, int64_t* t);
+
+/* Number of fused step-kernel launches issued since the handle was created. */
+int lbm_kernel_launches(LbmHandle* h, int64_t* n);
+
+/* Device bytes held by the handle. */
+int lbm_device_bytes(LbmHandle* h, int64_t* bytes);
+
+/* Runs `nsteps` as lbm_step and returns the elapsed device time in
+ * milliseconds, measured with CUDA events on the handle's stream. */
+int lbm_time_steps(LbmHandle* h, int64_t nsteps, double* ms);
+
+/* Waits (bounded by timeout_s seconds) for all work of the handle. */
+int lbm_synchronize(LbmHandle* h, double timeout_s);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* lbm_last_error(void);
+
+/* Releases the handle and its device memory. */
+int lbm_destroy(LbmHandle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_GB300_H */

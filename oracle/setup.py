@@ -195,23 +195,20 @@ def build_state(sim, periodic_mode="wrap"):
             sm = od["solid_motion_dict"]
             lin = np.array(sm["linear_velocity"], dtype=np.float64)
             ang = np.float64(sm["angular_velocity"])
-        for ind in np.nonzero(~st.ghost)[0]:
-            xg, yg = ind // st.nyp - 1, ind % st.nyp - 1
-            rx, ry = xg - cx, yg - cy
-            rxm, rym = rx, ry
-            if st.x_periodic:
-                if abs(rx + nx) < abs(rxm):
-                    rxm = rx + nx
-                if abs(rx - nx) < abs(rxm):
-                    rxm = rx - nx
-            if st.y_periodic:
-                if abs(ry + ny) < abs(rym):
-                    rym = ry + ny
-                if abs(ry - ny) < abs(rym):
-                    rym = ry - ny
-            if rxm * rxm + rym * rym <= r * r:
-                st.solid[ind] = True
-                st.velocity[ind, 0] = lin[0] - ang * rym
-                st.velocity[ind, 1] = lin[1] + ang * rxm
-                st.density[ind] = np.float64(od["density"])
+        ind = np.nonzero(~st.ghost)[0]
+        xg, yg = ind // st.nyp - 1, ind % st.nyp - 1
+        rx, ry = xg - cx, yg - cy
+        rxm, rym = rx.copy(), ry.copy()
+        if st.x_periodic:
+            rxm = np.where(np.abs(rx + nx) < np.abs(rxm), rx + nx, rxm)
+            rxm = np.where(np.abs(rx - nx) < np.abs(rxm), rx - nx, rxm)
+        if st.y_periodic:
+            rym = np.where(np.abs(ry + ny) < np.abs(rym), ry + ny, rym)
+            rym = np.where(np.abs(ry - ny) < np.abs(rym), ry - ny, rym)
+        inside = rxm * rxm + rym * rym <= r * r
+        hit = ind[inside]
+        st.solid[hit] = True
+        st.velocity[hit, 0] = lin[0] - ang * rym[inside]
+        st.velocity[hit, 1] = lin[1] + ang * rxm[inside]
+        st.density[hit] = np.float64(od["density"])
     return st

@@ -1,0 +1,151 @@
+// Auxiliary kernels of one storage precision (conversions, conservation sums)
+// and the KernelSet that bundles them with the fused step kernel.
+#pragma once
+#include "lbm_kernels.cuh"
+
+namespace lbm {
+
+constexpr int kStepBlock = 256;
+
+template <class S>
+__global__ void convert_kernel(const Geom g, const Params p, S* f, double* f64,
+                               int dir) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= g.nx) return;
+  const long long n = (long long)y * g.pitch + x;
+  const bool solid = g.cls[n] == 2;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const long long i = k * g.plane + n;
+    const double w = Store<S>::shifted ? Wk(k) : 0.0;
+    if (dir == 0) {
+      f64[i] = solid ? 0.0 : double(Store<S>::ld(f, i, p)) + w;
+    } else {
+      Store<S>::st(f, i, typename Store<S>::T(solid ? 0.0 : f64[i] - w), p);
+    }
+  }
+}
+
+template <class T>
+__global__ void moments_to_f64_kernel(const Geom g, const T* mr, const T* mx,
+                                      const T* my, double* out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= g.nx) return;
+  const long long n = (long long)y * g.pitch + x;
+  out[n] = double(mr[n]);
+  out[g.plane + n] = double(mx[n]);
+  out[2 * g.plane + n] = double(my[n]);
+}
+
+template <class T>
+__global__ void body_from_f64_kernel(const Geom g, const double* in, T* out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= g.nx) return;
+  const long long n = (long long)y * g.pitch + x;
+  out[n] = T(in[n]);
+  out[g.plane + n] = T(in[g.plane + n]);
+}
+
+// One block per row; fixed summation order -> deterministic.
+template <class S>
+__global__ void conservation_kernel(const Geom g, const Params p, const S* f,
+                                    double* partials) {
+  const int y = blockIdx.x;
+  double s[3] = {0, 0, 0};
+  for (int x = threadIdx.x; x < g.nx; x += blockDim.x) {
+    const long long n = (long long)y * g.pitch + x;
+    if (g.cls[n] == 2) continue;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const double v = double(Store<S>::ld(f, k * g.plane + n, p)) +
+                       (Store<S>::shifted ? Wk(k) : 0.0);
+      s[0] += v;
+      s[1] += CXk(k) * v;
+      s[2] += CYk(k) * v;
+    }
+  }
+  __shared__ double sh[3][256];
+  for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] = s[c];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x < 8)
+    partials[(long long)y * 8 + threadIdx.x] = threadIdx.x < 3 ? sh[threadIdx.x][0] : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+template <class S>
+struct Kernels {
+  using T = typename Store<S>::T;
+  static dim3 node_grid(const Geom& g) {
+    return dim3((g.nx + kStepBlock - 1) / kStepBlock, g.ny);
+  }
+  template <int COLL, int FORC>
+  static cudaError_t step_t(const StepArgs& a, dim3 grid, dim3 block, cudaStream_t s) {
+    step_kernel<S, COLL, FORC><<<grid, block, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  static cudaError_t step(int coll, int forc, const StepArgs& a, dim3 grid,
+                          dim3 block, cudaStream_t s) {
+    if (coll == 0) {
+      if (forc == 0) return step_t<0, 0>(a, grid, block, s);
+      if (forc == 1) return step_t<0, 1>(a, grid, block, s);
+      return step_t<0, 2>(a, grid, block, s);
+    }
+    if (forc == 0) return step_t<1, 0>(a, grid, block, s);
+    if (forc == 1) return step_t<1, 1>(a, grid, block, s);
+    return step_t<1, 2>(a, grid, block, s);
+  }
+  static cudaError_t init(const Geom& g, const Params& p, const double* rho,
+                          const double* u, void* f, void* mr, void* mx, void* my,
+                          cudaStream_t s) {
+    init_kernel<S><<<node_grid(g), kStepBlock, 0, s>>>(
+        g, p, rho, u, static_cast<S*>(f), static_cast<T*>(mr),
+        static_cast<T*>(mx), static_cast<T*>(my));
+    return cudaGetLastError();
+  }
+  static cudaError_t convert(const Geom& g, const Params& p, void* f,
+                             double* f64, int dir, cudaStream_t s) {
+    convert_kernel<S><<<node_grid(g), kStepBlock, 0, s>>>(g, p, static_cast<S*>(f),
+                                                           f64, dir);
+    return cudaGetLastError();
+  }
+  static cudaError_t moments_to_f64(const Geom& g, const void* mr, const void* mx,
+                                    const void* my, double* out, cudaStream_t s) {
+    moments_to_f64_kernel<T><<<node_grid(g), kStepBlock, 0, s>>>(
+        g, static_cast<const T*>(mr), static_cast<const T*>(mx),
+        static_cast<const T*>(my), out);
+    return cudaGetLastError();
+  }
+  static cudaError_t body_from_f64(const Geom& g, const double* in, void* out,
+                                   cudaStream_t s) {
+    body_from_f64_kernel<T><<<node_grid(g), kStepBlock, 0, s>>>(g, in,
+                                                                 static_cast<T*>(out));
+    return cudaGetLastError();
+  }
+  static cudaError_t conservation(const Geom& g, const Params& p, const void* f,
+                                  double* partials, cudaStream_t s) {
+    conservation_kernel<S><<<g.ny, 256, 0, s>>>(g, p, static_cast<const S*>(f), partials);
+    return cudaGetLastError();
+  }
+  static KernelSet make() {
+    KernelSet k;
+    k.elem_bytes = sizeof(S);
+    k.compute_bytes = sizeof(T);
+    k.step = &step;
+    k.init = &init;
+    k.convert = &convert;
+    k.moments_to_f64 = &moments_to_f64;
+    k.body_from_f64 = &body_from_f64;
+    k.conservation = &conservation;
+    return k;
+  }
+};
+
+}  // namespace lbm

@@ -1,0 +1,618 @@
+// C-ABI of liblbm_gb300.so (declarations and documentation: include/lbm_gb300.h).
+//
+// The handle owns every device allocation of one case.  All arguments are
+// validated on the host before any device work: in particular every bulk node
+// (a node without a link record) must have its eight neighbours inside the
+// grid and fluid, and every link source/aux index must be a valid fluid node,
+// so the fused kernel never reads outside its arrays.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "lbm_gb300.h"
+#include "lbm_internal.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define LBM_CUDA(expr)                                                         \
+  do {                                                                         \
+    cudaError_t e_ = (expr);                                                   \
+    if (e_ != cudaSuccess)                                                     \
+      return fail(LBM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+constexpr int kBlock = 256;
+constexpr int kGraphChunk = 32;   // steps per captured graph (even)
+constexpr int kCX[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+constexpr int kCY[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+
+}  // namespace
+
+struct LbmHandle {
+  LbmConfig cfg{};
+  const lbm::KernelSet* ks = nullptr;
+  lbm::Geom g{};
+  lbm::Params p{};
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  size_t dev_bytes = 0;
+  void* pop[2] = {nullptr, nullptr};
+  void* side[2] = {nullptr, nullptr};
+  void* mom[3] = {nullptr, nullptr, nullptr};
+  void* old[3] = {nullptr, nullptr, nullptr};
+  void* body = nullptr;
+  double* partials = nullptr;
+  long long nparts = 0;
+  double* red = nullptr;       // device [16]: residual sums, conservation sums
+  double* host_red = nullptr;  // pinned  [16]
+  double* stage = nullptr;     // device FP64 staging
+  size_t stage_elems = 0;
+  int cur = 0;
+  bool initialized = false, nopull = true, has_moments = false, has_residual = false;
+  int64_t t = 0, launches = 0;
+  cudaGraphExec_t gexec = nullptr;
+  int gparity = 0;
+  dim3 grid, block;
+  double timeout_s = 600.0;
+
+  ~LbmHandle() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    for (void* a : allocs) cudaFree(a);
+    if (host_red) cudaFreeHost(host_red);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  int alloc(void** p, size_t bytes) {
+    if (std::getenv("LBM_FAIL_ALLOC"))
+      return fail(LBM_ERR_ALLOC, "device allocation refused (LBM_FAIL_ALLOC is set)");
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(LBM_ERR_ALLOC, "cudaMalloc(" + std::to_string(bytes) +
+                                     " bytes): " + cudaGetErrorString(e));
+    }
+    allocs.push_back(*p);
+    dev_bytes += bytes;
+    return LBM_OK;
+  }
+
+  int wait() {
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+      cudaError_t e = cudaStreamQuery(stream);
+      if (e == cudaSuccess) return LBM_OK;
+      if (e != cudaErrorNotReady)
+        return fail(LBM_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e));
+      double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      if (el > timeout_s)
+        return fail(LBM_ERR_TIMEOUT, "device work did not finish within " +
+                                         std::to_string(timeout_s) + " s");
+      std::this_thread::sleep_for(std::chrono::microseconds(el < 0.01 ? 5 : 200));
+    }
+  }
+
+  int ensure_stage(size_t elems) {
+    if (stage_elems >= elems) return LBM_OK;
+    if (stage) {
+      LBM_CUDA(cudaStreamSynchronize(stream));
+      for (auto it = allocs.begin(); it != allocs.end(); ++it)
+        if (*it == stage) {
+          allocs.erase(it);
+          break;
+        }
+      dev_bytes -= stage_elems * sizeof(double);
+      cudaFree(stage);
+      stage = nullptr;
+      stage_elems = 0;
+    }
+    int rc = alloc(reinterpret_cast<void**>(&stage), elems * sizeof(double));
+    if (rc) return rc;
+    stage_elems = elems;
+    return LBM_OK;
+  }
+
+  long long host_nodes(int layout) const {
+    return layout == LBM_LAYOUT_PADDED ? (long long)(cfg.nx + 2) * (cfg.ny + 2)
+                                       : (long long)cfg.nx * cfg.ny;
+  }
+
+  int launch(int flags) {
+    lbm::StepArgs a;
+    a.g = g;
+    a.p = p;
+    a.fin = pop[cur];
+    a.fout = pop[cur ^ 1];
+    a.side_in = side[cur];
+    a.side_out = side[cur ^ 1];
+    a.rho = mom[0];
+    a.ux = mom[1];
+    a.uy = mom[2];
+    a.rho_old = old[0];
+    a.ux_old = old[1];
+    a.uy_old = old[2];
+    a.partials = partials;
+    a.body = body;
+    a.flags = flags;
+    LBM_CUDA(ks->step(cfg.collision, cfg.forcing, a, grid, block, stream));
+    cur ^= 1;
+    return LBM_OK;
+  }
+
+  int capture_graph() {
+    cudaGraph_t graph = nullptr;
+    LBM_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    const int c0 = cur;
+    int rc = LBM_OK;
+    for (int i = 0; i < kGraphChunk && rc == LBM_OK; ++i) rc = launch(0);
+    cudaError_t e = cudaStreamEndCapture(stream, &graph);
+    cur = c0;
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      gexec = nullptr;
+      return fail(LBM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+    gparity = c0;
+    return LBM_OK;
+  }
+};
+
+extern "C" {
+
+const char* lbm_last_error(void) { return g_err.c_str(); }
+
+int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
+               const LbmNodeLinks* links, int64_t nlinks, LbmHandle** out) {
+  if (!cfg || !node_solid || !out || (nlinks > 0 && !links) || nlinks < 0)
+    return fail(LBM_ERR_ARG, "lbm_create: null argument");
+  *out = nullptr;
+  const LbmConfig& c = *cfg;
+  if (c.nx < 1 || c.ny < 1 || c.ny > 65535 || c.nx > (1 << 26))
+    return fail(LBM_ERR_ARG, "lbm_create: grid must satisfy 1 <= nx, 1 <= ny <= 65535");
+  if (c.precision < LBM_FP64 || c.precision > LBM_FP16_SHIFTED)
+    return fail(LBM_ERR_ARG, "lbm_create: unknown precision");
+  if (c.collision != LBM_BGK && c.collision != LBM_MRT)
+    return fail(LBM_ERR_ARG, "lbm_create: unknown collision model");
+  if (c.forcing < LBM_FORCING_NONE || c.forcing > LBM_GUO_SECOND_ORDER)
+    return fail(LBM_ERR_ARG, "lbm_create: unknown forcing model");
+  if (!(c.omega > 0.0 && c.omega < 2.0))
+    return fail(LBM_ERR_ARG, "lbm_create: omega = 1/tau must lie in (0, 2)");
+  if (c.precision == LBM_FP16_SHIFTED && !(c.fp16_scale > 0.0))
+    return fail(LBM_ERR_ARG, "lbm_create: fp16_scale must be > 0");
+
+  const lbm::KernelSet* ks = c.precision == LBM_FP64 ? &lbm::kernels_fp64()
+                             : c.precision == LBM_FP32_SHIFTED ? &lbm::kernels_fp32()
+                                                                : &lbm::kernels_fp16();
+  const int nx = c.nx, ny = c.ny;
+  const int align = 128 / ks->elem_bytes;
+  const int pitch = (nx + align - 1) / align * align;
+  const long long plane = (long long)ny * pitch;
+  if (plane >= (1LL << 31) / 1)
+    return fail(LBM_ERR_ARG, "lbm_create: grid too large (ny*pitch must be < 2^31)");
+  const long long nin = (long long)nx * ny;
+
+  // ---- host-side geometry and link table --------------------------------
+  std::vector<uint8_t> cls(plane, 0);
+  for (int x = 0; x < nx; ++x)
+    for (int y = 0; y < ny; ++y)
+      if (node_solid[(long long)x * ny + y]) cls[(long long)y * pitch + x] = 2;
+  std::vector<int> recmap(plane, -1);
+  for (int64_t r = 0; r < nlinks; ++r) {
+    const int64_t node = links[r].node;
+    if (node < 0 || node >= nin)
+      return fail(LBM_ERR_ARG, "lbm_create: link record " + std::to_string(r) + " has node out of range");
+    const long long dn = (long long)(node % ny) * pitch + node / ny;
+    if (cls[dn] == 2)
+      return fail(LBM_ERR_ARG, "lbm_create: link record for a solid node " + std::to_string(node));
+    if (recmap[dn] >= 0)
+      return fail(LBM_ERR_ARG, "lbm_create: node " + std::to_string(node) + " has two link records");
+    recmap[dn] = (int)r;
+    cls[dn] = 1;
+  }
+  std::vector<int8_t> rtype(9 * std::max<int64_t>(nlinks, 1), 0);
+  std::vector<int> rsrc(9 * std::max<int64_t>(nlinks, 1), 0), raux(9 * std::max<int64_t>(nlinks, 1), 0);
+  std::vector<double> rparam(9 * std::max<int64_t>(nlinks, 1), 0.0);
+  for (int64_t r = 0; r < nlinks; ++r) {
+    const LbmNodeLinks& L = links[r];
+    for (int k = 0; k < 9; ++k) {
+      const int ty = L.type[k];
+      const size_t li = 9 * r + k;
+      rtype[li] = (int8_t)ty;
+      rparam[li] = L.param[k];
+      if (k == 0) continue;  // the rest population is always the node's own
+      if (ty == LBM_LINK_PULL) {
+        const int64_t s = L.src[k];
+        if (s < 0 || s >= nin)
+          return fail(LBM_ERR_ARG, "lbm_create: PULL source out of range at node " + std::to_string(L.node));
+        const long long ds = (long long)(s % ny) * pitch + s / ny;
+        if (cls[ds] == 2)
+          return fail(LBM_ERR_ARG, "lbm_create: PULL source is solid at node " + std::to_string(L.node));
+        rsrc[li] = (int)ds;
+      } else if (ty == LBM_LINK_ABB) {
+        const int64_t s = L.aux[k];
+        if (s < 0 || s >= nin)
+          return fail(LBM_ERR_ARG, "lbm_create: ABB neighbour out of range at node " + std::to_string(L.node));
+        const long long ds = (long long)(s % ny) * pitch + s / ny;
+        if (recmap[ds] < 0)
+          return fail(LBM_ERR_ARG, "lbm_create: ABB neighbour " + std::to_string(s) +
+                                       " of node " + std::to_string(L.node) + " has no link record");
+        raux[li] = recmap[ds];
+      } else if (ty != LBM_LINK_ZERO && ty != LBM_LINK_BB && ty != LBM_LINK_MBB) {
+        return fail(LBM_ERR_ARG, "lbm_create: unknown link type at node " + std::to_string(L.node));
+      }
+    }
+  }
+  // every bulk node must have in-grid fluid neighbours
+  for (int y = 0; y < ny; ++y)
+    for (int x = 0; x < nx; ++x) {
+      if (cls[(long long)y * pitch + x] != 0) continue;
+      for (int k = 1; k < 9; ++k) {
+        const int xs = x - kCX[k], ys = y - kCY[k];
+        if (xs < 0 || xs >= nx || ys < 0 || ys >= ny || cls[(long long)ys * pitch + xs] == 2)
+          return fail(LBM_ERR_ARG, "lbm_create: node (" + std::to_string(x) + "," +
+                                       std::to_string(y) + ") borders the grid edge or a solid but has no link record");
+      }
+    }
+  const int nseg = (nx + 31) / 32;
+  std::vector<uint8_t> segflag((size_t)ny * nseg, 0);
+  for (int y = 0; y < ny; ++y)
+    for (int x = 0; x < nx; ++x)
+      if (cls[(long long)y * pitch + x]) segflag[(size_t)y * nseg + x / 32] = 1;
+
+  // ---- device --------------------------------------------------------------
+  LbmHandle* h = new LbmHandle();
+  h->cfg = c;
+  h->ks = ks;
+  auto bail = [&](int rc) {
+    delete h;
+    return rc;
+  };
+  if (std::getenv("LBM_FAIL_ALLOC")) return bail(fail(LBM_ERR_ALLOC, "device allocation refused (LBM_FAIL_ALLOC is set)"));
+  cudaError_t e = cudaSetDevice(c.device);
+  if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e)));
+  e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
+
+  lbm::Geom& g = h->g;
+  g.nx = nx;
+  g.ny = ny;
+  g.pitch = pitch;
+  g.nseg = nseg;
+  g.plane = plane;
+  g.nrec = (int)nlinks;
+  const size_t eb = ks->elem_bytes, cb = ks->compute_bytes;
+  const size_t nrec1 = std::max<int64_t>(nlinks, 1);
+  void *d_cls, *d_seg, *d_recmap, *d_rtype, *d_rsrc, *d_rparam, *d_raux;
+  int rc;
+  if ((rc = h->alloc(&d_cls, plane)) || (rc = h->alloc(&d_seg, segflag.size())) ||
+      (rc = h->alloc(&d_recmap, plane * sizeof(int))) || (rc = h->alloc(&d_rtype, 9 * nrec1)) ||
+      (rc = h->alloc(&d_rsrc, 9 * nrec1 * sizeof(int))) ||
+      (rc = h->alloc(&d_rparam, 9 * nrec1 * sizeof(double))) ||
+      (rc = h->alloc(&d_raux, 9 * nrec1 * sizeof(int))) ||
+      (rc = h->alloc(&h->pop[0], 9 * plane * eb)) || (rc = h->alloc(&h->pop[1], 9 * plane * eb)) ||
+      (rc = h->alloc(&h->side[0], 3 * nrec1 * cb)) || (rc = h->alloc(&h->side[1], 3 * nrec1 * cb)))
+    return bail(rc);
+  for (int i = 0; i < 3; ++i)
+    if ((rc = h->alloc(&h->mom[i], plane * cb)) || (rc = h->alloc(&h->old[i], plane * cb)))
+      return bail(rc);
+  h->block = dim3(kBlock);
+  h->grid = dim3((nx + kBlock - 1) / kBlock, ny);
+  h->nparts = (long long)h->grid.x * h->grid.y;
+  if ((rc = h->alloc(reinterpret_cast<void**>(&h->partials), std::max<long long>(h->nparts, ny) * 8 * sizeof(double))) ||
+      (rc = h->alloc(reinterpret_cast<void**>(&h->red), 16 * sizeof(double))))
+    return bail(rc);
+  e = cudaMallocHost(reinterpret_cast<void**>(&h->host_red), 16 * sizeof(double));
+  if (e != cudaSuccess) return bail(fail(LBM_ERR_ALLOC, std::string("cudaMallocHost: ") + cudaGetErrorString(e)));
+  g.cls = (const uint8_t*)d_cls;
+  g.segflag = (const uint8_t*)d_seg;
+  g.recmap = (const int*)d_recmap;
+  g.rtype = (const int8_t*)d_rtype;
+  g.rsrc = (const int*)d_rsrc;
+  g.rparam = (const double*)d_rparam;
+  g.raux = (const int*)d_raux;
+  auto up = [&](void* d, const void* src, size_t bytes) {
+    return cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, h->stream);
+  };
+  if ((e = up(d_cls, cls.data(), plane)) != cudaSuccess ||
+      (e = up(d_seg, segflag.data(), segflag.size())) != cudaSuccess ||
+      (e = up(d_recmap, recmap.data(), plane * sizeof(int))) != cudaSuccess ||
+      (e = up(d_rtype, rtype.data(), rtype.size())) != cudaSuccess ||
+      (e = up(d_rsrc, rsrc.data(), rsrc.size() * sizeof(int))) != cudaSuccess ||
+      (e = up(d_rparam, rparam.data(), rparam.size() * sizeof(double))) != cudaSuccess ||
+      (e = up(d_raux, raux.data(), raux.size() * sizeof(int))) != cudaSuccess)
+    return bail(fail(LBM_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(e)));
+  for (int i = 0; i < 2; ++i) {
+    if ((e = cudaMemsetAsync(h->pop[i], 0, 9 * plane * eb, h->stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(h->side[i], 0, 3 * nrec1 * cb, h->stream)) != cudaSuccess)
+      return bail(fail(LBM_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
+  }
+  for (int i = 0; i < 3; ++i)
+    if ((e = cudaMemsetAsync(h->mom[i], 0, plane * cb, h->stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(h->old[i], 0, plane * cb, h->stream)) != cudaSuccess)
+      return bail(fail(LBM_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
+
+  lbm::Params& p = h->p;
+  p.omega = c.omega;
+  p.one_m_omega = 1 - c.omega;
+  p.one_m_half_omega = 1 - 0.5 * c.omega;
+  const bool fp64 = c.precision == LBM_FP64;
+  p.inv_cs_2 = fp64 ? c.inv_cs_2 : 3.0;
+  p.inv_cs_4 = fp64 ? c.inv_cs_4 : 9.0;
+  p.half_inv_cs_2 = 0.5 * p.inv_cs_2;
+  p.half_inv_cs_4 = 0.5 * p.inv_cs_4;
+  p.eps = c.eps;
+  p.gx = c.forcing ? c.gravity[0] : 0.0;
+  p.gy = c.forcing ? c.gravity[1] : 0.0;
+  p.s_e = c.mrt_s[0];
+  p.s_eps = c.mrt_s[1];
+  p.s_q = c.mrt_s[2];
+  p.s_nu = c.mrt_s[3];
+  p.scale = c.precision == LBM_FP16_SHIFTED ? c.fp16_scale : 1.0;
+  p.inv_scale = 1.0 / p.scale;
+  if (c.body_force_field) {
+    if ((rc = h->alloc(&h->body, 2 * plane * cb))) return bail(rc);
+    if ((e = cudaMemsetAsync(h->body, 0, 2 * plane * cb, h->stream)) != cudaSuccess)
+      return bail(fail(LBM_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
+  }
+  if (const char* to = std::getenv("LBM_SYNC_TIMEOUT_S")) h->timeout_s = std::atof(to);
+  if ((rc = h->wait())) return bail(rc);
+  *out = h;
+  return LBM_OK;
+}
+
+int lbm_destroy(LbmHandle* h) {
+  if (!h) return fail(LBM_ERR_ARG, "lbm_destroy: null handle");
+  cudaSetDevice(h->cfg.device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  delete h;
+  return LBM_OK;
+}
+
+int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout) {
+  if (!h || !rho || !u) return fail(LBM_ERR_ARG, "lbm_init_fields: null argument");
+  if (layout != LBM_LAYOUT_INNER && layout != LBM_LAYOUT_PADDED)
+    return fail(LBM_ERR_ARG, "lbm_init_fields: unknown layout");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  const long long nh = h->host_nodes(layout), plane = h->g.plane;
+  int rc = h->ensure_stage(3 * nh + 3 * plane);
+  if (rc) return rc;
+  double* hs = h->stage;           // host order: rho [nh], u [nh][2]
+  double* ds = h->stage + 3 * nh;  // device order: rho [plane], u [2][plane]
+  LBM_CUDA(cudaMemcpyAsync(hs, rho, nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(hs + nh, u, 2 * nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  LBM_CUDA(cudaMemsetAsync(ds, 0, 3 * plane * sizeof(double), h->stream));
+  LBM_CUDA(lbm::reorder(h->g, hs, ds, 1, layout, 1, h->stream));
+  LBM_CUDA(lbm::reorder(h->g, hs + nh, ds + plane, 2, layout, 1, h->stream));
+  LBM_CUDA(h->ks->init(h->g, h->p, ds, ds + plane, h->pop[h->cur], h->mom[0], h->mom[1],
+                       h->mom[2], h->stream));
+  for (int i = 0; i < 3; ++i)
+    LBM_CUDA(cudaMemsetAsync(h->old[i], 0, plane * h->ks->compute_bytes, h->stream));
+  if ((rc = h->wait())) return rc;
+  h->initialized = true;
+  h->nopull = true;
+  h->has_moments = true;
+  h->has_residual = false;
+  h->t = 0;
+  return LBM_OK;
+}
+
+int lbm_set_body_force(LbmHandle* h, const double* force) {
+  if (!h || !force) return fail(LBM_ERR_ARG, "lbm_set_body_force: null argument");
+  if (!h->body) return fail(LBM_ERR_STATE, "lbm_set_body_force: case was created without body_force_field");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  const long long nh = h->host_nodes(LBM_LAYOUT_INNER), plane = h->g.plane;
+  int rc = h->ensure_stage(2 * nh + 2 * plane);
+  if (rc) return rc;
+  double* hs = h->stage;
+  double* ds = h->stage + 2 * nh;
+  LBM_CUDA(cudaMemcpyAsync(hs, force, 2 * nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  LBM_CUDA(cudaMemsetAsync(ds, 0, 2 * plane * sizeof(double), h->stream));
+  LBM_CUDA(lbm::reorder(h->g, hs, ds, 2, LBM_LAYOUT_INNER, 1, h->stream));
+  LBM_CUDA(h->ks->body_from_f64(h->g, ds, h->body, h->stream));
+  return h->wait();
+}
+
+int lbm_step_ex(LbmHandle* h, int64_t nsteps, int flags) {
+  if (!h) return fail(LBM_ERR_ARG, "lbm_step: null handle");
+  if (nsteps < 0) return fail(LBM_ERR_ARG, "lbm_step: nsteps < 0");
+  if (flags & ~(LBM_STEP_MOMENTS | LBM_STEP_RESIDUAL)) return fail(LBM_ERR_ARG, "lbm_step: unknown flags");
+  if (!h->initialized) return fail(LBM_ERR_STATE, "lbm_step: call lbm_init_fields or lbm_set_populations first");
+  if (nsteps == 0) return LBM_OK;
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  int kflags = (flags & LBM_STEP_MOMENTS ? lbm::F_MOMENTS : 0) |
+               (flags & LBM_STEP_RESIDUAL ? lbm::F_RESIDUAL : 0);
+  int64_t s = 0;
+  int rc;
+  auto one = [&](int fl) {
+    int r = h->launch(fl);
+    if (r) return r;
+    h->nopull = false;
+    h->t += 1;
+    h->launches += 1;
+    return LBM_OK;
+  };
+  if (h->nopull) {
+    if ((rc = one(lbm::F_NOPULL | (nsteps == 1 ? kflags : 0)))) return rc;
+    s = 1;
+  }
+  int64_t plain = nsteps - s - (s < nsteps ? 1 : 0);
+  while (plain > 0) {
+    if (plain >= kGraphChunk && !std::getenv("LBM_NO_GRAPH")) {
+      if (!h->gexec && (rc = h->capture_graph())) return rc;
+      if (h->cur == h->gparity) {
+        LBM_CUDA(cudaGraphLaunch(h->gexec, h->stream));
+        h->t += kGraphChunk;
+        h->launches += kGraphChunk;
+        plain -= kGraphChunk;
+        continue;
+      }
+    }
+    if ((rc = one(0))) return rc;
+    --plain;
+  }
+  if (s < nsteps) {
+    if ((rc = one(kflags))) return rc;
+  }
+  if (flags & LBM_STEP_MOMENTS) h->has_moments = true;
+  if (flags & LBM_STEP_RESIDUAL) {
+    LBM_CUDA(lbm::finish_reduce(h->partials, h->nparts, h->red, h->stream));
+    LBM_CUDA(cudaMemcpyAsync(h->host_red, h->red, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    h->has_residual = true;
+  }
+  return LBM_OK;
+}
+
+int lbm_step(LbmHandle* h, int64_t nsteps) { return lbm_step_ex(h, nsteps, 0); }
+
+int lbm_get_moments(LbmHandle* h, double* rho, double* u, int layout) {
+  if (!h || !rho || !u) return fail(LBM_ERR_ARG, "lbm_get_moments: null argument");
+  if (layout != LBM_LAYOUT_INNER && layout != LBM_LAYOUT_PADDED)
+    return fail(LBM_ERR_ARG, "lbm_get_moments: unknown layout");
+  if (!h->has_moments) return fail(LBM_ERR_STATE, "lbm_get_moments: no moments recorded (use LBM_STEP_MOMENTS)");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  const long long nh = h->host_nodes(layout), plane = h->g.plane;
+  int rc = h->ensure_stage(3 * nh + 3 * plane);
+  if (rc) return rc;
+  double* hs = h->stage;
+  double* ds = h->stage + 3 * nh;
+  LBM_CUDA(h->ks->moments_to_f64(h->g, h->mom[0], h->mom[1], h->mom[2], ds, h->stream));
+  LBM_CUDA(cudaMemsetAsync(hs, 0, 3 * nh * sizeof(double), h->stream));
+  LBM_CUDA(lbm::reorder(h->g, ds, hs, 1, layout, 0, h->stream));
+  LBM_CUDA(lbm::reorder(h->g, ds + plane, hs + nh, 2, layout, 0, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(rho, hs, nh * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(u, hs + nh, 2 * nh * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return h->wait();
+}
+
+int lbm_residual(LbmHandle* h, double out[3]) {
+  if (!h || !out) return fail(LBM_ERR_ARG, "lbm_residual: null argument");
+  if (!h->has_residual) return fail(LBM_ERR_STATE, "lbm_residual: no residual step recorded (use LBM_STEP_RESIDUAL)");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  int rc = h->wait();
+  if (rc) return rc;
+  const double* s = h->host_red;
+  for (int c = 0; c < 3; ++c) out[c] = std::sqrt(s[2 * c] / (s[2 * c + 1] + h->cfg.eps));
+  if (s[6] > 0)
+    return fail(LBM_ERR_NONFINITE, "lbm_residual: " + std::to_string((long long)s[6]) +
+                                       " fluid nodes have non-finite density or velocity");
+  return LBM_OK;
+}
+
+int lbm_conservation(LbmHandle* h, double out[3]) {
+  if (!h || !out) return fail(LBM_ERR_ARG, "lbm_conservation: null argument");
+  if (!h->initialized) return fail(LBM_ERR_STATE, "lbm_conservation: not initialised");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  LBM_CUDA(h->ks->conservation(h->g, h->p, h->pop[h->cur], h->partials, h->stream));
+  LBM_CUDA(lbm::finish_reduce(h->partials, h->g.ny, h->red + 8, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(h->host_red + 8, h->red + 8, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  int rc = h->wait();
+  if (rc) return rc;
+  for (int c = 0; c < 3; ++c) out[c] = h->host_red[8 + c];
+  // the residual partial sums were overwritten; the host copy stays valid
+  return LBM_OK;
+}
+
+int lbm_get_populations(LbmHandle* h, double* pop) {
+  if (!h || !pop) return fail(LBM_ERR_ARG, "lbm_get_populations: null argument");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  const long long nh = h->host_nodes(LBM_LAYOUT_PADDED), plane = h->g.plane;
+  int rc = h->ensure_stage(9 * nh + 9 * plane);
+  if (rc) return rc;
+  double* hs = h->stage;
+  double* ds = h->stage + 9 * nh;
+  LBM_CUDA(h->ks->convert(h->g, h->p, h->pop[h->cur], ds, 0, h->stream));
+  LBM_CUDA(cudaMemsetAsync(hs, 0, 9 * nh * sizeof(double), h->stream));
+  LBM_CUDA(lbm::reorder(h->g, ds, hs, 9, LBM_LAYOUT_PADDED, 0, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(pop, hs, 9 * nh * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return h->wait();
+}
+
+int lbm_set_populations(LbmHandle* h, const double* pop_new) {
+  if (!h || !pop_new) return fail(LBM_ERR_ARG, "lbm_set_populations: null argument");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  const long long nh = h->host_nodes(LBM_LAYOUT_PADDED), plane = h->g.plane;
+  int rc = h->ensure_stage(9 * nh + 9 * plane);
+  if (rc) return rc;
+  double* hs = h->stage;
+  double* ds = h->stage + 9 * nh;
+  LBM_CUDA(cudaMemcpyAsync(hs, pop_new, 9 * nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  LBM_CUDA(cudaMemsetAsync(ds, 0, 9 * plane * sizeof(double), h->stream));
+  LBM_CUDA(lbm::reorder(h->g, hs, ds, 9, LBM_LAYOUT_PADDED, 1, h->stream));
+  LBM_CUDA(h->ks->convert(h->g, h->p, h->pop[h->cur], ds, 1, h->stream));
+  if ((rc = h->wait())) return rc;
+  h->initialized = true;
+  h->nopull = true;
+  return LBM_OK;
+}
+
+int lbm_time(LbmHandle* h, int64_t* t) {
+  if (!h || !t) return fail(LBM_ERR_ARG, "lbm_time: null argument");
+  *t = h->t;
+  return LBM_OK;
+}
+
+int lbm_kernel_launches(LbmHandle* h, int64_t* n) {
+  if (!h || !n) return fail(LBM_ERR_ARG, "lbm_kernel_launches: null argument");
+  *n = h->launches;
+  return LBM_OK;
+}
+
+int lbm_device_bytes(LbmHandle* h, int64_t* bytes) {
+  if (!h || !bytes) return fail(LBM_ERR_ARG, "lbm_device_bytes: null argument");
+  *bytes = (int64_t)h->dev_bytes;
+  return LBM_OK;
+}
+
+int lbm_time_steps(LbmHandle* h, int64_t nsteps, double* ms) {
+  if (!h || !ms) return fail(LBM_ERR_ARG, "lbm_time_steps: null argument");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  cudaEvent_t e0, e1;
+  LBM_CUDA(cudaEventCreate(&e0));
+  LBM_CUDA(cudaEventCreate(&e1));
+  int rc = LBM_OK;
+  cudaError_t e = cudaEventRecord(e0, h->stream);
+  if (e == cudaSuccess) {
+    rc = lbm_step(h, nsteps);
+    if (rc == LBM_OK) e = cudaEventRecord(e1, h->stream);
+  }
+  if (rc == LBM_OK && e == cudaSuccess) rc = h->wait();
+  float f = 0.f;
+  if (rc == LBM_OK && e == cudaSuccess) e = cudaEventElapsedTime(&f, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("events: ") + cudaGetErrorString(e));
+  *ms = f;
+  return LBM_OK;
+}
+
+int lbm_synchronize(LbmHandle* h, double timeout_s) {
+  if (!h) return fail(LBM_ERR_ARG, "lbm_synchronize: null handle");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  const double keep = h->timeout_s;
+  if (timeout_s > 0) h->timeout_s = timeout_s;
+  int rc = h->wait();
+  h->timeout_s = keep;
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,93 @@
+// Internal interface between the C-ABI layer (lbm_capi.cu) and the kernel
+// translation units (lbm_fp64.cu: FP64, built with --fmad=false so it keeps
+// the reference's rounding; lbm_lowp.cu: FP32 / FP16 shifted storage).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lbm {
+
+// Device-side geometry of one case.  Populations are SoA planes
+// [q][ny][pitch] (x fastest), node index n = y*pitch + x.
+struct Geom {
+  int nx, ny, pitch, nseg;   // nseg = ceil(nx/32) warp segments per row
+  long long plane;           // elements per population plane = ny*pitch
+  const uint8_t* cls;        // [plane] node class: 0 bulk, 1 special, 2 solid
+  const uint8_t* segflag;    // [ny*nseg] 0: all 32 nodes of the segment bulk
+  const int* recmap;         // [plane] record index of special nodes
+  int nrec;
+  const int8_t* rtype;       // [nrec*9] link kind
+  const int* rsrc;           // [nrec*9] PULL source node (device index)
+  const double* rparam;      // [nrec*9]
+  const int* raux;           // [nrec*9] ABB: record index of node x+n
+};
+
+struct Params {
+  double omega, one_m_omega, one_m_half_omega;
+  double inv_cs_2, inv_cs_4, half_inv_cs_2, half_inv_cs_4, eps;
+  double gx, gy;
+  double s_e, s_eps, s_q, s_nu;
+  double scale, inv_scale;   // FP16 storage scale
+};
+
+enum StepFlags {
+  F_NOPULL = 1,      // populations in `fin` already are the incoming ones
+  F_MOMENTS = 2,     // write rho/ux/uy
+  F_RESIDUAL = 4,    // residual sums against *_old, then *_old <- new
+};
+
+// Arguments of one fused step launch.  `void*` arrays are typed by the
+// instantiation: populations in storage type, the rest in compute type.
+struct StepArgs {
+  Geom g;
+  Params p;
+  const void* fin;
+  void* fout;
+  const void* side_in;   // [nrec*3] rho, ux, uy of the previous step
+  void* side_out;
+  void* rho; void* ux; void* uy;            // [plane] moments
+  void* rho_old; void* ux_old; void* uy_old;
+  double* partials;      // [nblocks*8] residual partial sums
+  const void* body;      // [2*plane] body force or null
+  int flags;
+};
+
+// Kernels of one storage precision.
+struct KernelSet {
+  int elem_bytes;        // storage bytes per population value
+  int compute_bytes;     // bytes per moment value
+  cudaError_t (*step)(int collision, int forcing, const StepArgs& a, dim3 grid,
+                      dim3 block, cudaStream_t s);
+  // f_eq(rho,u) into storage on fluid nodes (zeros on solids); moments get
+  // rho/u on every node.  rho [plane], u [2][plane], FP64, device order.
+  cudaError_t (*init)(const Geom& g, const Params& p, const double* rho,
+                      const double* u, void* f, void* mr, void* mx, void* my,
+                      cudaStream_t s);
+  // storage <-> FP64 [9][plane] (dir 0: to FP64, 1: from FP64); solids 0.
+  cudaError_t (*convert)(const Geom& g, const Params& p, void* f, double* f64,
+                         int dir, cudaStream_t s);
+  // moments (compute type) -> FP64 [3][plane]
+  cudaError_t (*moments_to_f64)(const Geom& g, const void* mr, const void* mx,
+                                const void* my, double* out, cudaStream_t s);
+  // FP64 [2][plane] -> compute type [2][plane]
+  cudaError_t (*body_from_f64)(const Geom& g, const double* in, void* out,
+                               cudaStream_t s);
+  // partial sums {sum f, sum cx f, sum cy f} per block row -> partials[ny][8]
+  cudaError_t (*conservation)(const Geom& g, const Params& p, const void* f,
+                              double* partials, cudaStream_t s);
+};
+
+const KernelSet& kernels_fp64();
+const KernelSet& kernels_fp32();
+const KernelSet& kernels_fp16();
+
+// Deterministic reduction of `nrows` rows of 8 doubles into out8 (fixed order).
+cudaError_t finish_reduce(const double* partials, long long nrows, double* out8,
+                          cudaStream_t s);
+// Host-order <-> device-order copies of FP64 node data with `ncomp`
+// components: host AoS [node][ncomp] in inner (ind = x*ny+y) or padded
+// (ind = (x+1)*(ny+2)+(y+1)) order; device SoA [ncomp][plane].
+cudaError_t reorder(const Geom& g, const double* in, double* out, int ncomp,
+                    int layout, int to_device, cudaStream_t s);
+
+}  // namespace lbm

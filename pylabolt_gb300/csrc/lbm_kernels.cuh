@@ -1,0 +1,480 @@
+// Fused D2Q9 fluidLB step for sm_103a: pull-stream + boundary links + moments
+// + (BGK | MRT) collision with (none | Guo linear | Guo second order) forcing,
+// optional moment output and FP64 residual partial sums, in one launch.
+//
+// One launch of step_kernel advances the device state from the post-collision
+// populations of step t-1 to those of step t.  Relative to the reference's
+// Solver.single_time_step (pylabolt/solvers/fluidLB.py:206-253) it performs
+// [stream + boundaries of step t-1] followed by [density, force, velocity,
+// collide of step t]; the moments it computes are the ones the reference holds
+// after step t.  Boundary rules that read moments of step t-1 (moving walls,
+// moving solids, anti-bounce-back) read them from a small side array that the
+// previous launch wrote for every boundary ("special") node.
+//
+// Storage:
+//   double : f in FP64; arithmetic follows the reference kernels' operation
+//            order literally (compile this instantiation with --fmad=false) so
+//            results are bit-identical to the reference CPU kernels.
+//   float  : g = f - w_i in FP32, FP32 arithmetic (shifted populations).
+//   __half : g * scale in FP16, FP32 arithmetic.
+#pragma once
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "lbm_internal.h"
+
+namespace lbm {
+
+__host__ __device__ constexpr int CXk(int k) {
+  return (k == 1 || k == 5 || k == 8) ? 1 : ((k == 3 || k == 6 || k == 7) ? -1 : 0);
+}
+__host__ __device__ constexpr int CYk(int k) {
+  return (k == 2 || k == 5 || k == 6) ? 1 : ((k == 4 || k == 7 || k == 8) ? -1 : 0);
+}
+__host__ __device__ constexpr int INVk(int k) {
+  return k == 0 ? 0 : (k <= 4 ? ((k + 1) % 4) + 1 : ((k - 3) % 4) + 5);
+}
+// D2Q9 weights 4/9, 1/9, 1/36 (FP64 values of pylabolt/base/lattice.py:54-57)
+__host__ __device__ constexpr double Wk(int k) {
+  return k == 0 ? 4.0 / 9.0 : (k <= 4 ? 1.0 / 9.0 : 1.0 / 36.0);
+}
+static_assert(INVk(1) == 3 && INVk(2) == 4 && INVk(3) == 1 && INVk(4) == 2 &&
+                  INVk(5) == 7 && INVk(6) == 8 && INVk(7) == 5 && INVk(8) == 6,
+              "inverse directions");
+
+enum : int { LINK_PULL = 0, LINK_ZERO = 1, LINK_BB = 2, LINK_MBB = 3, LINK_ABB = 4 };
+
+// A*x + B*y for A,B in {-1,0,1}, IEEE-identical to the reference's
+// float(A)*x + float(B)*y: a zero coefficient contributes a signed zero that
+// does not change a non-zero sum, +-1 products are exact.
+template <int A, int B, class T>
+__device__ __forceinline__ T lin2(T x, T y) {
+  if (A == 0 && B == 0) return T(0);
+  if (A == 0) return B > 0 ? y : -y;
+  if (B == 0) return A > 0 ? x : -x;
+  T ax = A > 0 ? x : -x;
+  return B > 0 ? ax + y : ax - y;
+}
+
+// ---------------------------------------------------------------------------
+// storage traits
+template <class S> struct Store;
+template <> struct Store<double> {
+  using T = double;
+  static constexpr bool shifted = false;
+  __device__ static __forceinline__ T ld(const double* __restrict__ p, long long i, const Params&) {
+    return p[i];
+  }
+  __device__ static __forceinline__ void st(double* __restrict__ p, long long i, T v, const Params&) {
+    p[i] = v;
+  }
+};
+template <> struct Store<float> {
+  using T = float;
+  static constexpr bool shifted = true;
+  __device__ static __forceinline__ T ld(const float* __restrict__ p, long long i, const Params&) {
+    return p[i];
+  }
+  __device__ static __forceinline__ void st(float* __restrict__ p, long long i, T v, const Params&) {
+    p[i] = v;
+  }
+};
+template <> struct Store<__half> {
+  using T = float;
+  static constexpr bool shifted = true;
+  __device__ static __forceinline__ T ld(const __half* __restrict__ p, long long i, const Params& q) {
+    return __half2float(p[i]) * float(q.inv_scale);
+  }
+  __device__ static __forceinline__ void st(__half* __restrict__ p, long long i, T v, const Params& q) {
+    p[i] = __float2half_rn(v * float(q.scale));
+  }
+};
+
+// ---------------------------------------------------------------------------
+// FP64, reference operation order (collision_kernels.py:5-153,
+// compute_fields_kernels.py:5-65, force_field_kernels.py:5-25).
+template <int K, int FORC>
+__device__ __forceinline__ double bgk_ref_k(double fk, double rho, double ux,
+                                            double uy, double hu2, double Fx,
+                                            double Fy, const Params& p) {
+  constexpr int cx = CXk(K), cy = CYk(K);
+  const double cu = lin2<cx, cy>(ux, uy);
+  double e;
+  if (cx == 0 && cy == 0)
+    e = 1.0 - hu2;
+  else
+    e = ((1.0 + p.inv_cs_2 * cu) + (p.half_inv_cs_4 * cu) * cu) - hu2;
+  const double pop_eq = (Wk(K) * rho) * e;
+  double out = p.one_m_omega * fk + p.omega * pop_eq;
+  if (FORC == 1) {
+    if (cx != 0 || cy != 0) {
+      const double ft = (Wk(K) * lin2<cx, cy>(Fx, Fy)) * p.inv_cs_2;
+      out = out + p.one_m_half_omega * ft;
+    }
+  } else if (FORC == 2) {
+    double const_x, const_y;
+    if (cx == 0)
+      const_x = (-ux) * p.inv_cs_2;
+    else
+      const_x = (double(cx) - ux) * p.inv_cs_2 + (cx > 0 ? cu : -cu) * p.inv_cs_4;
+    if (cy == 0)
+      const_y = (-uy) * p.inv_cs_2;
+    else
+      const_y = (double(cy) - uy) * p.inv_cs_2 + (cy > 0 ? cu : -cu) * p.inv_cs_4;
+    const double ft = Wk(K) * (const_x * Fx + const_y * Fy);
+    out = out + p.one_m_half_omega * ft;
+  }
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+// Moments.  FP64: reference order.  Shifted: deviation sums.
+template <bool SHIFTED, class T>
+__device__ __forceinline__ void moments(const T f[9], T& rho, T& drho, T& jx,
+                                        T& jy) {
+  if (!SHIFTED) {
+    T s = f[0];
+#pragma unroll
+    for (int k = 1; k < 9; ++k) s = s + f[k];
+    rho = s;
+    drho = s;
+    jx = ((((f[1] - f[3]) + f[5]) - f[6]) - f[7]) + f[8];
+    jy = ((((f[2] - f[4]) + f[5]) + f[6]) - f[7]) - f[8];
+  } else {
+    drho = ((f[0] + (f[1] + f[3])) + (f[2] + f[4])) + ((f[5] + f[7]) + (f[6] + f[8]));
+    rho = T(1) + drho;
+    jx = ((f[1] - f[3]) + (f[5] - f[7])) + (f[8] - f[6]);
+    jy = ((f[2] - f[4]) + (f[5] - f[7])) + (f[6] - f[8]);
+  }
+}
+
+// Shifted BGK: g* = g + omega (g_eq - g) + (1 - omega/2) Fbar, with
+// g_eq = w (drho + rho (3 cu + 4.5 cu^2 - 1.5 u^2)).
+template <int K, int FORC, class T>
+__device__ __forceinline__ T bgk_shift_k(T gk, T rho, T drho, T ux, T uy,
+                                         T u2, T Fx, T Fy, T omega, T omh) {
+  constexpr int cx = CXk(K), cy = CYk(K);
+  const T w = T(Wk(K));
+  const T cu = lin2<cx, cy>(ux, uy);
+  const T geq = w * (drho + rho * (T(3) * cu + T(4.5) * cu * cu - T(1.5) * u2));
+  T out = gk + omega * (geq - gk);
+  if (FORC == 1) {
+    if (cx != 0 || cy != 0) out += omh * (w * T(3) * lin2<cx, cy>(Fx, Fy));
+  } else if (FORC == 2) {
+    const T ex = (T(cx) - ux) * T(3) + T(9) * cu * T(cx);
+    const T ey = (T(cy) - uy) * T(3) + T(9) * cu * T(cy);
+    out += omh * (w * (ex * Fx + ey * Fy));
+  }
+  return out;
+}
+
+// MRT (project definition; the reference declares MRT without a kernel,
+// pylabolt/base/collision_operator.py:136-165).  Moment basis M of
+// collision_operator.py:147-157, S = diag(1, s_e, s_eps, 1, s_q, 1, s_q, s_nu,
+// s_nu), equilibrium moments M f_eq and Guo source moments M Fbar in closed form
+// for general inv_cs_2 (i2) / inv_cs_4 (i4).  Works on f (FP64) or on
+// g = f - w (shifted; M w = (1,-2,1,0,...)).
+template <int FORC, bool SHIFTED, class T>
+__device__ __forceinline__ void mrt_collide(T f[9], T rho, T drho, T ux, T uy,
+                                            T Fx, T Fy, const Params& p) {
+  const T i2 = T(p.inv_cs_2), i4 = T(p.inv_cs_4);
+  const T s_e = T(p.s_e), s_eps = T(p.s_eps), s_q = T(p.s_q), s_nu = T(p.s_nu);
+  const T a14 = f[1] + f[2] + f[3] + f[4];
+  const T a58 = f[5] + f[6] + f[7] + f[8];
+  T m[9];
+  m[0] = f[0] + a14 + a58;
+  m[1] = T(-4) * f[0] - a14 + T(2) * a58;
+  m[2] = T(4) * f[0] - T(2) * a14 + a58;
+  m[3] = f[1] - f[3] + f[5] - f[6] - f[7] + f[8];
+  m[4] = T(-2) * f[1] + T(2) * f[3] + f[5] - f[6] - f[7] + f[8];
+  m[5] = f[2] - f[4] + f[5] + f[6] - f[7] - f[8];
+  m[6] = T(-2) * f[2] + T(2) * f[4] + f[5] + f[6] - f[7] - f[8];
+  m[7] = f[1] - f[2] + f[3] - f[4];
+  m[8] = f[5] - f[6] + f[7] - f[8];
+  const T u2 = ux * ux + uy * uy;
+  const T third_i2 = i2 / T(3), ninth_i4 = i4 / T(9);
+  T meq[9];
+  // equilibrium moments; shifted form subtracts M w = (1, -2, 1, 0, ...)
+  meq[0] = rho - rho * ((T(3) * i2 - i4) / T(6)) * u2 - (SHIFTED ? T(1) : T(0));
+  meq[1] = SHIFTED ? (T(-2) * drho + rho * i2 * u2) : rho * (i2 * u2 - T(2));
+  meq[2] = SHIFTED ? (drho - rho * ((T(3) * i2 + i4) / T(6)) * u2)
+                   : rho - rho * ((T(3) * i2 + i4) / T(6)) * u2;
+  meq[3] = third_i2 * rho * ux;
+  meq[4] = -meq[3];
+  meq[5] = third_i2 * rho * uy;
+  meq[6] = -meq[5];
+  meq[7] = ninth_i4 * rho * (ux * ux - uy * uy);
+  meq[8] = ninth_i4 * rho * ux * uy;
+  T mf[9] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+  if (FORC != 0) {
+    mf[3] = third_i2 * Fx;
+    mf[4] = -mf[3];
+    mf[5] = third_i2 * Fy;
+    mf[6] = -mf[5];
+  }
+  if (FORC == 2) {
+    const T uF = Fx * ux + Fy * uy;
+    mf[0] = -((T(3) * i2 - i4) / T(3)) * uF;
+    mf[1] = T(2) * i2 * uF;
+    mf[2] = -((T(3) * i2 + i4) / T(3)) * uF;
+    mf[7] = T(2) * ninth_i4 * (Fx * ux - Fy * uy);
+    mf[8] = ninth_i4 * (Fx * uy + Fy * ux);
+  }
+  const T S[9] = {T(1), s_e, s_eps, T(1), s_q, T(1), s_q, s_nu, s_nu};
+  T a[9];
+  const T inv_norm[9] = {T(1) / T(9), T(1) / T(36), T(1) / T(36), T(1) / T(6),
+                         T(1) / T(12), T(1) / T(6), T(1) / T(12), T(1) / T(4),
+                         T(1) / T(4)};
+#pragma unroll
+  for (int i = 0; i < 9; ++i)
+    a[i] = (m[i] - S[i] * (m[i] - meq[i]) + (T(1) - T(0.5) * S[i]) * mf[i]) * inv_norm[i];
+  // f = M^T diag(1/|row|^2) m*
+  const T b = a[0] - a[1] - T(2) * a[2];
+  const T c = a[0] + T(2) * a[1] + a[2];
+  f[0] = a[0] - T(4) * a[1] + T(4) * a[2];
+  f[1] = b + a[3] - T(2) * a[4] + a[7];
+  f[2] = b + a[5] - T(2) * a[6] - a[7];
+  f[3] = b - a[3] + T(2) * a[4] + a[7];
+  f[4] = b - a[5] + T(2) * a[6] - a[7];
+  f[5] = c + a[3] + a[4] + a[5] + a[6] + a[8];
+  f[6] = c - a[3] - a[4] + a[5] + a[6] - a[8];
+  f[7] = c - a[3] - a[4] - a[5] - a[6] + a[8];
+  f[8] = c + a[3] + a[4] - a[5] - a[6] - a[8];
+}
+
+// ---------------------------------------------------------------------------
+// Incoming population of direction K at a boundary node (record r).
+template <int K, class S>
+__device__ __forceinline__ typename Store<S>::T special_link(
+    const Geom& g, const Params& p, const S* __restrict__ fin, long long n, int r,
+    const typename Store<S>::T* __restrict__ side) {
+  using T = typename Store<S>::T;
+  constexpr bool SH = Store<S>::shifted;
+  constexpr int KB = INVk(K);
+  const int li = r * 9 + K;
+  const int type = g.rtype[li];
+  if (type == LINK_PULL) return Store<S>::ld(fin, K * g.plane + g.rsrc[li], p);
+  if (type == LINK_ZERO) return SH ? T(-Wk(K)) : T(0);
+  const T raw = Store<S>::ld(fin, KB * g.plane + n, p);
+  if (type == LINK_BB) return raw;
+  if (type == LINK_MBB) {
+    // streaming_kernels.py:41-47 / fluid_boundary_kernels.py:54-62:
+    // raw - 2 w rho inv_cs_2 (c_kbar . u)
+    const T rho = side[3 * r];
+    if (!SH)
+      return raw - ((T(2.0 * Wk(KB)) * rho) * T(p.inv_cs_2)) * T(g.rparam[li]);
+    return raw - (T(2.0 * Wk(KB)) * rho * T(3)) * T(g.rparam[li]);
+  }
+  // LINK_ABB -- fluid_boundary_kernels.py:100-152
+  const int ra = g.raux[li];
+  const T ux = side[3 * r + 1], uy = side[3 * r + 2];
+  const T uex = ux + T(0.5) * (ux - side[3 * ra + 1]);
+  const T uey = uy + T(0.5) * (uy - side[3 * ra + 2]);
+  const T u2 = uex * uex + uey * uey;
+  const T cu = lin2<CXk(KB), CYk(KB)>(uex, uey);
+  const T rho_w = T(g.rparam[li]);
+  if (!SH) {
+    const T temp = (T(2.0 * Wk(KB)) * rho_w) *
+                   ((T(1) + (T(p.half_inv_cs_4) * cu) * cu) - T(p.half_inv_cs_2) * u2);
+    return -raw + temp;
+  }
+  return -raw + T(2.0 * Wk(KB)) *
+                    ((rho_w - T(1)) + rho_w * (T(4.5) * cu * cu - T(1.5) * u2));
+}
+
+template <class T>
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+template <class S, int COLL, int FORC>
+__global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
+  using T = typename Store<S>::T;
+  constexpr bool SH = Store<S>::shifted;
+  const Geom& g = a.g;
+  const Params& p = a.p;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  double red[7] = {0, 0, 0, 0, 0, 0, 0};
+
+  if (x < g.nx) {
+    const long long n = (long long)y * g.pitch + x;
+    const S* __restrict__ fin = static_cast<const S*>(a.fin);
+    S* __restrict__ fout = static_cast<S*>(a.fout);
+    int cls = 0;
+    if (g.segflag[y * g.nseg + (x >> 5)]) cls = g.cls[n];
+    if (cls != 2) {
+      T f[9];
+      int r = -1;
+      if (cls == 1) r = g.recmap[n];
+      if (a.flags & F_NOPULL) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) f[k] = Store<S>::ld(fin, k * g.plane + n, p);
+      } else if (cls == 0) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+          f[k] = Store<S>::ld(fin, k * g.plane + n - CYk(k) * g.pitch - CXk(k), p);
+      } else {
+        const T* side = static_cast<const T*>(a.side_in);
+        f[0] = Store<S>::ld(fin, n, p);
+        f[1] = special_link<1, S>(g, p, fin, n, r, side);
+        f[2] = special_link<2, S>(g, p, fin, n, r, side);
+        f[3] = special_link<3, S>(g, p, fin, n, r, side);
+        f[4] = special_link<4, S>(g, p, fin, n, r, side);
+        f[5] = special_link<5, S>(g, p, fin, n, r, side);
+        f[6] = special_link<6, S>(g, p, fin, n, r, side);
+        f[7] = special_link<7, S>(g, p, fin, n, r, side);
+        f[8] = special_link<8, S>(g, p, fin, n, r, side);
+      }
+
+      T rho, drho, jx, jy;
+      moments<SH>(f, rho, drho, jx, jy);
+      T Fx = T(0), Fy = T(0);
+      if (FORC != 0) {
+        if (a.body) {
+          const T* body = static_cast<const T*>(a.body);
+          Fx = body[n];
+          Fy = body[g.plane + n];
+        } else {
+          Fx = rho * T(p.gx);
+          Fy = rho * T(p.gy);
+        }
+      }
+      T ux, uy;
+      if (!SH) {
+        // compute_fields_kernels.py:61-65
+        const T inv_density = T(1) / (rho + T(p.eps));
+        ux = jx * inv_density + (T(0.5) * Fx) * inv_density;
+        uy = jy * inv_density + (T(0.5) * Fy) * inv_density;
+      } else {
+        const T inv_density = T(1) / rho;
+        ux = (jx + T(0.5) * Fx) * inv_density;
+        uy = (jy + T(0.5) * Fy) * inv_density;
+      }
+
+      if (COLL == 1) {
+        mrt_collide<FORC, SH>(f, rho, drho, ux, uy, Fx, Fy, p);
+      } else if (!SH) {
+        const T hu2 = T(p.half_inv_cs_2) * (ux * ux + uy * uy);
+        f[0] = bgk_ref_k<0, FORC>(f[0], rho, ux, uy, hu2, Fx, Fy, p);
+        f[1] = bgk_ref_k<1, FORC>(f[1], rho, ux, uy, hu2, Fx, Fy, p);
+        f[2] = bgk_ref_k<2, FORC>(f[2], rho, ux, uy, hu2, Fx, Fy, p);
+        f[3] = bgk_ref_k<3, FORC>(f[3], rho, ux, uy, hu2, Fx, Fy, p);
+        f[4] = bgk_ref_k<4, FORC>(f[4], rho, ux, uy, hu2, Fx, Fy, p);
+        f[5] = bgk_ref_k<5, FORC>(f[5], rho, ux, uy, hu2, Fx, Fy, p);
+        f[6] = bgk_ref_k<6, FORC>(f[6], rho, ux, uy, hu2, Fx, Fy, p);
+        f[7] = bgk_ref_k<7, FORC>(f[7], rho, ux, uy, hu2, Fx, Fy, p);
+        f[8] = bgk_ref_k<8, FORC>(f[8], rho, ux, uy, hu2, Fx, Fy, p);
+      } else {
+        const T u2 = ux * ux + uy * uy;
+        const T om = T(p.omega), omh = T(p.one_m_half_omega);
+        f[0] = bgk_shift_k<0, FORC>(f[0], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+        f[1] = bgk_shift_k<1, FORC>(f[1], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+        f[2] = bgk_shift_k<2, FORC>(f[2], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+        f[3] = bgk_shift_k<3, FORC>(f[3], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+        f[4] = bgk_shift_k<4, FORC>(f[4], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+        f[5] = bgk_shift_k<5, FORC>(f[5], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+        f[6] = bgk_shift_k<6, FORC>(f[6], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+        f[7] = bgk_shift_k<7, FORC>(f[7], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+        f[8] = bgk_shift_k<8, FORC>(f[8], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+      }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Store<S>::st(fout, k * g.plane + n, f[k], p);
+
+      if (r >= 0) {
+        T* side = static_cast<T*>(a.side_out);
+        side[3 * r] = rho;
+        side[3 * r + 1] = ux;
+        side[3 * r + 2] = uy;
+      }
+      if (a.flags & F_MOMENTS) {
+        static_cast<T*>(a.rho)[n] = rho;
+        static_cast<T*>(a.ux)[n] = ux;
+        static_cast<T*>(a.uy)[n] = uy;
+      }
+      if (a.flags & F_RESIDUAL) {
+        // compute_residues_kernels.py:6-73: sums over fluid nodes
+        T* ro = static_cast<T*>(a.rho_old);
+        T* xo = static_cast<T*>(a.ux_old);
+        T* yo = static_cast<T*>(a.uy_old);
+        const double v[3] = {double(rho), double(ux), double(uy)};
+        const double o[3] = {double(ro[n]), double(xo[n]), double(yo[n])};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const double d = v[c] - o[c];
+          red[2 * c] = d * d;
+          red[2 * c + 1] = o[c] * o[c];
+        }
+        red[6] = (isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2])) ? 0.0 : 1.0;
+        ro[n] = rho;
+        xo[n] = ux;
+        yo[n] = uy;
+      }
+    }
+  }
+
+  if (a.flags & F_RESIDUAL) {
+    __shared__ double sh[8][8];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+      const double v = warp_sum<double>(red[i]);
+      if (lane == 0) sh[wid][i] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 7) {
+      double s = 0;
+      const int nw = blockDim.x >> 5;
+      for (int w = 0; w < nw; ++w) s += sh[w][threadIdx.x];
+      a.partials[((long long)blockIdx.y * gridDim.x + blockIdx.x) * 8 + threadIdx.x] = s;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Initial equilibrium -- equilibrium_kernels.py:38-78.  rho/u are FP64 device
+// arrays in device order; moments (compute type) receive rho/u on every node.
+template <class S>
+__global__ void init_kernel(const Geom g, const Params p, const double* __restrict__ rho,
+                            const double* __restrict__ u, S* __restrict__ f,
+                            typename Store<S>::T* mr, typename Store<S>::T* mx,
+                            typename Store<S>::T* my) {
+  using T = typename Store<S>::T;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= g.nx) return;
+  const long long n = (long long)y * g.pitch + x;
+  const double r = rho[n], ux = u[n], uy = u[g.plane + n];
+  mr[n] = T(r);
+  mx[n] = T(ux);
+  my[n] = T(uy);
+  if (g.cls[n] == 2) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Store<S>::st(f, k * g.plane + n, T(0), p);
+    return;
+  }
+  const double hu2 = p.half_inv_cs_2 * (ux * ux + uy * uy);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const int cx = CXk(k), cy = CYk(k);
+    double cu = 0.0;
+    if (cx != 0 && cy != 0) cu = (cx > 0 ? ux : -ux) + (cy > 0 ? uy : -uy);
+    else if (cx != 0) cu = cx > 0 ? ux : -ux;
+    else if (cy != 0) cu = cy > 0 ? uy : -uy;
+    double e = (cx == 0 && cy == 0) ? 1.0 - hu2
+                                    : ((1.0 + p.inv_cs_2 * cu) + (p.half_inv_cs_4 * cu) * cu) - hu2;
+    if (Store<S>::shifted) {
+      // g_eq = f_eq - w computed without cancellation: w (r e - 1) = w ((r - 1) + r (e - 1))
+      const double em1 = (cx == 0 && cy == 0) ? -hu2
+                                              : (p.inv_cs_2 * cu + (p.half_inv_cs_4 * cu) * cu) - hu2;
+      Store<S>::st(f, k * g.plane + n, T(Wk(k) * ((r - 1.0) + r * em1)), p);
+    } else {
+      Store<S>::st(f, k * g.plane + n, T((Wk(k) * r) * e), p);
+    }
+  }
+}
+
+}  // namespace lbm

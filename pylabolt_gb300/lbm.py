@@ -1,0 +1,153 @@
+"""Python host object for one case on one GPU (wraps the C-ABI handle).
+
+``FluidLBM(case)`` plays the role of the reference's operator set for the
+fluidLB step (collision, force, compute-fields, streaming, boundary and
+residue operators bound to one backend, pylabolt/solvers/fluidLB.py:109-204):
+its methods are the calls the reference's ``Solver`` makes on them.
+"""
+import ctypes
+
+import numpy as np
+
+from . import capi
+from .capi import check, ptr
+from .config import Case
+from .geometry import build_links
+
+_STORAGE = {"fp64": capi.LBM_FP64, "fp32_shifted": capi.LBM_FP32_SHIFTED,
+            "fp16_shifted": capi.LBM_FP16_SHIFTED}
+_FORCING = {None: capi.LBM_FORCING_NONE, "guo_linear": capi.LBM_GUO_LINEAR,
+            "guo_second_order": capi.LBM_GUO_SECOND_ORDER}
+
+
+def make_config(case, storage=None, device=0):
+    storage = storage or case.storage
+    cfg = capi.LbmConfig()
+    cfg.nx, cfg.ny = case.nx, case.ny
+    cfg.precision = _STORAGE[storage]
+    cfg.collision = capi.LBM_MRT if case.collision == "MRT" else capi.LBM_BGK
+    cfg.forcing = _FORCING[case.forcing]
+    cfg.body_force_field = int(case.body_force_field is not None)
+    cfg.device = device
+    cfg.omega = case.omega
+    cfg.inv_cs_2, cfg.inv_cs_4, cfg.eps = case.inv_cs_2, case.inv_cs_4, case.eps
+    cfg.gravity[:] = [float(v) for v in case.gravity]
+    cfg.mrt_s[:] = list(case.mrt_rates)
+    cfg.fp16_scale = case.fp16_scale
+    return cfg
+
+
+class FluidLBM:
+    """One fluidLB case resident on the GPU."""
+
+    def __init__(self, case, storage=None, device=0):
+        if not isinstance(case, Case):
+            case = Case(case)
+        self.case = case
+        self.storage = storage or case.storage
+        self.lib = capi.load()
+        self.cfg = make_config(case, self.storage, device)
+        self.node_solid, self.links = build_links(case)
+        h = ctypes.c_void_p()
+        check(self.lib.lbm_create(ctypes.byref(self.cfg), ptr(self.node_solid),
+                                  ptr(self.links), len(self.links), ctypes.byref(h)))
+        self.h = h
+        if case.body_force_field is not None:
+            self.set_body_force(case.body_force_field)
+
+    # -- life cycle
+    def close(self):
+        if getattr(self, "h", None):
+            check(self.lib.lbm_destroy(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- set-up
+    def initialize(self, density=None, velocity=None):
+        """f = f_eq(rho, u) on fluid nodes (equilibrium_kernels.py:38-78)."""
+        rho = np.ascontiguousarray(self.case.density if density is None else density,
+                                   dtype=np.float64)
+        u = np.ascontiguousarray(self.case.velocity if velocity is None else velocity,
+                                 dtype=np.float64)
+        check(self.lib.lbm_init_fields(self.h, ptr(rho), ptr(u), capi.LAYOUT_INNER))
+
+    def set_body_force(self, force):
+        f = np.ascontiguousarray(force, dtype=np.float64)
+        check(self.lib.lbm_set_body_force(self.h, ptr(f)))
+
+    # -- time stepping
+    def step(self, nsteps=1, moments=False, residual=False):
+        flags = (capi.STEP_MOMENTS if moments else 0) | (capi.STEP_RESIDUAL if residual else 0)
+        check(self.lib.lbm_step_ex(self.h, int(nsteps), flags))
+
+    def time_steps(self, nsteps):
+        ms = ctypes.c_double()
+        check(self.lib.lbm_time_steps(self.h, int(nsteps), ctypes.byref(ms)))
+        return ms.value
+
+    def synchronize(self, timeout_s=600.0):
+        check(self.lib.lbm_synchronize(self.h, float(timeout_s)))
+
+    # -- results
+    def moments(self, layout=capi.LAYOUT_INNER):
+        """(rho, u) recorded at the last moments step: inner layout gives
+        ``[Nx, Ny]`` / ``[Nx, Ny, 2]``; padded gives the reference's
+        ``[(Nx+2)*(Ny+2)]`` / ``[..., 2]`` arrays (ghosts 0)."""
+        nx, ny = self.case.nx, self.case.ny
+        n = nx * ny if layout == capi.LAYOUT_INNER else (nx + 2) * (ny + 2)
+        rho = np.empty(n)
+        u = np.empty((n, 2))
+        check(self.lib.lbm_get_moments(self.h, ptr(rho), ptr(u), layout))
+        if layout == capi.LAYOUT_INNER:
+            return rho.reshape(nx, ny), u.reshape(nx, ny, 2)
+        return rho, u
+
+    def residual(self):
+        out = (ctypes.c_double * 3)()
+        check(self.lib.lbm_residual(self.h, out))
+        return np.array(out[:])
+
+    def conservation(self):
+        out = (ctypes.c_double * 3)()
+        check(self.lib.lbm_conservation(self.h, out))
+        return np.array(out[:])
+
+    def populations(self):
+        """Post-collision populations of the last step, padded AoS FP64."""
+        nx, ny = self.case.nx, self.case.ny
+        pop = np.empty(((nx + 2) * (ny + 2), 9))
+        check(self.lib.lbm_get_populations(self.h, ptr(pop)))
+        return pop
+
+    def set_populations(self, pop_new):
+        p = np.ascontiguousarray(pop_new, dtype=np.float64)
+        check(self.lib.lbm_set_populations(self.h, ptr(p)))
+
+    @property
+    def time(self):
+        t = ctypes.c_int64()
+        check(self.lib.lbm_time(self.h, ctypes.byref(t)))
+        return t.value
+
+    @property
+    def kernel_launches(self):
+        t = ctypes.c_int64()
+        check(self.lib.lbm_kernel_launches(self.h, ctypes.byref(t)))
+        return t.value
+
+    @property
+    def device_bytes(self):
+        t = ctypes.c_int64()
+        check(self.lib.lbm_device_bytes(self.h, ctypes.byref(t)))
+        return t.value

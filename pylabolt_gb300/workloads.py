@@ -1,0 +1,109 @@
+"""Case dictionaries of the benchmark workloads (synthetic inputs).
+
+No dataset is involved: every workload is a lattice-Boltzmann case generated
+here from its stated shape and parameters, with seeded random perturbations.
+
+* ``cavity``     lid-driven cavity, BGK, bounce-back walls + moving lid
+* ``poiseuille`` gravity-driven channel, MRT + Guo forcing, periodic in x
+* ``cylinder``   channel with a cylinder, anti-bounce-back pressure inlet /
+                 outlet, bounce-back walls and cylinder, seeded +-1e-4 velocity
+                 perturbation (numpy default_rng(seed))
+"""
+import numpy as np
+
+
+def _base(nx, ny, kin_visc, precision="double", storage=None, model="BGK",
+          forcing=None, gravity=None, mrt_rates=None):
+    cd = {"start_time": 0, "end_time": 0, "std_out_interval": None,
+          "save_interval": None, "checkpoint_interval": None, "precision": precision}
+    if storage:
+        cd["storage"] = storage
+    col = {"model": model, "equilibrium": "density_based_second_order",
+           "forcing_model": forcing}
+    if mrt_rates:
+        col["mrt_rates"] = dict(mrt_rates)
+    return {
+        "control_dict": cd,
+        "mesh_dict": {"grid": [nx, ny]},
+        "lattice_dict": {"lattice_type": "D2Q9"},
+        "decompose_dict": {"nx": 1, "ny": 1},
+        "transport_dict": {"kin_visc": kin_visc},
+        "initial_fields_dict": {"default": {"fluid": {
+            "velocity": {"type": "fixed", "value": [0.0, 0.0]},
+            "density": {"type": "fixed", "value": 1.0},
+            "pressure": {"type": "fixed", "value": 0.0}}}},
+        "boundary_dict": {"options": {}},
+        "obstacle_dict": {"options": {}},
+        "collision_dict": {"fluid": col},
+        "forcing_dict": {} if gravity is None else {"gravity": list(gravity)},
+    }
+
+
+def cavity(n=128, re=100.0, lid=0.1, storage=None, lid_last=True):
+    """Lid-driven cavity, nu = U N / Re, tau = 3 nu + 1/2 (128^2, Re 100 ->
+    nu = 0.128, tau = 0.884)."""
+    kin_visc = lid * n / re
+    c = _base(n, n, kin_visc, storage=storage)
+    walls = {"wall": True, "segments": [[[0, 0], [0, n - 1]], [[n - 1, 0], [n - 1, n - 1]],
+                                         [[0, 0], [n - 1, 0]]],
+             "fluid": {"type": "bounce_back"}}
+    lid_d = {"wall": True, "segments": [[[0, n - 1], [n - 1, n - 1]]],
+             "fluid": {"type": "fixed_velocity", "value": [lid, 0.0]}}
+    if lid_last:
+        c["boundary_dict"]["walls"] = walls
+        c["boundary_dict"]["lid"] = lid_d
+    else:
+        c["boundary_dict"]["lid"] = lid_d
+        c["boundary_dict"]["walls"] = walls
+    return c
+
+
+def poiseuille(nx=1024, ny=512, u_c=0.05, re=100.0, model="MRT", storage=None,
+               rates=(1.4, 1.4, 1.2), forcing="guo_second_order"):
+    """Gravity-driven plane Poiseuille flow, periodic in x, bounce-back walls in
+    y.  The walls sit half a link outside the first and last rows, so the
+    channel height is H = ny; nu = u_c H / Re, g_x = 8 nu u_c / H^2."""
+    h = float(ny)
+    kin_visc = u_c * h / re
+    gx = 8.0 * kin_visc * u_c / (h * h)
+    c = _base(nx, ny, kin_visc, model=model, forcing=forcing, gravity=[gx, 0.0],
+              storage=storage,
+              mrt_rates={"s_e": rates[0], "s_eps": rates[1], "s_q": rates[2]}
+              if model == "MRT" else None)
+    c["boundary_dict"]["inout"] = {"wall": False, "segments": [
+        [[0, 0], [0, ny - 1]], [[nx - 1, 0], [nx - 1, ny - 1]]], "fluid": {"type": "periodic"}}
+    c["boundary_dict"]["walls"] = {"wall": True, "segments": [
+        [[0, 0], [nx - 1, 0]], [[0, ny - 1], [nx - 1, ny - 1]]], "fluid": {"type": "bounce_back"}}
+    return c, {"gx": gx, "kin_visc": kin_visc, "H": h, "u_c": u_c}
+
+
+def poiseuille_profile(ny, gx, kin_visc):
+    """Analytic u_x(y) for walls at y = -1/2 and y = ny - 1/2."""
+    y = np.arange(ny) + 0.5
+    return gx / (2.0 * kin_visc) * y * (ny - y)
+
+
+def cylinder(nx=8192, ny=2048, model="BGK", storage=None, kin_visc=0.04, radius=128.0,
+             center=(2048, 1027), rho_in=1.0005, rho_out=1.0, seed=0, amp=1e-4,
+             rates=(1.4, 1.4, 1.2)):
+    """Channel with a cylinder of diameter 256 at (2048, 1024+3): anti-bounce-back
+    pressure inlet (rho 1.0005) / outlet (rho 1.0), bounce-back top / bottom and
+    cylinder, u0 ~ U(-amp, amp) per component from default_rng(seed)."""
+    c = _base(nx, ny, kin_visc, model=model, storage=storage,
+              mrt_rates={"s_e": rates[0], "s_eps": rates[1], "s_q": rates[2]}
+              if model == "MRT" else None)
+    b = c["boundary_dict"]
+    b["inlet"] = {"wall": False, "segments": [[[0, 0], [0, ny - 1]]],
+                  "fluid": {"type": "fixed_pressure", "value": rho_in}}
+    b["outlet"] = {"wall": False, "segments": [[[nx - 1, 0], [nx - 1, ny - 1]]],
+                   "fluid": {"type": "fixed_pressure", "value": rho_out}}
+    b["walls"] = {"wall": True, "segments": [[[0, 0], [nx - 1, 0]],
+                                              [[0, ny - 1], [nx - 1, ny - 1]]],
+                  "fluid": {"type": "bounce_back"}}
+    c["obstacle_dict"]["cylinder"] = {"type": "circle", "radius": float(radius),
+                                      "center": [int(center[0]), int(center[1])],
+                                      "density": 1.0, "static": True}
+    rng = np.random.default_rng(seed)
+    u0 = rng.uniform(-amp, amp, size=(nx, ny, 2))
+    c["initial_fields_dict"]["default"]["fluid"]["velocity"] = {"type": "array", "value": u0}
+    return c

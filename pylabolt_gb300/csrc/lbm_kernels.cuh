@@ -278,8 +278,10 @@ __device__ __forceinline__ typename Store<S>::T special_link(
                    ((T(1) + (T(p.half_inv_cs_4) * cu) * cu) - T(p.half_inv_cs_2) * u2);
     return -raw + temp;
   }
-  return -raw + T(2.0 * Wk(KB)) *
-                    ((rho_w - T(1)) + rho_w * (T(4.5) * cu * cu - T(1.5) * u2));
+  // rho_w - 1 is formed in FP64: rounding rho_w itself to FP32 would shift the
+  // imposed density difference by up to 6e-8 absolute.
+  const T drho_w = T(g.rparam[li] - 1.0);
+  return -raw + T(2.0 * Wk(KB)) * (drho_w + rho_w * (T(4.5) * cu * cu - T(1.5) * u2));
 }
 
 template <class T>

@@ -162,6 +162,11 @@ int lbm_time(LbmHandle* h, int64_t* t);
 /* Number of fused step-kernel launches issued since the handle was created. */
 int lbm_kernel_launches(LbmHandle* h, int64_t* n);
 
+/* Launch shape of the fused step picked by the autotuner on the first step
+ * (nodes per thread, threads per block); LBM_VARIANT="v,b" forces one,
+ * LBM_TUNE=0 keeps the default. */
+int lbm_kernel_variant(LbmHandle* h, int* nodes_per_thread, int* block_threads);
+
 /* Device bytes held by the handle. */
 int lbm_device_bytes(LbmHandle* h, int64_t* bytes);
 

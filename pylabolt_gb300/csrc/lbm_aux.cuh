@@ -13,7 +13,7 @@ __global__ void convert_kernel(const Geom g, const Params p, S* f, double* f64,
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   if (x >= g.nx) return;
-  const long long n = (long long)y * g.pitch + x;
+  const long long n = g.node(x, y);
   const bool solid = g.cls[n] == 2;
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
@@ -33,7 +33,7 @@ __global__ void moments_to_f64_kernel(const Geom g, const T* mr, const T* mx,
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   if (x >= g.nx) return;
-  const long long n = (long long)y * g.pitch + x;
+  const long long n = g.node(x, y);
   out[n] = double(mr[n]);
   out[g.plane + n] = double(mx[n]);
   out[2 * g.plane + n] = double(my[n]);
@@ -44,7 +44,7 @@ __global__ void body_from_f64_kernel(const Geom g, const double* in, T* out) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   if (x >= g.nx) return;
-  const long long n = (long long)y * g.pitch + x;
+  const long long n = g.node(x, y);
   out[n] = T(in[n]);
   out[g.plane + n] = T(in[g.plane + n]);
 }
@@ -56,7 +56,7 @@ __global__ void conservation_kernel(const Geom g, const Params p, const S* f,
   const int y = blockIdx.x;
   double s[3] = {0, 0, 0};
   for (int x = threadIdx.x; x < g.nx; x += blockDim.x) {
-    const long long n = (long long)y * g.pitch + x;
+    const long long n = g.node(x, y);
     if (g.cls[n] == 2) continue;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
@@ -87,20 +87,33 @@ struct Kernels {
     return dim3((g.nx + kStepBlock - 1) / kStepBlock, g.ny);
   }
   template <int COLL, int FORC>
-  static cudaError_t step_t(const StepArgs& a, dim3 grid, dim3 block, cudaStream_t s) {
-    step_kernel<S, COLL, FORC><<<grid, block, 0, s>>>(a);
+  static cudaError_t step_t(const StepArgs& a, Variant v, cudaStream_t s) {
+    const dim3 grid = step_grid(a.g, v);
+    if constexpr (Store<S>::shifted) {
+      constexpr int V1 = sizeof(S) == 4 ? 4 : 8;
+      constexpr int V2 = sizeof(S) == 4 ? 2 : 4;
+      if (v.vec == V1) {
+        step_vec_kernel<S, V1, COLL, FORC><<<grid, v.block, 0, s>>>(a);
+        return cudaGetLastError();
+      }
+      if (v.vec == V2) {
+        step_vec_kernel<S, V2, COLL, FORC><<<grid, v.block, 0, s>>>(a);
+        return cudaGetLastError();
+      }
+    }
+    if (v.vec != 1) return cudaErrorInvalidValue;
+    step_kernel<S, COLL, FORC><<<grid, v.block, 0, s>>>(a);
     return cudaGetLastError();
   }
-  static cudaError_t step(int coll, int forc, const StepArgs& a, dim3 grid,
-                          dim3 block, cudaStream_t s) {
+  static cudaError_t step(int coll, int forc, const StepArgs& a, Variant v, cudaStream_t s) {
     if (coll == 0) {
-      if (forc == 0) return step_t<0, 0>(a, grid, block, s);
-      if (forc == 1) return step_t<0, 1>(a, grid, block, s);
-      return step_t<0, 2>(a, grid, block, s);
+      if (forc == 0) return step_t<0, 0>(a, v, s);
+      if (forc == 1) return step_t<0, 1>(a, v, s);
+      return step_t<0, 2>(a, v, s);
     }
-    if (forc == 0) return step_t<1, 0>(a, grid, block, s);
-    if (forc == 1) return step_t<1, 1>(a, grid, block, s);
-    return step_t<1, 2>(a, grid, block, s);
+    if (forc == 0) return step_t<1, 0>(a, v, s);
+    if (forc == 1) return step_t<1, 1>(a, v, s);
+    return step_t<1, 2>(a, v, s);
   }
   static cudaError_t init(const Geom& g, const Params& p, const double* rho,
                           const double* u, void* f, void* mr, void* mx, void* my,
@@ -139,6 +152,17 @@ struct Kernels {
     k.elem_bytes = sizeof(S);
     k.compute_bytes = sizeof(T);
     k.step = &step;
+    if constexpr (Store<S>::shifted) {
+      constexpr int V1 = sizeof(S) == 4 ? 4 : 8;
+      constexpr int V2 = sizeof(S) == 4 ? 2 : 4;
+      const Variant vs[] = {{V1, 256}, {V1, 128}, {V2, 256}, {V2, 128}, {1, 256}};
+      k.nvariants = 5;
+      for (int i = 0; i < 5; ++i) k.variants[i] = vs[i];
+    } else {
+      const Variant vs[] = {{1, 256}, {1, 128}, {1, 512}};
+      k.nvariants = 3;
+      for (int i = 0; i < 3; ++i) k.variants[i] = vs[i];
+    }
     k.init = &init;
     k.convert = &convert;
     k.moments_to_f64 = &moments_to_f64;

@@ -9,6 +9,7 @@
 
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -35,7 +36,6 @@ int fail(int code, const std::string& msg) {
       return fail(LBM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
-constexpr int kBlock = 256;
 constexpr int kGraphChunk = 32;   // steps per captured graph (even)
 constexpr int kCX[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
 constexpr int kCY[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
@@ -50,14 +50,15 @@ struct LbmHandle {
   cudaStream_t stream = nullptr;
   std::vector<void*> allocs;
   size_t dev_bytes = 0;
-  void* pop[2] = {nullptr, nullptr};
+  void* pop[2] = {nullptr, nullptr};      // first population plane
+  void* pop_raw[2] = {nullptr, nullptr};  // allocation (one guard row each side)
   void* side[2] = {nullptr, nullptr};
   void* mom[3] = {nullptr, nullptr, nullptr};
   void* old[3] = {nullptr, nullptr, nullptr};
   void* body = nullptr;
   double* partials = nullptr;
-  long long nparts = 0;
   double* red = nullptr;       // device [16]: residual sums, conservation sums
+  double* scratch = nullptr;   // device [kFinishBlocks*8]: first reduction stage
   double* host_red = nullptr;  // pinned  [16]
   double* stage = nullptr;     // device FP64 staging
   size_t stage_elems = 0;
@@ -66,7 +67,9 @@ struct LbmHandle {
   int64_t t = 0, launches = 0;
   cudaGraphExec_t gexec = nullptr;
   int gparity = 0;
-  dim3 grid, block;
+  lbm::Variant variant{1, 256};
+  bool tuned = false;
+  double tune_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   double timeout_s = 600.0;
 
   ~LbmHandle() {
@@ -130,7 +133,11 @@ struct LbmHandle {
                                        : (long long)cfg.nx * cfg.ny;
   }
 
-  int launch(int flags) {
+  // One fused step launch; advance=false leaves the state untouched (the
+  // kernel only writes the other population buffer and side array).
+  int launch(int flags, bool advance = true) { return launch_v(flags, variant, advance); }
+
+  int launch_v(int flags, lbm::Variant v, bool advance) {
     lbm::StepArgs a;
     a.g = g;
     a.p = p;
@@ -147,9 +154,59 @@ struct LbmHandle {
     a.partials = partials;
     a.body = body;
     a.flags = flags;
-    LBM_CUDA(ks->step(cfg.collision, cfg.forcing, a, grid, block, stream));
-    cur ^= 1;
+    LBM_CUDA(ks->step(cfg.collision, cfg.forcing, a, v, stream));
+    if (advance) cur ^= 1;
     return LBM_OK;
+  }
+
+  long long nparts_of(lbm::Variant v) const {
+    const dim3 gr = lbm::step_grid(g, v);
+    return (long long)gr.x * gr.y;
+  }
+
+  // Times every candidate launch shape on the current state (without
+  // advancing it) and keeps the fastest.
+  int autotune() {
+    tuned = true;
+    if (const char* f = std::getenv("LBM_VARIANT")) {
+      int vec = 0, blk = 0;
+      if (std::sscanf(f, "%d,%d", &vec, &blk) == 2) {
+        for (int i = 0; i < ks->nvariants; ++i)
+          if (ks->variants[i].vec == vec && ks->variants[i].block == blk) {
+            variant = ks->variants[i];
+            return LBM_OK;
+          }
+        return fail(LBM_ERR_ARG, std::string("LBM_VARIANT does not name a candidate: ") + f);
+      }
+    }
+    variant = ks->variants[0];
+    const char* t = std::getenv("LBM_TUNE");
+    if (t && t[0] == '0') return LBM_OK;
+    const int flags = nopull ? lbm::F_NOPULL : 0;
+    cudaEvent_t e0, e1;
+    LBM_CUDA(cudaEventCreate(&e0));
+    LBM_CUDA(cudaEventCreate(&e1));
+    double best = 1e30;
+    int rc = LBM_OK;
+    for (int i = 0; i < ks->nvariants && rc == LBM_OK; ++i) {
+      const lbm::Variant v = ks->variants[i];
+      if ((rc = launch_v(flags, v, false))) break;
+      cudaEventRecord(e0, stream);
+      for (int r = 0; r < 3 && rc == LBM_OK; ++r) rc = launch_v(flags, v, false);
+      cudaEventRecord(e1, stream);
+      if (rc == LBM_OK) rc = wait();
+      float ms = 0.f;
+      if (rc == LBM_OK && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) {
+        tune_ms[i] = ms / 3.0;
+        if (ms < best) {
+          best = ms;
+          variant = v;
+        }
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
   }
 
   int capture_graph() {
@@ -203,24 +260,25 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
                              : c.precision == LBM_FP32_SHIFTED ? &lbm::kernels_fp32()
                                                                 : &lbm::kernels_fp16();
   const int nx = c.nx, ny = c.ny;
-  const int align = 128 / ks->elem_bytes;
+  const int align = 512 / ks->elem_bytes;   // one warp's row segment
   const int pitch = (nx + align - 1) / align * align;
-  const long long plane = (long long)ny * pitch;
+  const long long plane = (long long)(ny + 2) * pitch;
   if (plane >= (1LL << 31) / 1)
     return fail(LBM_ERR_ARG, "lbm_create: grid too large (ny*pitch must be < 2^31)");
   const long long nin = (long long)nx * ny;
 
   // ---- host-side geometry and link table --------------------------------
-  std::vector<uint8_t> cls(plane, 0);
+  auto dnode = [&](long long x, long long y) { return (y + 1) * pitch + x; };
+  std::vector<uint8_t> cls(plane, 3);   // 3: padding row / column
   for (int x = 0; x < nx; ++x)
     for (int y = 0; y < ny; ++y)
-      if (node_solid[(long long)x * ny + y]) cls[(long long)y * pitch + x] = 2;
+      cls[dnode(x, y)] = node_solid[(long long)x * ny + y] ? 2 : 0;
   std::vector<int> recmap(plane, -1);
   for (int64_t r = 0; r < nlinks; ++r) {
     const int64_t node = links[r].node;
     if (node < 0 || node >= nin)
       return fail(LBM_ERR_ARG, "lbm_create: link record " + std::to_string(r) + " has node out of range");
-    const long long dn = (long long)(node % ny) * pitch + node / ny;
+    const long long dn = dnode(node / ny, node % ny);
     if (cls[dn] == 2)
       return fail(LBM_ERR_ARG, "lbm_create: link record for a solid node " + std::to_string(node));
     if (recmap[dn] >= 0)
@@ -243,7 +301,7 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
         const int64_t s = L.src[k];
         if (s < 0 || s >= nin)
           return fail(LBM_ERR_ARG, "lbm_create: PULL source out of range at node " + std::to_string(L.node));
-        const long long ds = (long long)(s % ny) * pitch + s / ny;
+        const long long ds = dnode(s / ny, s % ny);
         if (cls[ds] == 2)
           return fail(LBM_ERR_ARG, "lbm_create: PULL source is solid at node " + std::to_string(L.node));
         rsrc[li] = (int)ds;
@@ -251,7 +309,7 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
         const int64_t s = L.aux[k];
         if (s < 0 || s >= nin)
           return fail(LBM_ERR_ARG, "lbm_create: ABB neighbour out of range at node " + std::to_string(L.node));
-        const long long ds = (long long)(s % ny) * pitch + s / ny;
+        const long long ds = dnode(s / ny, s % ny);
         if (recmap[ds] < 0)
           return fail(LBM_ERR_ARG, "lbm_create: ABB neighbour " + std::to_string(s) +
                                        " of node " + std::to_string(L.node) + " has no link record");
@@ -264,10 +322,10 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   // every bulk node must have in-grid fluid neighbours
   for (int y = 0; y < ny; ++y)
     for (int x = 0; x < nx; ++x) {
-      if (cls[(long long)y * pitch + x] != 0) continue;
+      if (cls[dnode(x, y)] != 0) continue;
       for (int k = 1; k < 9; ++k) {
         const int xs = x - kCX[k], ys = y - kCY[k];
-        if (xs < 0 || xs >= nx || ys < 0 || ys >= ny || cls[(long long)ys * pitch + xs] == 2)
+        if (xs < 0 || xs >= nx || ys < 0 || ys >= ny || cls[dnode(xs, ys)] == 2)
           return fail(LBM_ERR_ARG, "lbm_create: node (" + std::to_string(x) + "," +
                                        std::to_string(y) + ") borders the grid edge or a solid but has no link record");
       }
@@ -276,7 +334,7 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   std::vector<uint8_t> segflag((size_t)ny * nseg, 0);
   for (int y = 0; y < ny; ++y)
     for (int x = 0; x < nx; ++x)
-      if (cls[(long long)y * pitch + x]) segflag[(size_t)y * nseg + x / 32] = 1;
+      if (cls[dnode(x, y)]) segflag[(size_t)y * nseg + x / 32] = 1;
 
   // ---- device --------------------------------------------------------------
   LbmHandle* h = new LbmHandle();
@@ -308,17 +366,21 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
       (rc = h->alloc(&d_rsrc, 9 * nrec1 * sizeof(int))) ||
       (rc = h->alloc(&d_rparam, 9 * nrec1 * sizeof(double))) ||
       (rc = h->alloc(&d_raux, 9 * nrec1 * sizeof(int))) ||
-      (rc = h->alloc(&h->pop[0], 9 * plane * eb)) || (rc = h->alloc(&h->pop[1], 9 * plane * eb)) ||
+      (rc = h->alloc(&h->pop_raw[0], (9 * plane + 2 * pitch) * eb)) ||
+      (rc = h->alloc(&h->pop_raw[1], (9 * plane + 2 * pitch) * eb)) ||
       (rc = h->alloc(&h->side[0], 3 * nrec1 * cb)) || (rc = h->alloc(&h->side[1], 3 * nrec1 * cb)))
     return bail(rc);
+  // one guard row before and after the nine planes
+  for (int i = 0; i < 2; ++i) h->pop[i] = static_cast<char*>(h->pop_raw[i]) + pitch * eb;
   for (int i = 0; i < 3; ++i)
     if ((rc = h->alloc(&h->mom[i], plane * cb)) || (rc = h->alloc(&h->old[i], plane * cb)))
       return bail(rc);
-  h->block = dim3(kBlock);
-  h->grid = dim3((nx + kBlock - 1) / kBlock, ny);
-  h->nparts = (long long)h->grid.x * h->grid.y;
-  if ((rc = h->alloc(reinterpret_cast<void**>(&h->partials), std::max<long long>(h->nparts, ny) * 8 * sizeof(double))) ||
-      (rc = h->alloc(reinterpret_cast<void**>(&h->red), 16 * sizeof(double))))
+  h->variant = ks->variants[0];
+  long long maxparts = ny;
+  for (int i = 0; i < ks->nvariants; ++i) maxparts = std::max(maxparts, h->nparts_of(ks->variants[i]));
+  if ((rc = h->alloc(reinterpret_cast<void**>(&h->partials), maxparts * 8 * sizeof(double))) ||
+      (rc = h->alloc(reinterpret_cast<void**>(&h->red), 16 * sizeof(double))) ||
+      (rc = h->alloc(reinterpret_cast<void**>(&h->scratch), lbm::kFinishBlocks * 8 * sizeof(double))))
     return bail(rc);
   e = cudaMallocHost(reinterpret_cast<void**>(&h->host_red), 16 * sizeof(double));
   if (e != cudaSuccess) return bail(fail(LBM_ERR_ALLOC, std::string("cudaMallocHost: ") + cudaGetErrorString(e)));
@@ -341,7 +403,7 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
       (e = up(d_raux, raux.data(), raux.size() * sizeof(int))) != cudaSuccess)
     return bail(fail(LBM_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(e)));
   for (int i = 0; i < 2; ++i) {
-    if ((e = cudaMemsetAsync(h->pop[i], 0, 9 * plane * eb, h->stream)) != cudaSuccess ||
+    if ((e = cudaMemsetAsync(h->pop_raw[i], 0, (9 * plane + 2 * pitch) * eb, h->stream)) != cudaSuccess ||
         (e = cudaMemsetAsync(h->side[i], 0, 3 * nrec1 * cb, h->stream)) != cudaSuccess)
       return bail(fail(LBM_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
   }
@@ -450,6 +512,7 @@ int lbm_step_ex(LbmHandle* h, int64_t nsteps, int flags) {
     h->launches += 1;
     return LBM_OK;
   };
+  if (!h->tuned && (rc = h->autotune())) return rc;
   if (h->nopull) {
     if ((rc = one(lbm::F_NOPULL | (nsteps == 1 ? kflags : 0)))) return rc;
     s = 1;
@@ -474,7 +537,7 @@ int lbm_step_ex(LbmHandle* h, int64_t nsteps, int flags) {
   }
   if (flags & LBM_STEP_MOMENTS) h->has_moments = true;
   if (flags & LBM_STEP_RESIDUAL) {
-    LBM_CUDA(lbm::finish_reduce(h->partials, h->nparts, h->red, h->stream));
+    LBM_CUDA(lbm::finish_reduce(h->partials, h->nparts_of(h->variant), h->scratch, h->red, h->stream));
     LBM_CUDA(cudaMemcpyAsync(h->host_red, h->red, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     h->has_residual = true;
   }
@@ -522,7 +585,7 @@ int lbm_conservation(LbmHandle* h, double out[3]) {
   if (!h->initialized) return fail(LBM_ERR_STATE, "lbm_conservation: not initialised");
   LBM_CUDA(cudaSetDevice(h->cfg.device));
   LBM_CUDA(h->ks->conservation(h->g, h->p, h->pop[h->cur], h->partials, h->stream));
-  LBM_CUDA(lbm::finish_reduce(h->partials, h->g.ny, h->red + 8, h->stream));
+  LBM_CUDA(lbm::finish_reduce(h->partials, h->g.ny, h->scratch, h->red + 8, h->stream));
   LBM_CUDA(cudaMemcpyAsync(h->host_red + 8, h->red + 8, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   int rc = h->wait();
   if (rc) return rc;
@@ -573,6 +636,14 @@ int lbm_time(LbmHandle* h, int64_t* t) {
 int lbm_kernel_launches(LbmHandle* h, int64_t* n) {
   if (!h || !n) return fail(LBM_ERR_ARG, "lbm_kernel_launches: null argument");
   *n = h->launches;
+  return LBM_OK;
+}
+
+int lbm_kernel_variant(LbmHandle* h, int* nodes_per_thread, int* block_threads) {
+  if (!h || !nodes_per_thread || !block_threads)
+    return fail(LBM_ERR_ARG, "lbm_kernel_variant: null argument");
+  *nodes_per_thread = h->variant.vec;
+  *block_threads = h->variant.block;
   return LBM_OK;
 }
 

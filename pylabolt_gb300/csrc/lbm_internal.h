@@ -7,12 +7,16 @@
 
 namespace lbm {
 
-// Device-side geometry of one case.  Populations are SoA planes
-// [q][ny][pitch] (x fastest), node index n = y*pitch + x.
+// Device-side geometry of one case.  Populations are SoA planes of
+// (ny+2) rows of `pitch` elements (x fastest); row 0 and row ny+1 are padding
+// rows so that vector loads of the rows above/below an edge row stay inside
+// the allocation.  Node (x, y) has index n = (y+1)*pitch + x.  `pitch` is a
+// multiple of the 512-byte row segment of one warp.
 struct Geom {
   int nx, ny, pitch, nseg;   // nseg = ceil(nx/32) warp segments per row
-  long long plane;           // elements per population plane = ny*pitch
+  long long plane;           // elements per population plane = (ny+2)*pitch
   const uint8_t* cls;        // [plane] node class: 0 bulk, 1 special, 2 solid
+                             // (3 on padding rows and columns)
   const uint8_t* segflag;    // [ny*nseg] 0: all 32 nodes of the segment bulk
   const int* recmap;         // [plane] record index of special nodes
   int nrec;
@@ -20,6 +24,10 @@ struct Geom {
   const int* rsrc;           // [nrec*9] PULL source node (device index)
   const double* rparam;      // [nrec*9]
   const int* raux;           // [nrec*9] ABB: record index of node x+n
+#ifdef __CUDACC__
+  __host__ __device__
+#endif
+  long long node(int x, int y) const { return (long long)(y + 1) * pitch + x; }
 };
 
 struct Params {
@@ -52,12 +60,21 @@ struct StepArgs {
   int flags;
 };
 
+// Launch shape of the fused step: nodes per thread (1 = scalar kernel) and
+// threads per block.
+struct Variant {
+  int vec;
+  int block;
+};
+
 // Kernels of one storage precision.
 struct KernelSet {
   int elem_bytes;        // storage bytes per population value
   int compute_bytes;     // bytes per moment value
-  cudaError_t (*step)(int collision, int forcing, const StepArgs& a, dim3 grid,
-                      dim3 block, cudaStream_t s);
+  cudaError_t (*step)(int collision, int forcing, const StepArgs& a, Variant v,
+                      cudaStream_t s);
+  int nvariants;             // candidate launch shapes for the autotuner
+  Variant variants[8];
   // f_eq(rho,u) into storage on fluid nodes (zeros on solids); moments get
   // rho/u on every node.  rho [plane], u [2][plane], FP64, device order.
   cudaError_t (*init)(const Geom& g, const Params& p, const double* rho,
@@ -81,9 +98,16 @@ const KernelSet& kernels_fp64();
 const KernelSet& kernels_fp32();
 const KernelSet& kernels_fp16();
 
-// Deterministic reduction of `nrows` rows of 8 doubles into out8 (fixed order).
-cudaError_t finish_reduce(const double* partials, long long nrows, double* out8,
-                          cudaStream_t s);
+// Deterministic reduction of `nrows` rows of 8 doubles into out8 (fixed
+// order); `scratch` holds kFinishBlocks rows.
+constexpr int kFinishBlocks = 128;
+cudaError_t finish_reduce(const double* partials, long long nrows, double* scratch,
+                          double* out8, cudaStream_t s);
+// grid of the fused step for variant v
+inline dim3 step_grid(const Geom& g, Variant v) {
+  const long long per_block = (long long)v.block * v.vec;
+  return dim3((unsigned)((g.pitch + per_block - 1) / per_block), (unsigned)g.ny);
+}
 // Host-order <-> device-order copies of FP64 node data with `ncomp`
 // components: host AoS [node][ncomp] in inner (ind = x*ny+y) or padded
 // (ind = (x+1)*(ny+2)+(y+1)) order; device SoA [ncomp][plane].

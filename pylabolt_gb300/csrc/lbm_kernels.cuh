@@ -284,7 +284,6 @@ __device__ __forceinline__ typename Store<S>::T special_link(
   return -raw + T(2.0 * Wk(KB)) * (drho_w + rho_w * (T(4.5) * cu * cu - T(1.5) * u2));
 }
 
-template <class T>
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -292,10 +291,144 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // ---------------------------------------------------------------------------
+// Moments, force, velocity and collision of one node: f holds the incoming
+// populations (f, or g = f - w when shifted) and receives the post-collision
+// ones.
 template <class S, int COLL, int FORC>
-__global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
+__device__ __forceinline__ void node_update(typename Store<S>::T f[9], const StepArgs& a,
+                                            long long n, typename Store<S>::T& rho,
+                                            typename Store<S>::T& ux,
+                                            typename Store<S>::T& uy) {
   using T = typename Store<S>::T;
   constexpr bool SH = Store<S>::shifted;
+  const Params& p = a.p;
+  T drho, jx, jy;
+  moments<SH>(f, rho, drho, jx, jy);
+  T Fx = T(0), Fy = T(0);
+  if (FORC != 0) {
+    if (a.body) {
+      const T* body = static_cast<const T*>(a.body);
+      Fx = body[n];
+      Fy = body[a.g.plane + n];
+    } else {
+      Fx = rho * T(p.gx);
+      Fy = rho * T(p.gy);
+    }
+  }
+  if (!SH) {
+    // compute_fields_kernels.py:61-65
+    const T inv_density = T(1) / (rho + T(p.eps));
+    ux = jx * inv_density + (T(0.5) * Fx) * inv_density;
+    uy = jy * inv_density + (T(0.5) * Fy) * inv_density;
+  } else {
+    const T inv_density = T(1) / rho;
+    ux = (jx + T(0.5) * Fx) * inv_density;
+    uy = (jy + T(0.5) * Fy) * inv_density;
+  }
+  if (COLL == 1) {
+    mrt_collide<FORC, SH>(f, rho, drho, ux, uy, Fx, Fy, p);
+  } else if (!SH) {
+    const T hu2 = T(p.half_inv_cs_2) * (ux * ux + uy * uy);
+    f[0] = bgk_ref_k<0, FORC>(f[0], rho, ux, uy, hu2, Fx, Fy, p);
+    f[1] = bgk_ref_k<1, FORC>(f[1], rho, ux, uy, hu2, Fx, Fy, p);
+    f[2] = bgk_ref_k<2, FORC>(f[2], rho, ux, uy, hu2, Fx, Fy, p);
+    f[3] = bgk_ref_k<3, FORC>(f[3], rho, ux, uy, hu2, Fx, Fy, p);
+    f[4] = bgk_ref_k<4, FORC>(f[4], rho, ux, uy, hu2, Fx, Fy, p);
+    f[5] = bgk_ref_k<5, FORC>(f[5], rho, ux, uy, hu2, Fx, Fy, p);
+    f[6] = bgk_ref_k<6, FORC>(f[6], rho, ux, uy, hu2, Fx, Fy, p);
+    f[7] = bgk_ref_k<7, FORC>(f[7], rho, ux, uy, hu2, Fx, Fy, p);
+    f[8] = bgk_ref_k<8, FORC>(f[8], rho, ux, uy, hu2, Fx, Fy, p);
+  } else {
+    const T u2 = ux * ux + uy * uy;
+    const T om = T(p.omega), omh = T(p.one_m_half_omega);
+    f[0] = bgk_shift_k<0, FORC>(f[0], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+    f[1] = bgk_shift_k<1, FORC>(f[1], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+    f[2] = bgk_shift_k<2, FORC>(f[2], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+    f[3] = bgk_shift_k<3, FORC>(f[3], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+    f[4] = bgk_shift_k<4, FORC>(f[4], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+    f[5] = bgk_shift_k<5, FORC>(f[5], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+    f[6] = bgk_shift_k<6, FORC>(f[6], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+    f[7] = bgk_shift_k<7, FORC>(f[7], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+    f[8] = bgk_shift_k<8, FORC>(f[8], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+  }
+}
+
+// Incoming populations of a boundary node from its link record.
+template <class S>
+__device__ __forceinline__ void special_links(typename Store<S>::T f[9], const StepArgs& a,
+                                              const S* __restrict__ fin, long long n, int r) {
+  using T = typename Store<S>::T;
+  const T* side = static_cast<const T*>(a.side_in);
+  f[1] = special_link<1, S>(a.g, a.p, fin, n, r, side);
+  f[2] = special_link<2, S>(a.g, a.p, fin, n, r, side);
+  f[3] = special_link<3, S>(a.g, a.p, fin, n, r, side);
+  f[4] = special_link<4, S>(a.g, a.p, fin, n, r, side);
+  f[5] = special_link<5, S>(a.g, a.p, fin, n, r, side);
+  f[6] = special_link<6, S>(a.g, a.p, fin, n, r, side);
+  f[7] = special_link<7, S>(a.g, a.p, fin, n, r, side);
+  f[8] = special_link<8, S>(a.g, a.p, fin, n, r, side);
+}
+
+// Side data, moment output and residual terms of one updated node.
+template <class T>
+__device__ __forceinline__ void node_outputs(const StepArgs& a, long long n, int r, T rho,
+                                             T ux, T uy, double red[7]) {
+  if (r >= 0) {
+    T* side = static_cast<T*>(a.side_out);
+    side[3 * r] = rho;
+    side[3 * r + 1] = ux;
+    side[3 * r + 2] = uy;
+  }
+  if (a.flags & F_MOMENTS) {
+    static_cast<T*>(a.rho)[n] = rho;
+    static_cast<T*>(a.ux)[n] = ux;
+    static_cast<T*>(a.uy)[n] = uy;
+  }
+  if (a.flags & F_RESIDUAL) {
+    // compute_residues_kernels.py:6-73: sums over fluid nodes
+    T* ro = static_cast<T*>(a.rho_old);
+    T* xo = static_cast<T*>(a.ux_old);
+    T* yo = static_cast<T*>(a.uy_old);
+    const double v[3] = {double(rho), double(ux), double(uy)};
+    const double o[3] = {double(ro[n]), double(xo[n]), double(yo[n])};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double d = v[c] - o[c];
+      red[2 * c] += d * d;
+      red[2 * c + 1] += o[c] * o[c];
+    }
+    red[6] += (isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2])) ? 0.0 : 1.0;
+    ro[n] = rho;
+    xo[n] = ux;
+    yo[n] = uy;
+  }
+}
+
+__device__ __forceinline__ void block_residual(const StepArgs& a, double red[7]) {
+  __shared__ double sh[32][8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < 7; ++i) {
+    const double v = warp_sum(red[i]);
+    if (lane == 0) sh[wid][i] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 7) {
+    double s = 0;
+    const int nw = blockDim.x >> 5;
+    for (int w = 0; w < nw; ++w) s += sh[w][threadIdx.x];
+    a.partials[((long long)blockIdx.y * gridDim.x + blockIdx.x) * 8 + threadIdx.x] = s;
+  }
+  if (threadIdx.x == 7)
+    a.partials[((long long)blockIdx.y * gridDim.x + blockIdx.x) * 8 + 7] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Scalar kernel: one node per thread.  Used for FP64 (whose cost is its FP64
+// arithmetic, not memory) and as an autotuner candidate.
+template <class S, int COLL, int FORC>
+__global__ void __launch_bounds__(512) step_kernel(const StepArgs a) {
+  using T = typename Store<S>::T;
   const Geom& g = a.g;
   const Params& p = a.p;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -303,7 +436,7 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
   double red[7] = {0, 0, 0, 0, 0, 0, 0};
 
   if (x < g.nx) {
-    const long long n = (long long)y * g.pitch + x;
+    const long long n = g.node(x, y);
     const S* __restrict__ fin = static_cast<const S*>(a.fin);
     S* __restrict__ fout = static_cast<S*>(a.fout);
     int cls = 0;
@@ -320,120 +453,175 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
         for (int k = 0; k < 9; ++k)
           f[k] = Store<S>::ld(fin, k * g.plane + n - CYk(k) * g.pitch - CXk(k), p);
       } else {
-        const T* side = static_cast<const T*>(a.side_in);
         f[0] = Store<S>::ld(fin, n, p);
-        f[1] = special_link<1, S>(g, p, fin, n, r, side);
-        f[2] = special_link<2, S>(g, p, fin, n, r, side);
-        f[3] = special_link<3, S>(g, p, fin, n, r, side);
-        f[4] = special_link<4, S>(g, p, fin, n, r, side);
-        f[5] = special_link<5, S>(g, p, fin, n, r, side);
-        f[6] = special_link<6, S>(g, p, fin, n, r, side);
-        f[7] = special_link<7, S>(g, p, fin, n, r, side);
-        f[8] = special_link<8, S>(g, p, fin, n, r, side);
+        special_links<S>(f, a, fin, n, r);
       }
-
-      T rho, drho, jx, jy;
-      moments<SH>(f, rho, drho, jx, jy);
-      T Fx = T(0), Fy = T(0);
-      if (FORC != 0) {
-        if (a.body) {
-          const T* body = static_cast<const T*>(a.body);
-          Fx = body[n];
-          Fy = body[g.plane + n];
-        } else {
-          Fx = rho * T(p.gx);
-          Fy = rho * T(p.gy);
-        }
-      }
-      T ux, uy;
-      if (!SH) {
-        // compute_fields_kernels.py:61-65
-        const T inv_density = T(1) / (rho + T(p.eps));
-        ux = jx * inv_density + (T(0.5) * Fx) * inv_density;
-        uy = jy * inv_density + (T(0.5) * Fy) * inv_density;
-      } else {
-        const T inv_density = T(1) / rho;
-        ux = (jx + T(0.5) * Fx) * inv_density;
-        uy = (jy + T(0.5) * Fy) * inv_density;
-      }
-
-      if (COLL == 1) {
-        mrt_collide<FORC, SH>(f, rho, drho, ux, uy, Fx, Fy, p);
-      } else if (!SH) {
-        const T hu2 = T(p.half_inv_cs_2) * (ux * ux + uy * uy);
-        f[0] = bgk_ref_k<0, FORC>(f[0], rho, ux, uy, hu2, Fx, Fy, p);
-        f[1] = bgk_ref_k<1, FORC>(f[1], rho, ux, uy, hu2, Fx, Fy, p);
-        f[2] = bgk_ref_k<2, FORC>(f[2], rho, ux, uy, hu2, Fx, Fy, p);
-        f[3] = bgk_ref_k<3, FORC>(f[3], rho, ux, uy, hu2, Fx, Fy, p);
-        f[4] = bgk_ref_k<4, FORC>(f[4], rho, ux, uy, hu2, Fx, Fy, p);
-        f[5] = bgk_ref_k<5, FORC>(f[5], rho, ux, uy, hu2, Fx, Fy, p);
-        f[6] = bgk_ref_k<6, FORC>(f[6], rho, ux, uy, hu2, Fx, Fy, p);
-        f[7] = bgk_ref_k<7, FORC>(f[7], rho, ux, uy, hu2, Fx, Fy, p);
-        f[8] = bgk_ref_k<8, FORC>(f[8], rho, ux, uy, hu2, Fx, Fy, p);
-      } else {
-        const T u2 = ux * ux + uy * uy;
-        const T om = T(p.omega), omh = T(p.one_m_half_omega);
-        f[0] = bgk_shift_k<0, FORC>(f[0], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-        f[1] = bgk_shift_k<1, FORC>(f[1], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-        f[2] = bgk_shift_k<2, FORC>(f[2], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-        f[3] = bgk_shift_k<3, FORC>(f[3], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-        f[4] = bgk_shift_k<4, FORC>(f[4], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-        f[5] = bgk_shift_k<5, FORC>(f[5], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-        f[6] = bgk_shift_k<6, FORC>(f[6], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-        f[7] = bgk_shift_k<7, FORC>(f[7], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-        f[8] = bgk_shift_k<8, FORC>(f[8], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-      }
+      T rho, ux, uy;
+      node_update<S, COLL, FORC>(f, a, n, rho, ux, uy);
 #pragma unroll
       for (int k = 0; k < 9; ++k) Store<S>::st(fout, k * g.plane + n, f[k], p);
+      node_outputs<T>(a, n, r, rho, ux, uy, red);
+    }
+  }
+  if (a.flags & F_RESIDUAL) block_residual(a, red);
+}
 
-      if (r >= 0) {
-        T* side = static_cast<T*>(a.side_out);
-        side[3 * r] = rho;
-        side[3 * r + 1] = ux;
-        side[3 * r + 2] = uy;
-      }
-      if (a.flags & F_MOMENTS) {
-        static_cast<T*>(a.rho)[n] = rho;
-        static_cast<T*>(a.ux)[n] = ux;
-        static_cast<T*>(a.uy)[n] = uy;
-      }
-      if (a.flags & F_RESIDUAL) {
-        // compute_residues_kernels.py:6-73: sums over fluid nodes
-        T* ro = static_cast<T*>(a.rho_old);
-        T* xo = static_cast<T*>(a.ux_old);
-        T* yo = static_cast<T*>(a.uy_old);
-        const double v[3] = {double(rho), double(ux), double(uy)};
-        const double o[3] = {double(ro[n]), double(xo[n]), double(yo[n])};
+// ---------------------------------------------------------------------------
+// Vector I/O of V consecutive nodes (16- or 8-byte aligned accesses).
+template <class S, int V> struct VecIO;
+template <int V> struct VecIO<float, V> {
+  static_assert(V == 2 || V == 4, "float vectors of 2 or 4");
+  __device__ static __forceinline__ void load(const float* __restrict__ p, float (&out)[V], const Params&) {
+    if constexpr (V == 4) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+      out[0] = v.x; out[1] = v.y; out[2] = v.z; out[3] = v.w;
+    } else {
+      const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+      out[0] = v.x; out[1] = v.y;
+    }
+  }
+  __device__ static __forceinline__ float ld1(const float* __restrict__ p, const Params&) { return __ldg(p); }
+  __device__ static __forceinline__ void store(float* __restrict__ p, const float (&in)[V], const Params&) {
+    if constexpr (V == 4)
+      *reinterpret_cast<float4*>(p) = make_float4(in[0], in[1], in[2], in[3]);
+    else
+      *reinterpret_cast<float2*>(p) = make_float2(in[0], in[1]);
+  }
+};
+template <int V> struct VecIO<__half, V> {
+  static_assert(V == 4 || V == 8, "half vectors of 4 or 8");
+  __device__ static __forceinline__ void load(const __half* __restrict__ p, float (&out)[V], const Params& q) {
+    const float s = float(q.inv_scale);
+    uint32_t w[V / 2];
+    if constexpr (V == 8) {
+      const uint4 raw = __ldg(reinterpret_cast<const uint4*>(p));
+      w[0] = raw.x; w[1] = raw.y; w[2] = raw.z; w[3] = raw.w;
+    } else {
+      const uint2 raw = __ldg(reinterpret_cast<const uint2*>(p));
+      w[0] = raw.x; w[1] = raw.y;
+    }
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const double d = v[c] - o[c];
-          red[2 * c] = d * d;
-          red[2 * c + 1] = o[c] * o[c];
+    for (int i = 0; i < V / 2; ++i) {
+      __half2 h;
+      memcpy(&h, &w[i], 4);
+      const float2 t = __half22float2(h);
+      out[2 * i] = t.x * s;
+      out[2 * i + 1] = t.y * s;
+    }
+  }
+  __device__ static __forceinline__ float ld1(const __half* __restrict__ p, const Params& q) {
+    return __half2float(p[0]) * float(q.inv_scale);
+  }
+  __device__ static __forceinline__ void store(__half* __restrict__ p, const float (&in)[V], const Params& q) {
+    const float s = float(q.scale);
+    uint32_t w[V / 2];
+#pragma unroll
+    for (int i = 0; i < V / 2; ++i) {
+      const __half2 h = __floats2half2_rn(in[2 * i] * s, in[2 * i + 1] * s);
+      memcpy(&w[i], &h, 4);
+    }
+    if constexpr (V == 8)
+      *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
+    else
+      *reinterpret_cast<uint2*>(p) = make_uint2(w[0], w[1]);
+  }
+};
+
+// Pulls direction K for the V nodes of this lane: one aligned vector load of
+// the source row plus a warp shuffle for the x shift (lane 0 / lane 31 load
+// the one element that crosses the warp's segment).
+template <class S, int V, int K>
+__device__ __forceinline__ void pull_dir(const S* __restrict__ fin, const Geom& g,
+                                         const Params& p, long long n0, int lane,
+                                         bool nopull, float (&f)[9][V]) {
+  constexpr int cx = CXk(K), cy = CYk(K);
+  const S* row = fin + K * g.plane + n0 - (nopull ? 0 : cy * g.pitch);
+  float a[V];
+  VecIO<S, V>::load(row, a, p);
+  if (cx == 0 || nopull) {  // nopull is the same for the whole grid
+#pragma unroll
+    for (int v = 0; v < V; ++v) f[K][v] = a[v];
+    return;
+  }
+  if constexpr (cx == 1) {
+    float prev = __shfl_up_sync(0xffffffffu, a[V - 1], 1);
+    if (lane == 0) prev = VecIO<S, V>::ld1(row - 1, p);
+    f[K][0] = prev;
+#pragma unroll
+    for (int v = 1; v < V; ++v) f[K][v] = a[v - 1];
+  } else {
+    float next = __shfl_down_sync(0xffffffffu, a[0], 1);
+    if (lane == 31) next = VecIO<S, V>::ld1(row + V, p);
+#pragma unroll
+    for (int v = 0; v < V - 1; ++v) f[K][v] = a[v + 1];
+    f[K][V - 1] = next;
+  }
+}
+
+// Vector kernel: each thread updates V consecutive nodes of one row; a warp
+// covers 32*V nodes (512 bytes of every population plane).  All lanes take
+// part in the loads and shuffles; boundary / solid / padding nodes are then
+// handled per node.
+template <class S, int V, int COLL, int FORC>
+__global__ void __launch_bounds__(256) step_vec_kernel(const StepArgs a) {
+  static_assert(Store<S>::shifted, "vector kernel is for shifted storage");
+  const Geom& g = a.g;
+  const Params& p = a.p;
+  const int lane = threadIdx.x & 31;
+  const int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * V;
+  const int warp_x0 = x0 - lane * V;
+  const int y = blockIdx.y;
+  double red[7] = {0, 0, 0, 0, 0, 0, 0};
+
+  if (warp_x0 < g.pitch) {
+    const long long n0 = g.node(x0, y);
+    const S* __restrict__ fin = static_cast<const S*>(a.fin);
+    S* __restrict__ fout = static_cast<S*>(a.fout);
+    const bool nopull = (a.flags & F_NOPULL) != 0;
+    float f[9][V];
+    pull_dir<S, V, 0>(fin, g, p, n0, lane, nopull, f);
+    pull_dir<S, V, 1>(fin, g, p, n0, lane, nopull, f);
+    pull_dir<S, V, 2>(fin, g, p, n0, lane, nopull, f);
+    pull_dir<S, V, 3>(fin, g, p, n0, lane, nopull, f);
+    pull_dir<S, V, 4>(fin, g, p, n0, lane, nopull, f);
+    pull_dir<S, V, 5>(fin, g, p, n0, lane, nopull, f);
+    pull_dir<S, V, 6>(fin, g, p, n0, lane, nopull, f);
+    pull_dir<S, V, 7>(fin, g, p, n0, lane, nopull, f);
+    pull_dir<S, V, 8>(fin, g, p, n0, lane, nopull, f);
+
+    if (x0 < g.nx) {
+      uint8_t cls[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) cls[v] = 0;
+      if (g.segflag[y * g.nseg + (x0 >> 5)]) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) cls[v] = g.cls[n0 + v];
+      } else if (x0 + V > g.nx) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) cls[v] = (x0 + v < g.nx) ? 0 : 3;
+      }
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        if (cls[v] >= 2) continue;  // solid or padding: keep as loaded
+        float fn[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) fn[k] = f[k][v];
+        int r = -1;
+        if (cls[v] == 1) {
+          r = g.recmap[n0 + v];
+          if (!nopull) special_links<S>(fn, a, fin, n0 + v, r);
         }
-        red[6] = (isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2])) ? 0.0 : 1.0;
-        ro[n] = rho;
-        xo[n] = ux;
-        yo[n] = uy;
-      }
-    }
-  }
-
-  if (a.flags & F_RESIDUAL) {
-    __shared__ double sh[8][8];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        float rho, ux, uy;
+        node_update<S, COLL, FORC>(fn, a, n0 + v, rho, ux, uy);
 #pragma unroll
-    for (int i = 0; i < 7; ++i) {
-      const double v = warp_sum<double>(red[i]);
-      if (lane == 0) sh[wid][i] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < 7) {
-      double s = 0;
-      const int nw = blockDim.x >> 5;
-      for (int w = 0; w < nw; ++w) s += sh[w][threadIdx.x];
-      a.partials[((long long)blockIdx.y * gridDim.x + blockIdx.x) * 8 + threadIdx.x] = s;
+        for (int k = 0; k < 9; ++k) f[k][v] = fn[k];
+        node_outputs<float>(a, n0 + v, r, rho, ux, uy, red);
+      }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) VecIO<S, V>::store(fout + k * g.plane + n0, f[k], p);
     }
   }
+  if (a.flags & F_RESIDUAL) block_residual(a, red);
 }
 
 // ---------------------------------------------------------------------------
@@ -448,7 +636,7 @@ __global__ void init_kernel(const Geom g, const Params p, const double* __restri
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   if (x >= g.nx) return;
-  const long long n = (long long)y * g.pitch + x;
+  const long long n = g.node(x, y);
   const double r = rho[n], ux = u[n], uy = u[g.plane + n];
   mr[n] = T(r);
   mx[n] = T(ux);

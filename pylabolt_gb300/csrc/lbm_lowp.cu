@@ -15,13 +15,18 @@ const KernelSet& kernels_fp16() {
   return k;
 }
 
-// Sums rows of 8 doubles.  One block of 256 threads: thread t sums rows
-// t, t+256, ... in order, then a fixed-shape tree -> same result every run.
+// Sums rows of 8 doubles in two fixed-shape stages (same result every run):
+// kFinishBlocks blocks each sum a contiguous range of rows (thread t takes
+// rows t, t+256, ... of the range, then a shared-memory tree), and one block
+// sums those kFinishBlocks rows the same way.
 __global__ void finish_reduce_kernel(const double* __restrict__ partials,
-                                     long long nrows, double* out8) {
+                                     long long nrows, double* out) {
   __shared__ double sh[8][256];
+  const long long per = (nrows + gridDim.x - 1) / gridDim.x;
+  const long long r0 = blockIdx.x * per;
+  const long long r1 = r0 + per < nrows ? r0 + per : nrows;
   double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  for (long long r = threadIdx.x; r < nrows; r += blockDim.x)
+  for (long long r = r0 + threadIdx.x; r < r1; r += blockDim.x)
 #pragma unroll
     for (int c = 0; c < 8; ++c) s[c] += partials[r * 8 + c];
 #pragma unroll
@@ -33,12 +38,13 @@ __global__ void finish_reduce_kernel(const double* __restrict__ partials,
       for (int c = 0; c < 8; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x < 8) out8[threadIdx.x] = sh[threadIdx.x][0];
+  if (threadIdx.x < 8) out[blockIdx.x * 8 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
-cudaError_t finish_reduce(const double* partials, long long nrows, double* out8,
-                          cudaStream_t s) {
-  finish_reduce_kernel<<<1, 256, 0, s>>>(partials, nrows, out8);
+cudaError_t finish_reduce(const double* partials, long long nrows, double* scratch,
+                          double* out8, cudaStream_t s) {
+  finish_reduce_kernel<<<kFinishBlocks, 256, 0, s>>>(partials, nrows, scratch);
+  finish_reduce_kernel<<<1, 256, 0, s>>>(scratch, kFinishBlocks, out8);
   return cudaGetLastError();
 }
 
@@ -51,7 +57,7 @@ __global__ void reorder_kernel(const Geom g, const double* __restrict__ in,
   if (x >= g.nx) return;
   const long long hn = layout == 0 ? (long long)x * g.ny + y
                                    : (long long)(x + 1) * (g.ny + 2) + (y + 1);
-  const long long dn = (long long)y * g.pitch + x;
+  const long long dn = g.node(x, y);
   for (int c = 0; c < ncomp; ++c) {
     if (to_device)
       out[c * g.plane + dn] = in[hn * ncomp + c];

@@ -147,6 +147,13 @@ class FluidLBM:
         return t.value
 
     @property
+    def kernel_variant(self):
+        """(nodes per thread, threads per block) of the fused step."""
+        v, b = ctypes.c_int(), ctypes.c_int()
+        check(self.lib.lbm_kernel_variant(self.h, ctypes.byref(v), ctypes.byref(b)))
+        return v.value, b.value
+
+    @property
     def device_bytes(self):
         t = ctypes.c_int64()
         check(self.lib.lbm_device_bytes(self.h, ctypes.byref(t)))

@@ -1,0 +1,166 @@
+"""FP32 / FP16 shifted storage against FP64, MRT against the oracle, every
+autotuner launch shape, and the large-case checks (full-size cavity bit-exact
+against the C oracle, Poiseuille against the analytic start-up flow)."""
+import os
+
+import numpy as np
+import pytest
+
+from _golden import golden_names, load_golden
+from pylabolt_gb300 import capi, workloads
+from pylabolt_gb300.config import Case
+from pylabolt_gb300.lbm import FluidLBM
+
+pytestmark = pytest.mark.gpu
+
+FP32_U_TOL = 1e-5     # max |u32 - u64| / max |u64|
+FP16_U_TOL = 2e-2
+MRT_TOL = 1e-12       # FP64 MRT, CUDA closed form vs oracle matrix form
+
+
+def _run(case, storage, steps, variant=None):
+    old = os.environ.get("LBM_VARIANT")
+    if variant:
+        os.environ["LBM_VARIANT"] = f"{variant[0]},{variant[1]}"
+    try:
+        with FluidLBM(case, storage=storage) as sim:
+            sim.initialize()
+            sim.step(steps, moments=True)
+            rho, u = sim.moments()
+            return rho, u, sim.populations(), sim.kernel_variant
+    finally:
+        if variant:
+            if old is None:
+                del os.environ["LBM_VARIANT"]
+            else:
+                os.environ["LBM_VARIANT"] = old
+
+
+def _rel(a, b, mask):
+    return np.abs(a[mask] - b[mask]).max() / max(np.abs(b[mask]).max(), 1e-300)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_shifted_storage_error_vs_fp64(name):
+    case_d, d = load_golden(name)
+    case = Case(case_d)
+    steps = int(d["nsteps"])
+    _, u64, _, _ = _run(case, "fp64", steps)
+    fluid = ~case.solid
+    _, u32, _, _ = _run(case, "fp32_shifted", steps)
+    _, u16, _, _ = _run(case, "fp16_shifted", steps)
+    assert _rel(u32, u64, fluid) <= FP32_U_TOL
+    assert _rel(u16, u64, fluid) <= FP16_U_TOL
+
+
+@pytest.mark.parametrize("storage,variants", [
+    ("fp64", [(1, 256), (1, 128), (1, 512)]),
+    ("fp32_shifted", [(4, 256), (4, 128), (2, 256), (2, 128), (1, 256)]),
+    ("fp16_shifted", [(8, 256), (8, 128), (4, 256), (4, 128), (1, 256)])])
+def test_every_launch_shape_agrees(storage, variants):
+    """The autotuner may pick any candidate: all must give the same result
+    (FP64 bit for bit; shifted storage within one rounding per step)."""
+    case_d, _ = load_golden("channel_cylinder_abb")
+    case = Case(case_d)
+    outs = [_run(case, storage, 40, v) for v in variants]
+    for (r, u, p, shape), v in zip(outs, variants):
+        assert shape == v
+    r0, u0, p0, _ = outs[0]
+    fluid = ~case.solid
+    for r, u, p, _ in outs[1:]:
+        if storage == "fp64":
+            assert np.array_equal(u, u0) and np.array_equal(p, p0)
+        else:
+            assert _rel(u, u0, fluid) <= 1e-5
+
+
+def test_mrt_fp64_matches_oracle():
+    from oracle.setup import build_state
+    from oracle import lbm_np
+    case_d, _ = load_golden("poiseuille_guo2")
+    case_d["collision_dict"]["fluid"]["model"] = "MRT"
+    case_d["collision_dict"]["fluid"]["mrt_rates"] = {"s_e": 1.4, "s_eps": 1.4, "s_q": 1.2}
+    st = build_state(case_d)
+    lbm_np.run(st, 300)
+    case = Case(case_d)
+    rho, u, pop, _ = _run(case, "fp64", 300)
+    ref_u = st.inner(st.velocity)
+    ref_r = st.inner(st.density)
+    assert np.abs(rho - ref_r).max() <= MRT_TOL * np.abs(ref_r).max()
+    assert np.abs(u - ref_u).max() <= MRT_TOL * np.abs(ref_u).max()
+
+
+def test_mrt_with_all_rates_omega_is_bgk():
+    """M^-1 S M = omega I: MRT with every rate = omega reduces to BGK."""
+    case_d, _ = load_golden("poiseuille_guo2")
+    case = Case(case_d)
+    _, u_bgk, _, _ = _run(case, "fp64", 200)
+    om = case.omega
+    case_d["collision_dict"]["fluid"]["model"] = "MRT"
+    case_d["collision_dict"]["fluid"]["mrt_rates"] = {"s_e": om, "s_eps": om, "s_q": om, "s_nu": om}
+    case_m = Case(case_d)
+    _, u_mrt, _, _ = _run(case_m, "fp64", 200)
+    assert np.abs(u_mrt - u_bgk).max() <= 1e-12 * np.abs(u_bgk).max()
+
+
+def test_cavity_128_20000_steps_bit_exact_vs_c_oracle():
+    """Lid-driven cavity 128x128, Re 100, 20,000 steps (the full cavity run)."""
+    from oracle.setup import build_state
+    from oracle.clib import COracle
+    case_d = workloads.cavity(128)
+    st = build_state(case_d)
+    co = COracle(st)
+    co.initialize()
+    co.run(20000)
+    case = Case(case_d)
+    rho, u, pop, _ = _run(case, "fp64", 20000)
+    assert np.array_equal(rho, st.inner(st.density))
+    assert np.array_equal(u, st.inner(st.velocity))
+    # FP32 shifted against the same FP64 field
+    _, u32, _, _ = _run(case, "fp32_shifted", 20000)
+    assert _rel(u32, u, np.ones_like(case.solid)) <= FP32_U_TOL
+
+
+def test_cylinder_small_bit_exact_vs_c_oracle():
+    """Cylinder channel (anti-bounce-back inlet/outlet) at 512x128, 300 steps."""
+    from oracle.setup import build_state
+    from oracle.clib import COracle
+    case_d = workloads.cylinder(nx=512, ny=128, radius=16.0, center=(128, 67))
+    st = build_state(case_d)
+    co = COracle(st)
+    co.initialize()
+    co.run(300)
+    case = Case(case_d)
+    rho, u, _, _ = _run(case, "fp64", 300)
+    m = ~case.solid
+    assert np.array_equal(rho[m], st.inner(st.density)[m])
+    assert np.array_equal(u[m], st.inner(st.velocity)[m])
+
+
+def _poiseuille_startup(ny, gx, nu, t, terms=200):
+    """u_x(y, t) of plane Poiseuille flow started from rest (walls at y=-1/2
+    and y=ny-1/2): parabola minus its Fourier decay."""
+    h = float(ny)
+    y = np.arange(ny) + 0.5
+    u = gx / (2 * nu) * y * (h - y)
+    for n in range(1, 2 * terms, 2):
+        u -= (4 * gx * h * h / (nu * (n * np.pi) ** 3) * np.sin(n * np.pi * y / h) *
+              np.exp(-nu * (n * np.pi / h) ** 2 * t))
+    return u
+
+
+def test_poiseuille_mrt_guo_full_size_vs_analytic():
+    """1024x512 MRT + Guo, 50,000 steps: FP64 and FP32 against the analytic
+    start-up profile and FP32 against FP64."""
+    case_d, par = workloads.poiseuille()
+    case = Case(case_d)
+    steps = 50000
+    _, u64, _, _ = _run(case, "fp64", steps)
+    _, u32, _, _ = _run(case, "fp32_shifted", steps)
+    prof = _poiseuille_startup(case.ny, par["gx"], par["kin_visc"], steps)
+    ux64 = u64[:, :, 0]
+    # x-uniform flow
+    assert np.abs(ux64 - ux64[:1]).max() <= 1e-12 * np.abs(ux64).max()
+    err = np.abs(ux64[0] - prof).max() / prof.max()
+    assert err < 5e-3, err
+    assert _rel(u32, u64, np.ones(u64.shape, bool)) <= FP32_U_TOL

@@ -15,7 +15,9 @@ pytestmark = pytest.mark.gpu
 
 FP32_U_TOL = 1e-5     # max |u32 - u64| / max |u64|
 FP16_U_TOL = 2e-2
-MRT_TOL = 1e-12       # FP64 MRT, CUDA closed form vs oracle matrix form
+# FP64 MRT, CUDA closed form vs oracle matrix form: both round differently, so
+# the bound is FP64 round-off accumulated over the run on O(1) populations.
+MRT_ATOL = 1e-13
 
 
 def _run(case, storage, steps, variant=None):
@@ -86,8 +88,9 @@ def test_mrt_fp64_matches_oracle():
     rho, u, pop, _ = _run(case, "fp64", 300)
     ref_u = st.inner(st.velocity)
     ref_r = st.inner(st.density)
-    assert np.abs(rho - ref_r).max() <= MRT_TOL * np.abs(ref_r).max()
-    assert np.abs(u - ref_u).max() <= MRT_TOL * np.abs(ref_u).max()
+    assert np.abs(rho - ref_r).max() <= MRT_ATOL
+    assert np.abs(u - ref_u).max() <= MRT_ATOL
+    assert np.abs(u - ref_u).max() <= 1e-10 * np.abs(ref_u).max()
 
 
 def test_mrt_with_all_rates_omega_is_bgk():
@@ -100,7 +103,7 @@ def test_mrt_with_all_rates_omega_is_bgk():
     case_d["collision_dict"]["fluid"]["mrt_rates"] = {"s_e": om, "s_eps": om, "s_q": om, "s_nu": om}
     case_m = Case(case_d)
     _, u_mrt, _, _ = _run(case_m, "fp64", 200)
-    assert np.abs(u_mrt - u_bgk).max() <= 1e-12 * np.abs(u_bgk).max()
+    assert np.abs(u_mrt - u_bgk).max() <= MRT_ATOL
 
 
 def test_cavity_128_20000_steps_bit_exact_vs_c_oracle():

@@ -195,7 +195,9 @@ __device__ __forceinline__ void mrt_collide(T f[9], T rho, T drho, T ux, T uy,
   const T third_i2 = i2 / T(3), ninth_i4 = i4 / T(9);
   T meq[9];
   // equilibrium moments; shifted form subtracts M w = (1, -2, 1, 0, ...)
-  meq[0] = rho - rho * ((T(3) * i2 - i4) / T(6)) * u2 - (SHIFTED ? T(1) : T(0));
+  // shifted: rho_eq - 1 = drho - ..., never (1 + drho) - 1, which would round
+  // the mass deviation to the FP32 spacing of 1
+  meq[0] = (SHIFTED ? drho : rho) - rho * ((T(3) * i2 - i4) / T(6)) * u2;
   meq[1] = SHIFTED ? (T(-2) * drho + rho * i2 * u2) : rho * (i2 * u2 - T(2));
   meq[2] = SHIFTED ? (drho - rho * ((T(3) * i2 + i4) / T(6)) * u2)
                    : rho - rho * ((T(3) * i2 + i4) / T(6)) * u2;

@@ -220,6 +220,8 @@ def run_gb300(args, world, rank, local):
     barrier()
     clk = clocks.stop()
     launches = sim.kernel_launches - launches0
+    variant = sim.kernel_variant
+    tuning = sim.tuning
     if dist is not None:
         t = torch.tensor([ms], device=f"cuda:{device}", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -288,7 +290,11 @@ def run_gb300(args, world, rank, local):
                        "bytes_per_lattice_update": B_LU[args.storage],
                        "l2": "inputs larger than L2 (two population buffers of "
                              f"{9 * nodes * B_LU[args.storage] / 18 / 1e6:.0f} MB)",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}",
+                       "kernel": {"kind": ["scalar", "vector", "tma_pipeline"][variant[0]],
+                                  "nodes_per_thread": variant[1], "block": variant[2],
+                                  "stages": variant[3],
+                                  "autotune_ms": [round(t, 4) for t in tuning]}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": traffic},

@@ -162,10 +162,16 @@ int lbm_time(LbmHandle* h, int64_t* t);
 /* Number of fused step-kernel launches issued since the handle was created. */
 int lbm_kernel_launches(LbmHandle* h, int64_t* n);
 
-/* Launch shape of the fused step picked by the autotuner on the first step
- * (nodes per thread, threads per block); LBM_VARIANT="v,b" forces one,
- * LBM_TUNE=0 keeps the default. */
-int lbm_kernel_variant(LbmHandle* h, int* nodes_per_thread, int* block_threads);
+/* Launch shape of the fused step picked by the autotuner on the first step:
+ * out = {kind (0 scalar, 1 vector, 2 TMA pipeline), nodes per thread,
+ * threads per block, shared-memory stages}.  LBM_VARIANT="kind,vec,block,stages"
+ * forces one candidate, LBM_TUNE=0 keeps the first.  (Extension: the
+ * reference launches every kernel with 256 threads, backend.py:59-75.) */
+int lbm_kernel_variant(LbmHandle* h, int out[4]);
+
+/* Per-candidate mean step time (ms) measured by the autotuner; *n receives the
+ * number of candidates (at most 12). */
+int lbm_tuning(LbmHandle* h, double* ms_per_candidate, int* n);
 
 /* Device bytes held by the handle. */
 int lbm_device_bytes(LbmHandle* h, int64_t* bytes);

@@ -58,7 +58,7 @@ _LIB = None
 EXPORTS = ["lbm_create", "lbm_init_fields", "lbm_set_body_force", "lbm_step",
            "lbm_step_ex", "lbm_get_moments", "lbm_residual", "lbm_conservation",
            "lbm_get_populations", "lbm_set_populations", "lbm_time",
-           "lbm_kernel_launches", "lbm_kernel_variant", "lbm_device_bytes", "lbm_time_steps",
+           "lbm_kernel_launches", "lbm_kernel_variant", "lbm_tuning", "lbm_device_bytes", "lbm_time_steps",
            "lbm_synchronize", "lbm_last_error", "lbm_destroy"]
 
 
@@ -92,7 +92,8 @@ def load(build=True):
         "lbm_time": [P, ctypes.POINTER(i64)],
         "lbm_kernel_launches": [P, ctypes.POINTER(i64)],
         "lbm_device_bytes": [P, ctypes.POINTER(i64)],
-        "lbm_kernel_variant": [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
+        "lbm_kernel_variant": [P, ctypes.POINTER(ctypes.c_int)],
+        "lbm_tuning": [P, dbl, ctypes.POINTER(ctypes.c_int)],
         "lbm_time_steps": [P, i64, dbl],
         "lbm_synchronize": [P, ctypes.c_double],
         "lbm_destroy": [P],

@@ -87,33 +87,47 @@ struct Kernels {
     return dim3((g.nx + kStepBlock - 1) / kStepBlock, g.ny);
   }
   template <int COLL, int FORC>
-  static cudaError_t step_t(const StepArgs& a, Variant v, cudaStream_t s) {
-    const dim3 grid = step_grid(a.g, v);
+  static cudaError_t step_t(const StepArgs& a, Variant v, int sms, cudaStream_t s) {
+    const dim3 grid = step_grid(a.g, v, sms, sizeof(S));
     if constexpr (Store<S>::shifted) {
+      if (v.kind == 2) {
+        if (v.stages < 1 || v.stages > 8) return cudaErrorInvalidValue;
+        const int smem = v.stages * tma_stage_bytes(sizeof(S));
+        static int configured = 0;   // bytes the attribute was last raised to
+        if (smem > configured) {
+          cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<S, COLL, FORC>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+          if (e != cudaSuccess) return e;
+          configured = smem;
+        }
+        step_tma_kernel<S, COLL, FORC><<<grid, v.block, smem, s>>>(a, v.stages);
+        return cudaGetLastError();
+      }
       constexpr int V1 = sizeof(S) == 4 ? 4 : 8;
       constexpr int V2 = sizeof(S) == 4 ? 2 : 4;
-      if (v.vec == V1) {
+      if (v.kind == 1 && v.vec == V1) {
         step_vec_kernel<S, V1, COLL, FORC><<<grid, v.block, 0, s>>>(a);
         return cudaGetLastError();
       }
-      if (v.vec == V2) {
+      if (v.kind == 1 && v.vec == V2) {
         step_vec_kernel<S, V2, COLL, FORC><<<grid, v.block, 0, s>>>(a);
         return cudaGetLastError();
       }
     }
-    if (v.vec != 1) return cudaErrorInvalidValue;
+    if (v.kind != 0) return cudaErrorInvalidValue;
     step_kernel<S, COLL, FORC><<<grid, v.block, 0, s>>>(a);
     return cudaGetLastError();
   }
-  static cudaError_t step(int coll, int forc, const StepArgs& a, Variant v, cudaStream_t s) {
+  static cudaError_t step(int coll, int forc, const StepArgs& a, Variant v, int sms,
+                          cudaStream_t s) {
     if (coll == 0) {
-      if (forc == 0) return step_t<0, 0>(a, v, s);
-      if (forc == 1) return step_t<0, 1>(a, v, s);
-      return step_t<0, 2>(a, v, s);
+      if (forc == 0) return step_t<0, 0>(a, v, sms, s);
+      if (forc == 1) return step_t<0, 1>(a, v, sms, s);
+      return step_t<0, 2>(a, v, sms, s);
     }
-    if (forc == 0) return step_t<1, 0>(a, v, s);
-    if (forc == 1) return step_t<1, 1>(a, v, s);
-    return step_t<1, 2>(a, v, s);
+    if (forc == 0) return step_t<1, 0>(a, v, sms, s);
+    if (forc == 1) return step_t<1, 1>(a, v, sms, s);
+    return step_t<1, 2>(a, v, sms, s);
   }
   static cudaError_t init(const Geom& g, const Params& p, const double* rho,
                           const double* u, void* f, void* mr, void* mx, void* my,
@@ -155,11 +169,13 @@ struct Kernels {
     if constexpr (Store<S>::shifted) {
       constexpr int V1 = sizeof(S) == 4 ? 4 : 8;
       constexpr int V2 = sizeof(S) == 4 ? 2 : 4;
-      const Variant vs[] = {{V1, 256}, {V1, 128}, {V2, 256}, {V2, 128}, {1, 256}};
-      k.nvariants = 5;
-      for (int i = 0; i < 5; ++i) k.variants[i] = vs[i];
+      const Variant vs[] = {{2, 0, 256, 4}, {2, 0, 512, 4}, {2, 0, 256, 2}, {2, 0, 512, 2},
+                            {2, 0, 256, 3}, {1, V1, 256, 0}, {1, V1, 128, 0}, {1, V2, 256, 0},
+                            {0, 1, 256, 0}, {0, 1, 128, 0}};
+      k.nvariants = 10;
+      for (int i = 0; i < 10; ++i) k.variants[i] = vs[i];
     } else {
-      const Variant vs[] = {{1, 256}, {1, 128}, {1, 512}};
+      const Variant vs[] = {{0, 1, 256, 0}, {0, 1, 128, 0}, {0, 1, 512, 0}};
       k.nvariants = 3;
       for (int i = 0; i < 3; ++i) k.variants[i] = vs[i];
     }

@@ -67,15 +67,19 @@ struct LbmHandle {
   int64_t t = 0, launches = 0;
   cudaGraphExec_t gexec = nullptr;
   int gparity = 0;
-  lbm::Variant variant{1, 256};
+  lbm::Variant variant{0, 1, 256, 0};
+  int sms = 1;                 // multiprocessors of the device
+  int* err_host = nullptr;     // mapped pinned word the kernels set on a failed wait
+  int* err_dev = nullptr;
   bool tuned = false;
-  double tune_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  double tune_ms[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   double timeout_s = 600.0;
 
   ~LbmHandle() {
     if (gexec) cudaGraphExecDestroy(gexec);
     for (void* a : allocs) cudaFree(a);
     if (host_red) cudaFreeHost(host_red);
+    if (err_host) cudaFreeHost(err_host);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -97,7 +101,13 @@ struct LbmHandle {
     auto t0 = std::chrono::steady_clock::now();
     for (;;) {
       cudaError_t e = cudaStreamQuery(stream);
-      if (e == cudaSuccess) return LBM_OK;
+      if (e == cudaSuccess) {
+        if (err_host && *reinterpret_cast<volatile int*>(err_host) != 0) {
+          *err_host = 0;
+          return fail(LBM_ERR_TIMEOUT, "a bounded mbarrier wait in the step kernel expired");
+        }
+        return LBM_OK;
+      }
       if (e != cudaErrorNotReady)
         return fail(LBM_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e));
       double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -153,14 +163,15 @@ struct LbmHandle {
     a.uy_old = old[2];
     a.partials = partials;
     a.body = body;
+    a.err = err_dev;
     a.flags = flags;
-    LBM_CUDA(ks->step(cfg.collision, cfg.forcing, a, v, stream));
+    LBM_CUDA(ks->step(cfg.collision, cfg.forcing, a, v, sms, stream));
     if (advance) cur ^= 1;
     return LBM_OK;
   }
 
   long long nparts_of(lbm::Variant v) const {
-    const dim3 gr = lbm::step_grid(g, v);
+    const dim3 gr = lbm::step_grid(g, v, sms, ks->elem_bytes);
     return (long long)gr.x * gr.y;
   }
 
@@ -169,10 +180,11 @@ struct LbmHandle {
   int autotune() {
     tuned = true;
     if (const char* f = std::getenv("LBM_VARIANT")) {
-      int vec = 0, blk = 0;
-      if (std::sscanf(f, "%d,%d", &vec, &blk) == 2) {
+      int kind = -1, vec = 0, blk = 0, st = 0;
+      if (std::sscanf(f, "%d,%d,%d,%d", &kind, &vec, &blk, &st) == 4) {
         for (int i = 0; i < ks->nvariants; ++i)
-          if (ks->variants[i].vec == vec && ks->variants[i].block == blk) {
+          if (ks->variants[i].kind == kind && ks->variants[i].vec == vec &&
+              ks->variants[i].block == blk && ks->variants[i].stages == st) {
             variant = ks->variants[i];
             return LBM_OK;
           }
@@ -260,7 +272,8 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
                              : c.precision == LBM_FP32_SHIFTED ? &lbm::kernels_fp32()
                                                                 : &lbm::kernels_fp16();
   const int nx = c.nx, ny = c.ny;
-  const int align = 512 / ks->elem_bytes;   // one warp's row segment
+  // rows are whole TMA tiles (4096 B) for shifted storage, 512 B for FP64
+  const int align = (c.precision == LBM_FP64 ? 512 : lbm::kTmaRowBytes) / ks->elem_bytes;
   const int pitch = (nx + align - 1) / align * align;
   const long long plane = (long long)(ny + 2) * pitch;
   if (plane >= (1LL << 31) / 1)
@@ -375,6 +388,13 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   for (int i = 0; i < 3; ++i)
     if ((rc = h->alloc(&h->mom[i], plane * cb)) || (rc = h->alloc(&h->old[i], plane * cb)))
       return bail(rc);
+  e = cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, c.device);
+  if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("device attribute: ") + cudaGetErrorString(e)));
+  e = cudaHostAlloc(reinterpret_cast<void**>(&h->err_host), sizeof(int), cudaHostAllocMapped);
+  if (e != cudaSuccess) return bail(fail(LBM_ERR_ALLOC, std::string("cudaHostAlloc: ") + cudaGetErrorString(e)));
+  *h->err_host = 0;
+  e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&h->err_dev), h->err_host, 0);
+  if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaHostGetDevicePointer: ") + cudaGetErrorString(e)));
   h->variant = ks->variants[0];
   long long maxparts = ny;
   for (int i = 0; i < ks->nvariants; ++i) maxparts = std::max(maxparts, h->nparts_of(ks->variants[i]));
@@ -639,11 +659,19 @@ int lbm_kernel_launches(LbmHandle* h, int64_t* n) {
   return LBM_OK;
 }
 
-int lbm_kernel_variant(LbmHandle* h, int* nodes_per_thread, int* block_threads) {
-  if (!h || !nodes_per_thread || !block_threads)
-    return fail(LBM_ERR_ARG, "lbm_kernel_variant: null argument");
-  *nodes_per_thread = h->variant.vec;
-  *block_threads = h->variant.block;
+int lbm_kernel_variant(LbmHandle* h, int out[4]) {
+  if (!h || !out) return fail(LBM_ERR_ARG, "lbm_kernel_variant: null argument");
+  out[0] = h->variant.kind;
+  out[1] = h->variant.vec;
+  out[2] = h->variant.block;
+  out[3] = h->variant.stages;
+  return LBM_OK;
+}
+
+int lbm_tuning(LbmHandle* h, double* ms_per_candidate, int* ncandidates) {
+  if (!h || !ms_per_candidate || !ncandidates) return fail(LBM_ERR_ARG, "lbm_tuning: null argument");
+  *ncandidates = h->ks->nvariants;
+  for (int i = 0; i < h->ks->nvariants; ++i) ms_per_candidate[i] = h->tune_ms[i];
   return LBM_OK;
 }
 

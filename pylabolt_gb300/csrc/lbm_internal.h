@@ -57,24 +57,34 @@ struct StepArgs {
   void* rho_old; void* ux_old; void* uy_old;
   double* partials;      // [nblocks*8] residual partial sums
   const void* body;      // [2*plane] body force or null
+  int* err;              // device-visible error word (bounded waits)
   int flags;
 };
 
-// Launch shape of the fused step: nodes per thread (1 = scalar kernel) and
-// threads per block.
+// Launch shape of the fused step.
+//   kind 0: scalar kernel, one node per thread
+//   kind 1: vector kernel, `vec` consecutive nodes per thread
+//   kind 2: persistent TMA-pipelined kernel: tiles of one row segment of
+//           kTmaRowBytes, `stages` shared-memory stages, `block` threads
 struct Variant {
+  int kind;
   int vec;
   int block;
+  int stages;
 };
+
+constexpr int kTmaRowBytes = 4096;   // tile width in bytes of one plane row
+constexpr int kTmaHaloBytes = 16;    // TMA granule: halo on each side
+constexpr int kErrWaitTimeout = 1;   // err code: an mbarrier wait timed out
 
 // Kernels of one storage precision.
 struct KernelSet {
   int elem_bytes;        // storage bytes per population value
   int compute_bytes;     // bytes per moment value
   cudaError_t (*step)(int collision, int forcing, const StepArgs& a, Variant v,
-                      cudaStream_t s);
+                      int sms, cudaStream_t s);
   int nvariants;             // candidate launch shapes for the autotuner
-  Variant variants[8];
+  Variant variants[12];
   // f_eq(rho,u) into storage on fluid nodes (zeros on solids); moments get
   // rho/u on every node.  rho [plane], u [2][plane], FP64, device order.
   cudaError_t (*init)(const Geom& g, const Params& p, const double* rho,
@@ -103,8 +113,23 @@ const KernelSet& kernels_fp16();
 constexpr int kFinishBlocks = 128;
 cudaError_t finish_reduce(const double* partials, long long nrows, double* scratch,
                           double* out8, cudaStream_t s);
-// grid of the fused step for variant v
-inline dim3 step_grid(const Geom& g, Variant v) {
+// Shared memory of one TMA stage (nine halo-padded row windows).
+inline int tma_stage_bytes(int elem_bytes) {
+  return 9 * (kTmaRowBytes + 2 * kTmaHaloBytes);
+}
+// Number of SMs of the current device (cached by the caller's handle).
+// grid of the fused step for variant v (`sms` multiprocessors)
+inline dim3 step_grid(const Geom& g, Variant v, int sms, int elem_bytes) {
+  if (v.kind == 2) {
+    const long long tiles = (long long)g.ny * (g.pitch / (kTmaRowBytes / elem_bytes));
+    const int smem = v.stages * tma_stage_bytes(elem_bytes) + 1024;
+    int per_sm = (227 * 1024) / smem;
+    if (per_sm * v.block > 2048) per_sm = 2048 / v.block;
+    if (per_sm < 1) per_sm = 1;
+    long long blocks = (long long)sms * per_sm;
+    if (blocks > tiles) blocks = tiles;
+    return dim3((unsigned)blocks, 1);
+  }
   const long long per_block = (long long)v.block * v.vec;
   return dim3((unsigned)((g.pitch + per_block - 1) / per_block), (unsigned)g.ny);
 }

@@ -627,6 +627,188 @@ __global__ void __launch_bounds__(256) step_vec_kernel(const StepArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Persistent TMA-pipelined kernel (shifted storage).
+//
+// Work is split into tiles: one row y and a segment of W = kTmaRowBytes bytes
+// of every population plane.  For a tile, thread 0 issues nine bulk copies
+// (cp.async.bulk, one per direction k) of the source row y - c_ky over
+// [x0 - H, x0 + W + H) into one shared-memory stage and arms the stage's
+// mbarrier with the byte count; the block then reads each node's nine
+// incoming populations from shared memory at offset x - x0 + H - c_kx.  The
+// ring of `stages` stages keeps stages-1 tiles of loads in flight while the
+// block computes, without holding them in registers.  Stores go straight to
+// global memory (each warp writes 32 consecutive nodes per direction).
+// Every mbarrier wait is bounded in wall-clock time; on expiry the kernel
+// records kErrWaitTimeout, waits (bounded) for its own copies and returns.
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Waits for `parity` of the barrier; false after ~1 s (then *err is set).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, int* err) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  while (!mbar_try_wait(bar, parity)) {
+    if (global_ns() - t0 > 1000000000ull) {
+      atomicExch(err, kErrWaitTimeout);
+      return false;
+    }
+  }
+  return true;
+}
+
+template <class S>
+__device__ __forceinline__ float smem_ld(const S* p, const Params& q);
+template <>
+__device__ __forceinline__ float smem_ld<float>(const float* p, const Params&) { return *p; }
+template <>
+__device__ __forceinline__ float smem_ld<__half>(const __half* p, const Params& q) {
+  return __half2float(*p) * float(q.inv_scale);
+}
+
+template <class S, int COLL, int FORC>
+__global__ void __launch_bounds__(512) step_tma_kernel(const StepArgs a, int stages) {
+  static_assert(Store<S>::shifted, "TMA kernel is for shifted storage");
+  constexpr int W = kTmaRowBytes / sizeof(S);       // nodes per tile
+  constexpr int H = kTmaHaloBytes / sizeof(S);      // halo elements
+  constexpr int RW = W + 2 * H;                     // row window elements
+  constexpr uint32_t kCopyBytes = RW * sizeof(S);
+  constexpr uint32_t kStageBytes = 9 * kCopyBytes;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long bars[8];
+  const Geom& g = a.g;
+  const Params& p = a.p;
+  const int tiles_per_row = g.pitch / W;
+  const long long ntiles = (long long)g.ny * tiles_per_row;
+  const bool nopull = (a.flags & F_NOPULL) != 0;
+  const S* __restrict__ fin = static_cast<const S*>(a.fin);
+  S* __restrict__ fout = static_cast<S*>(a.fout);
+  double red[7] = {0, 0, 0, 0, 0, 0, 0};
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < stages; ++s) mbar_init(smem_u32(&bars[s]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  auto issue = [&](long long tile, int s) {
+    const int y = (int)(tile / tiles_per_row);
+    const int x0 = (int)(tile % tiles_per_row) * W;
+    const uint32_t bar = smem_u32(&bars[s]);
+    mbar_expect_tx(bar, kStageBytes);
+    const uint32_t dst0 = smem_u32(smem_raw + (size_t)s * kStageBytes);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const int dy = nopull ? 0 : CYk(k);
+      const S* src = fin + k * g.plane + g.node(x0, y) - (long long)dy * g.pitch - H;
+      bulk_g2s(dst0 + k * kCopyBytes, src, kCopyBytes, bar);
+    }
+  };
+
+  // prologue: fill the ring (thread 0 counts the tiles it has issued)
+  long long issued = 0;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < stages; ++s) {
+      const long long t = blockIdx.x + (long long)s * gridDim.x;
+      if (t < ntiles) {
+        issue(t, s);
+        ++issued;
+      }
+    }
+  }
+
+  bool ok = true;
+  long long it = 0;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+    const int s = (int)(it % stages);
+    const uint32_t parity = (uint32_t)((it / stages) & 1);
+    const bool got = mbar_wait_bounded(smem_u32(&bars[s]), parity, a.err);
+    if (__syncthreads_or(!got)) {  // the whole block leaves together
+      ok = false;
+      break;
+    }
+    const S* stage = reinterpret_cast<const S*>(smem_raw + (size_t)s * kStageBytes);
+    const int y = (int)(tile / tiles_per_row);
+    const int x0 = (int)(tile % tiles_per_row) * W;
+    for (int xl = threadIdx.x; xl < W; xl += blockDim.x) {
+      const int x = x0 + xl;
+      if (x >= g.nx) continue;
+      const long long n = g.node(x, y);
+      int cls = 0;
+      if (g.segflag[y * g.nseg + (x >> 5)]) cls = g.cls[n];
+      if (cls == 2) continue;
+      float f[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        const int dx = nopull ? 0 : CXk(k);
+        f[k] = smem_ld<S>(stage + k * RW + xl + H - dx, p);
+      }
+      int r = -1;
+      if (cls == 1) {
+        r = g.recmap[n];
+        if (!nopull) special_links<S>(f, a, fin, n, r);
+      }
+      float rho, ux, uy;
+      node_update<S, COLL, FORC>(f, a, n, rho, ux, uy);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Store<S>::st(fout, k * g.plane + n, f[k], p);
+      node_outputs<float>(a, n, r, rho, ux, uy, red);
+    }
+    __syncthreads();  // every thread is done reading stage s
+    if (threadIdx.x == 0) {
+      const long long next = tile + (long long)stages * gridDim.x;
+      if (next < ntiles) {
+        issue(next, s);
+        ++issued;
+      }
+    }
+  }
+  if (!ok && threadIdx.x == 0) {
+    // drain the copies still in flight (iterations it .. issued-1), bounded,
+    // so no bulk copy lands in shared memory after the block has left
+    for (long long j = it; j < issued; ++j) {
+      const uint32_t bar = smem_u32(&bars[j % stages]);
+      const uint32_t par = (uint32_t)((j / stages) & 1);
+      const unsigned long long t0 = global_ns();
+      while (!mbar_try_wait(bar, par) && global_ns() - t0 < 1000000000ull) {
+      }
+    }
+  }
+  __syncthreads();
+  if (a.flags & F_RESIDUAL) block_residual(a, red);
+}
+
+// ---------------------------------------------------------------------------
 // Initial equilibrium -- equilibrium_kernels.py:38-78.  rho/u are FP64 device
 // arrays in device order; moments (compute type) receive rho/u on every node.
 template <class S>

@@ -148,10 +148,19 @@ class FluidLBM:
 
     @property
     def kernel_variant(self):
-        """(nodes per thread, threads per block) of the fused step."""
-        v, b = ctypes.c_int(), ctypes.c_int()
-        check(self.lib.lbm_kernel_variant(self.h, ctypes.byref(v), ctypes.byref(b)))
-        return v.value, b.value
+        """(kind, nodes per thread, threads per block, stages) of the fused
+        step; kind 0 scalar, 1 vector, 2 TMA pipeline."""
+        out = (ctypes.c_int * 4)()
+        check(self.lib.lbm_kernel_variant(self.h, out))
+        return tuple(out[:])
+
+    @property
+    def tuning(self):
+        """Mean step time (ms) of every autotuner candidate."""
+        out = (ctypes.c_double * 12)()
+        n = ctypes.c_int()
+        check(self.lib.lbm_tuning(self.h, out, ctypes.byref(n)))
+        return list(out[:n.value])
 
     @property
     def device_bytes(self):

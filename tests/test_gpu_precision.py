@@ -27,7 +27,7 @@ MRT_ATOL = 1e-13
 def _run(case, storage, steps, variant=None):
     old = os.environ.get("LBM_VARIANT")
     if variant:
-        os.environ["LBM_VARIANT"] = f"{variant[0]},{variant[1]}"
+        os.environ["LBM_VARIANT"] = ",".join(str(v) for v in variant)
     try:
         with FluidLBM(case, storage=storage) as sim:
             sim.initialize()
@@ -59,10 +59,21 @@ def test_shifted_storage_error_vs_fp64(name):
     assert _rel(u16, u64, fluid) <= FP16_U_TOL
 
 
+# (kind, nodes per thread, threads per block, stages): every autotuner candidate
+SHIFTED_VARIANTS = {
+    "fp32_shifted": [(2, 0, 256, 4), (2, 0, 512, 4), (2, 0, 256, 2), (2, 0, 512, 2),
+                     (2, 0, 256, 3), (1, 4, 256, 0), (1, 4, 128, 0), (1, 2, 256, 0),
+                     (0, 1, 256, 0), (0, 1, 128, 0)],
+    "fp16_shifted": [(2, 0, 256, 4), (2, 0, 512, 4), (2, 0, 256, 2), (2, 0, 512, 2),
+                     (2, 0, 256, 3), (1, 8, 256, 0), (1, 8, 128, 0), (1, 4, 256, 0),
+                     (0, 1, 256, 0), (0, 1, 128, 0)],
+}
+
+
 @pytest.mark.parametrize("storage,variants", [
-    ("fp64", [(1, 256), (1, 128), (1, 512)]),
-    ("fp32_shifted", [(4, 256), (4, 128), (2, 256), (2, 128), (1, 256)]),
-    ("fp16_shifted", [(8, 256), (8, 128), (4, 256), (4, 128), (1, 256)])])
+    ("fp64", [(0, 1, 256, 0), (0, 1, 128, 0), (0, 1, 512, 0)]),
+    ("fp32_shifted", SHIFTED_VARIANTS["fp32_shifted"]),
+    ("fp16_shifted", SHIFTED_VARIANTS["fp16_shifted"])])
 def test_every_launch_shape_agrees(storage, variants):
     """The autotuner may pick any candidate: all must give the same result
     (FP64 bit for bit; shifted storage within one rounding per step)."""

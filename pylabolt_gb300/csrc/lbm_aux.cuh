@@ -115,7 +115,12 @@ struct Kernels {
       }
     }
     if (v.kind != 0) return cudaErrorInvalidValue;
-    step_kernel<S, COLL, FORC><<<grid, v.block, 0, s>>>(a);
+    if (v.stages == 1) {
+      if (v.block > 256) return cudaErrorInvalidValue;
+      step_kernel<S, COLL, FORC, 1><<<grid, v.block, 0, s>>>(a);
+    } else {
+      step_kernel<S, COLL, FORC, 0><<<grid, v.block, 0, s>>>(a);
+    }
     return cudaGetLastError();
   }
   static cudaError_t step(int coll, int forc, const StepArgs& a, Variant v, int sms,
@@ -169,13 +174,15 @@ struct Kernels {
     if constexpr (Store<S>::shifted) {
       constexpr int V1 = sizeof(S) == 4 ? 4 : 8;
       constexpr int V2 = sizeof(S) == 4 ? 2 : 4;
-      const Variant vs[] = {{2, 0, 256, 4}, {2, 0, 512, 4}, {2, 0, 256, 2}, {2, 0, 512, 2},
-                            {2, 0, 256, 3}, {1, V1, 256, 0}, {1, V1, 128, 0}, {1, V2, 256, 0},
-                            {0, 1, 256, 0}, {0, 1, 128, 0}};
-      k.nvariants = 10;
-      for (int i = 0; i < 10; ++i) k.variants[i] = vs[i];
+      // kind 2: {threads, stages}; kind 1: {nodes per thread, threads};
+      // kind 0: {threads, register cap}
+      const Variant vs[] = {{2, 0, 256, 4}, {2, 0, 512, 3}, {2, 0, 512, 2}, {2, 0, 1024, 2},
+                            {2, 0, 256, 2}, {1, V1, 256, 0}, {1, V2, 256, 0}, {0, 1, 128, 0},
+                            {0, 1, 256, 0}, {0, 1, 128, 1}, {0, 1, 256, 1}};
+      k.nvariants = 11;
+      for (int i = 0; i < 11; ++i) k.variants[i] = vs[i];
     } else {
-      const Variant vs[] = {{0, 1, 256, 0}, {0, 1, 128, 0}, {0, 1, 512, 0}};
+      const Variant vs[] = {{0, 1, 128, 0}, {0, 1, 256, 0}, {0, 1, 512, 0}};
       k.nvariants = 3;
       for (int i = 0; i < 3; ++i) k.variants[i] = vs[i];
     }

@@ -194,7 +194,7 @@ struct LbmHandle {
     variant = ks->variants[0];
     const char* t = std::getenv("LBM_TUNE");
     if (t && t[0] == '0') return LBM_OK;
-    const int flags = nopull ? lbm::F_NOPULL : 0;
+    const int flags = 0;
     cudaEvent_t e0, e1;
     LBM_CUDA(cudaEventCreate(&e0));
     LBM_CUDA(cudaEventCreate(&e1));
@@ -450,6 +450,18 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   p.s_nu = c.mrt_s[3];
   p.scale = c.precision == LBM_FP16_SHIFTED ? c.fp16_scale : 1.0;
   p.inv_scale = 1.0 / p.scale;
+  {
+    const double w[3] = {4.0 / 9.0, 1.0 / 9.0, 1.0 / 36.0};
+    p.f_om1 = (float)(1.0 - c.omega);
+    for (int i = 0; i < 3; ++i) {
+      p.f_q[i] = (float)(c.omega * w[i] * p.scale);
+      p.f_omh[i] = (float)((1.0 - 0.5 * c.omega) * w[i] * p.scale);
+    }
+    p.f_gx = (float)p.gx;
+    p.f_gy = (float)p.gy;
+    p.f_scale = (float)p.scale;
+    p.f_inv_scale = (float)p.inv_scale;
+  }
   if (c.body_force_field) {
     if ((rc = h->alloc(&h->body, 2 * plane * cb))) return bail(rc);
     if ((e = cudaMemsetAsync(h->body, 0, 2 * plane * cb, h->stream)) != cudaSuccess)
@@ -532,11 +544,12 @@ int lbm_step_ex(LbmHandle* h, int64_t nsteps, int flags) {
     h->launches += 1;
     return LBM_OK;
   };
-  if (!h->tuned && (rc = h->autotune())) return rc;
   if (h->nopull) {
     if ((rc = one(lbm::F_NOPULL | (nsteps == 1 ? kflags : 0)))) return rc;
     s = 1;
   }
+  // tune on the steady (pulling) step, which all later steps use
+  if (!h->tuned && !h->nopull && s < nsteps && (rc = h->autotune())) return rc;
   int64_t plain = nsteps - s - (s < nsteps ? 1 : 0);
   while (plain > 0) {
     if (plain >= kGraphChunk && !std::getenv("LBM_NO_GRAPH")) {

@@ -62,6 +62,9 @@ template <class S> struct Store;
 template <> struct Store<double> {
   using T = double;
   static constexpr bool shifted = false;
+  static constexpr bool scaled = false;
+  __device__ static __forceinline__ T ldr(const double* __restrict__ p, long long i) { return p[i]; }
+  __device__ static __forceinline__ void str(double* __restrict__ p, long long i, T v) { p[i] = v; }
   __device__ static __forceinline__ T ld(const double* __restrict__ p, long long i, const Params&) {
     return p[i];
   }
@@ -72,6 +75,9 @@ template <> struct Store<double> {
 template <> struct Store<float> {
   using T = float;
   static constexpr bool shifted = true;
+  static constexpr bool scaled = false;
+  __device__ static __forceinline__ T ldr(const float* __restrict__ p, long long i) { return p[i]; }
+  __device__ static __forceinline__ void str(float* __restrict__ p, long long i, T v) { p[i] = v; }
   __device__ static __forceinline__ T ld(const float* __restrict__ p, long long i, const Params&) {
     return p[i];
   }
@@ -79,9 +85,18 @@ template <> struct Store<float> {
     p[i] = v;
   }
 };
+// FP16 stores g * scale; ldr/str move the stored (scaled) value, ld/st the
+// physical g.
 template <> struct Store<__half> {
   using T = float;
   static constexpr bool shifted = true;
+  static constexpr bool scaled = true;
+  __device__ static __forceinline__ T ldr(const __half* __restrict__ p, long long i) {
+    return __half2float(p[i]);
+  }
+  __device__ static __forceinline__ void str(__half* __restrict__ p, long long i, T v) {
+    p[i] = __float2half_rn(v);
+  }
   __device__ static __forceinline__ T ld(const __half* __restrict__ p, long long i, const Params& q) {
     return __half2float(p[i]) * float(q.inv_scale);
   }
@@ -166,6 +181,45 @@ __device__ __forceinline__ T bgk_shift_k(T gk, T rho, T drho, T ux, T uy,
     out += omh * (w * (ex * Fx + ey * Fy));
   }
   return out;
+}
+
+// Shifted BGK on stored values G = scale * g (scale 1 for FP32 storage),
+// written over the opposite-direction pairs (k, kbar): with
+// A = drho - 1.5 rho u^2 and C = 3 rho (c_k . u), the equilibrium deviations are
+// g_eq,k = w (A + 1.5 C (c_k . u) + C) and g_eq,kbar = w (A + 1.5 C (c_k . u) - C);
+// g* = (1 - omega) g + omega g_eq (+ (1 - omega/2) Guo source, split the same
+// way into its even and odd parts).
+template <int FORC>
+__device__ __forceinline__ void bgk_shift_pairs(float G[9], float rho, float drho, float ux,
+                                                float uy, float Fx, float Fy, const Params& p) {
+  const float om1 = p.f_om1;
+  const float A = drho - 1.5f * rho * (ux * ux + uy * uy);
+  const float r3 = 3.f * rho;
+  G[0] = om1 * G[0] + p.f_q[0] * A;
+  const float cus[4] = {ux, uy, ux + uy, uy - ux};
+  const int ks[4] = {1, 2, 5, 6};
+  const int kbs[4] = {3, 4, 7, 8};
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float q = p.f_q[j < 2 ? 1 : 2];
+    const float C = r3 * cus[j];
+    const float S = A + 1.5f * C * cus[j];
+    G[ks[j]] = om1 * G[ks[j]] + q * (S + C);
+    G[kbs[j]] = om1 * G[kbs[j]] + q * (S - C);
+  }
+  if (FORC != 0) {
+    const float cfs[4] = {Fx, Fy, Fx + Fy, Fy - Fx};
+    const float uF = ux * Fx + uy * Fy;
+    if (FORC == 2) G[0] += p.f_omh[0] * (-3.f * uF);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float h = p.f_omh[j < 2 ? 1 : 2];
+      const float O = 3.f * cfs[j];
+      const float E = FORC == 2 ? 9.f * cus[j] * cfs[j] - 3.f * uF : 0.f;
+      G[ks[j]] += h * (E + O);
+      G[kbs[j]] += h * (E - O);
+    }
+  }
 }
 
 // MRT (project definition; the reference declares MRT without a kernel,
@@ -306,30 +360,48 @@ __device__ __forceinline__ void node_update(typename Store<S>::T f[9], const Ste
   const Params& p = a.p;
   T drho, jx, jy;
   moments<SH>(f, rho, drho, jx, jy);
+  if constexpr (Store<S>::scaled) {
+    // f holds G = scale * g: rescale the moments only
+    drho *= p.f_inv_scale;
+    jx *= p.f_inv_scale;
+    jy *= p.f_inv_scale;
+    rho = T(1) + drho;
+  }
   T Fx = T(0), Fy = T(0);
   if (FORC != 0) {
     if (a.body) {
       const T* body = static_cast<const T*>(a.body);
       Fx = body[n];
       Fy = body[a.g.plane + n];
+    } else if constexpr (SH) {
+      Fx = rho * p.f_gx;
+      Fy = rho * p.f_gy;
     } else {
       Fx = rho * T(p.gx);
       Fy = rho * T(p.gy);
     }
   }
-  if (!SH) {
+  if constexpr (!SH) {
     // compute_fields_kernels.py:61-65
     const T inv_density = T(1) / (rho + T(p.eps));
     ux = jx * inv_density + (T(0.5) * Fx) * inv_density;
     uy = jy * inv_density + (T(0.5) * Fy) * inv_density;
   } else {
-    const T inv_density = T(1) / rho;
+    const T inv_density = __frcp_rn(rho);
     ux = (jx + T(0.5) * Fx) * inv_density;
     uy = (jy + T(0.5) * Fy) * inv_density;
   }
-  if (COLL == 1) {
+  if constexpr (COLL == 1) {
+    if constexpr (Store<S>::scaled) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) f[k] *= p.f_inv_scale;
+    }
     mrt_collide<FORC, SH>(f, rho, drho, ux, uy, Fx, Fy, p);
-  } else if (!SH) {
+    if constexpr (Store<S>::scaled) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) f[k] *= p.f_scale;
+    }
+  } else if constexpr (!SH) {
     const T hu2 = T(p.half_inv_cs_2) * (ux * ux + uy * uy);
     f[0] = bgk_ref_k<0, FORC>(f[0], rho, ux, uy, hu2, Fx, Fy, p);
     f[1] = bgk_ref_k<1, FORC>(f[1], rho, ux, uy, hu2, Fx, Fy, p);
@@ -341,17 +413,7 @@ __device__ __forceinline__ void node_update(typename Store<S>::T f[9], const Ste
     f[7] = bgk_ref_k<7, FORC>(f[7], rho, ux, uy, hu2, Fx, Fy, p);
     f[8] = bgk_ref_k<8, FORC>(f[8], rho, ux, uy, hu2, Fx, Fy, p);
   } else {
-    const T u2 = ux * ux + uy * uy;
-    const T om = T(p.omega), omh = T(p.one_m_half_omega);
-    f[0] = bgk_shift_k<0, FORC>(f[0], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-    f[1] = bgk_shift_k<1, FORC>(f[1], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-    f[2] = bgk_shift_k<2, FORC>(f[2], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-    f[3] = bgk_shift_k<3, FORC>(f[3], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-    f[4] = bgk_shift_k<4, FORC>(f[4], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-    f[5] = bgk_shift_k<5, FORC>(f[5], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-    f[6] = bgk_shift_k<6, FORC>(f[6], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-    f[7] = bgk_shift_k<7, FORC>(f[7], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
-    f[8] = bgk_shift_k<8, FORC>(f[8], rho, drho, ux, uy, u2, Fx, Fy, om, omh);
+    bgk_shift_pairs<FORC>(f, rho, drho, ux, uy, Fx, Fy, p);
   }
 }
 
@@ -369,6 +431,10 @@ __device__ __forceinline__ void special_links(typename Store<S>::T f[9], const S
   f[6] = special_link<6, S>(a.g, a.p, fin, n, r, side);
   f[7] = special_link<7, S>(a.g, a.p, fin, n, r, side);
   f[8] = special_link<8, S>(a.g, a.p, fin, n, r, side);
+  if constexpr (Store<S>::scaled) {
+#pragma unroll
+    for (int k = 1; k < 9; ++k) f[k] *= a.p.f_scale;
+  }
 }
 
 // Side data, moment output and residual terms of one updated node.
@@ -428,8 +494,9 @@ __device__ __forceinline__ void block_residual(const StepArgs& a, double red[7])
 // ---------------------------------------------------------------------------
 // Scalar kernel: one node per thread.  Used for FP64 (whose cost is its FP64
 // arithmetic, not memory) and as an autotuner candidate.
-template <class S, int COLL, int FORC>
-__global__ void __launch_bounds__(512) step_kernel(const StepArgs a) {
+// CAP = 1 asks for 8 resident blocks of 256 threads (at most 32 registers).
+template <class S, int COLL, int FORC, int CAP>
+__global__ void __launch_bounds__(CAP ? 256 : 512, CAP ? 8 : 1) step_kernel(const StepArgs a) {
   using T = typename Store<S>::T;
   const Geom& g = a.g;
   const Params& p = a.p;
@@ -449,19 +516,19 @@ __global__ void __launch_bounds__(512) step_kernel(const StepArgs a) {
       if (cls == 1) r = g.recmap[n];
       if (a.flags & F_NOPULL) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) f[k] = Store<S>::ld(fin, k * g.plane + n, p);
+        for (int k = 0; k < 9; ++k) f[k] = Store<S>::ldr(fin, k * g.plane + n);
       } else if (cls == 0) {
 #pragma unroll
         for (int k = 0; k < 9; ++k)
-          f[k] = Store<S>::ld(fin, k * g.plane + n - CYk(k) * g.pitch - CXk(k), p);
+          f[k] = Store<S>::ldr(fin, k * g.plane + n - CYk(k) * g.pitch - CXk(k));
       } else {
-        f[0] = Store<S>::ld(fin, n, p);
+        f[0] = Store<S>::ldr(fin, n);
         special_links<S>(f, a, fin, n, r);
       }
       T rho, ux, uy;
       node_update<S, COLL, FORC>(f, a, n, rho, ux, uy);
 #pragma unroll
-      for (int k = 0; k < 9; ++k) Store<S>::st(fout, k * g.plane + n, f[k], p);
+      for (int k = 0; k < 9; ++k) Store<S>::str(fout, k * g.plane + n, f[k]);
       node_outputs<T>(a, n, r, rho, ux, uy, red);
     }
   }
@@ -492,8 +559,7 @@ template <int V> struct VecIO<float, V> {
 };
 template <int V> struct VecIO<__half, V> {
   static_assert(V == 4 || V == 8, "half vectors of 4 or 8");
-  __device__ static __forceinline__ void load(const __half* __restrict__ p, float (&out)[V], const Params& q) {
-    const float s = float(q.inv_scale);
+  __device__ static __forceinline__ void load(const __half* __restrict__ p, float (&out)[V], const Params&) {
     uint32_t w[V / 2];
     if constexpr (V == 8) {
       const uint4 raw = __ldg(reinterpret_cast<const uint4*>(p));
@@ -507,19 +573,18 @@ template <int V> struct VecIO<__half, V> {
       __half2 h;
       memcpy(&h, &w[i], 4);
       const float2 t = __half22float2(h);
-      out[2 * i] = t.x * s;
-      out[2 * i + 1] = t.y * s;
+      out[2 * i] = t.x;
+      out[2 * i + 1] = t.y;
     }
   }
-  __device__ static __forceinline__ float ld1(const __half* __restrict__ p, const Params& q) {
-    return __half2float(p[0]) * float(q.inv_scale);
+  __device__ static __forceinline__ float ld1(const __half* __restrict__ p, const Params&) {
+    return __half2float(p[0]);
   }
-  __device__ static __forceinline__ void store(__half* __restrict__ p, const float (&in)[V], const Params& q) {
-    const float s = float(q.scale);
+  __device__ static __forceinline__ void store(__half* __restrict__ p, const float (&in)[V], const Params&) {
     uint32_t w[V / 2];
 #pragma unroll
     for (int i = 0; i < V / 2; ++i) {
-      const __half2 h = __floats2half2_rn(in[2 * i] * s, in[2 * i + 1] * s);
+      const __half2 h = __floats2half2_rn(in[2 * i], in[2 * i + 1]);
       memcpy(&w[i], &h, 4);
     }
     if constexpr (V == 8)
@@ -692,12 +757,12 @@ __device__ __forceinline__ float smem_ld(const S* p, const Params& q);
 template <>
 __device__ __forceinline__ float smem_ld<float>(const float* p, const Params&) { return *p; }
 template <>
-__device__ __forceinline__ float smem_ld<__half>(const __half* p, const Params& q) {
-  return __half2float(*p) * float(q.inv_scale);
+__device__ __forceinline__ float smem_ld<__half>(const __half* p, const Params&) {
+  return __half2float(*p);
 }
 
 template <class S, int COLL, int FORC>
-__global__ void __launch_bounds__(512) step_tma_kernel(const StepArgs a, int stages) {
+__global__ void __launch_bounds__(1024) step_tma_kernel(const StepArgs a, int stages) {
   static_assert(Store<S>::shifted, "TMA kernel is for shifted storage");
   constexpr int W = kTmaRowBytes / sizeof(S);       // nodes per tile
   constexpr int H = kTmaHaloBytes / sizeof(S);      // halo elements
@@ -781,7 +846,7 @@ __global__ void __launch_bounds__(512) step_tma_kernel(const StepArgs a, int sta
       float rho, ux, uy;
       node_update<S, COLL, FORC>(f, a, n, rho, ux, uy);
 #pragma unroll
-      for (int k = 0; k < 9; ++k) Store<S>::st(fout, k * g.plane + n, f[k], p);
+      for (int k = 0; k < 9; ++k) Store<S>::str(fout, k * g.plane + n, f[k]);
       node_outputs<float>(a, n, r, rho, ux, uy, red);
     }
     __syncthreads();  // every thread is done reading stage s

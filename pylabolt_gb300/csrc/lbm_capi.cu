@@ -452,9 +452,9 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   p.inv_scale = 1.0 / p.scale;
   {
     const double w[3] = {4.0 / 9.0, 1.0 / 9.0, 1.0 / 36.0};
-    p.f_om1 = (float)(1.0 - c.omega);
+    p.f_omega = (float)c.omega;
     for (int i = 0; i < 3; ++i) {
-      p.f_q[i] = (float)(c.omega * w[i] * p.scale);
+      p.f_wsc[i] = (float)(w[i] * p.scale);
       p.f_omh[i] = (float)((1.0 - 0.5 * c.omega) * w[i] * p.scale);
     }
     p.f_gx = (float)p.gx;

@@ -37,8 +37,8 @@ struct Params {
   double s_e, s_eps, s_q, s_nu;
   double scale, inv_scale;   // FP16 storage scale
   // FP32 constants of the shifted-storage collision (scale = storage scale)
-  float f_om1;               // 1 - omega
-  float f_q[3];              // omega * w * scale for |c|^2 = 0, 1, 2
+  float f_omega;             // omega
+  float f_wsc[3];            // w * scale for |c|^2 = 0, 1, 2
   float f_omh[3];            // (1 - omega/2) * w * scale for |c|^2 = 0, 1, 2
   float f_gx, f_gy, f_scale, f_inv_scale;
 };

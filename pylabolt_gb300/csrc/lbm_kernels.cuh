@@ -186,26 +186,28 @@ __device__ __forceinline__ T bgk_shift_k(T gk, T rho, T drho, T ux, T uy,
 // Shifted BGK on stored values G = scale * g (scale 1 for FP32 storage),
 // written over the opposite-direction pairs (k, kbar): with
 // A = drho - 1.5 rho u^2 and C = 3 rho (c_k . u), the equilibrium deviations are
-// g_eq,k = w (A + 1.5 C (c_k . u) + C) and g_eq,kbar = w (A + 1.5 C (c_k . u) - C);
-// g* = (1 - omega) g + omega g_eq (+ (1 - omega/2) Guo source, split the same
-// way into its even and odd parts).
+// g_eq,k = w (A + 1.5 C (c_k . u) + C) and g_eq,kbar = w (A + 1.5 C (c_k . u) - C).
+// The update is g* = g + omega (g_eq - g): adding the small relaxation term to
+// g rounds far less than (1 - omega) g + omega g_eq, whose two large products
+// drift the FP32 state over long runs.  The Guo source (times 1 - omega/2) is
+// split the same way into its even and odd parts.
 template <int FORC>
 __device__ __forceinline__ void bgk_shift_pairs(float G[9], float rho, float drho, float ux,
                                                 float uy, float Fx, float Fy, const Params& p) {
-  const float om1 = p.f_om1;
+  const float om = p.f_omega;
   const float A = drho - 1.5f * rho * (ux * ux + uy * uy);
   const float r3 = 3.f * rho;
-  G[0] = om1 * G[0] + p.f_q[0] * A;
+  G[0] += om * (p.f_wsc[0] * A - G[0]);
   const float cus[4] = {ux, uy, ux + uy, uy - ux};
   const int ks[4] = {1, 2, 5, 6};
   const int kbs[4] = {3, 4, 7, 8};
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    const float q = p.f_q[j < 2 ? 1 : 2];
+    const float q = p.f_wsc[j < 2 ? 1 : 2];
     const float C = r3 * cus[j];
     const float S = A + 1.5f * C * cus[j];
-    G[ks[j]] = om1 * G[ks[j]] + q * (S + C);
-    G[kbs[j]] = om1 * G[kbs[j]] + q * (S - C);
+    G[ks[j]] += om * (q * (S + C) - G[ks[j]]);
+    G[kbs[j]] += om * (q * (S - C) - G[kbs[j]]);
   }
   if (FORC != 0) {
     const float cfs[4] = {Fx, Fy, Fx + Fy, Fy - Fx};

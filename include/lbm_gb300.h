@@ -183,6 +183,43 @@ int lbm_time_steps(LbmHandle* h, int64_t nsteps, double* ms);
 /* Waits (bounded by timeout_s seconds) for all work of the handle. */
 int lbm_synchronize(LbmHandle* h, double timeout_s);
 
+/* A population array owned by the caller, in device memory: value of node
+ * (x, y), direction k (D2Q9 order of pylabolt/base/lattice.py) at
+ * pop[k*plane + y*pitch + x], stored as f (LBM_FP64), g = f - w_k
+ * (LBM_FP32_SHIFTED) or g * fp16_scale (LBM_FP16_SHIFTED). */
+typedef struct {
+  int32_t precision;
+  int32_t nx, ny;
+  int32_t reserved;
+  int64_t pitch;            /* elements from one row to the next            */
+  int64_t plane;            /* elements from one direction to the next      */
+  const void* pop;          /* device pointer                               */
+  const uint8_t* exclude;   /* device pointer or NULL: [y*pitch + x] != 0
+                               leaves the node out (e.g. solid nodes)       */
+  double fp16_scale;
+} LbmPopView;
+
+#define LBM_NOALLOC_MAX_ROWS 8192
+
+/* No counterpart in the reference.  Same sums as lbm_conservation
+ * ({sum f, sum cx f, sum cy f} over the nodes not excluded, FP64), for a
+ * population array the caller owns, for callers that cannot allocate device
+ * memory: code embedded in a host application that hands out all device
+ * memory from its own pool, code running while a stream is captured (where
+ * cudaMalloc is not permitted), or monitoring loops that cannot take
+ * cudaMalloc's implicit synchronisation.  It allocates nothing: its scratch is
+ * a fixed device array inside the library (LBM_NOALLOC_MAX_ROWS + 64 rows of
+ * 8 doubles, about 0.5 MB, held by every GPU that loads the library until the
+ * process exits).  out_device receives 3 doubles; the work is queued on
+ * `stream` (a cudaStream_t, NULL for the default stream) and the call returns
+ * without waiting.  ny above LBM_NOALLOC_MAX_ROWS is rejected (LBM_ERR_ARG).
+ * The first call on each device looks up the scratch array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * All calls share the one scratch array: calls whose work overlaps on the GPU
+ * (other streams, or other host threads on the same device) race and must be
+ * serialised by the caller. */
+int lbm_conservation_noalloc(const LbmPopView* view, double* out_device, void* stream);
+
 /* Message of the last failing call on this thread ("" if none). */
 const char* lbm_last_error(void);
 

@@ -23,6 +23,7 @@ UNITS = {
     "lbm_fp64.cu": ["--fmad=false"],
     "lbm_lowp.cu": [],
     "lbm_capi.cu": [],
+    "lbm_noalloc.cu": [],
 }
 
 

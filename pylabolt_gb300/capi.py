@@ -46,6 +46,15 @@ class LbmConfig(ctypes.Structure):
                 ("fp16_scale", ctypes.c_double)]
 
 
+class LbmPopView(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int32), ("nx", ctypes.c_int32), ("ny", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("pitch", ctypes.c_int64), ("plane", ctypes.c_int64),
+                ("pop", ctypes.c_void_p), ("exclude", ctypes.c_void_p),
+                ("fp16_scale", ctypes.c_double)]
+
+
+NOALLOC_MAX_ROWS = 8192
+
 # numpy mirror of LbmNodeLinks (must match the C struct byte for byte)
 NODE_LINKS_DTYPE = np.dtype([("node", "<i8"), ("src", "<i8", 9), ("aux", "<i8", 9),
                              ("param", "<f8", 9), ("type", "i1", 9),
@@ -59,7 +68,7 @@ EXPORTS = ["lbm_create", "lbm_init_fields", "lbm_set_body_force", "lbm_step",
            "lbm_step_ex", "lbm_get_moments", "lbm_residual", "lbm_conservation",
            "lbm_get_populations", "lbm_set_populations", "lbm_time",
            "lbm_kernel_launches", "lbm_kernel_variant", "lbm_tuning", "lbm_device_bytes", "lbm_time_steps",
-           "lbm_synchronize", "lbm_last_error", "lbm_destroy"]
+           "lbm_synchronize", "lbm_last_error", "lbm_destroy", "lbm_conservation_noalloc"]
 
 
 def lib_path():
@@ -97,6 +106,7 @@ def load(build=True):
         "lbm_time_steps": [P, i64, dbl],
         "lbm_synchronize": [P, ctypes.c_double],
         "lbm_destroy": [P],
+        "lbm_conservation_noalloc": [ctypes.POINTER(LbmPopView), P, P],
     }
     for name, argtypes in sig.items():
         fn = getattr(lib, name)

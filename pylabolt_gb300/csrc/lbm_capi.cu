@@ -42,6 +42,10 @@ constexpr int kCY[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
 
 }  // namespace
 
+namespace lbm {
+void record_error(const std::string& msg) { g_err = msg; }
+}  // namespace lbm
+
 struct LbmHandle {
   LbmConfig cfg{};
   const lbm::KernelSet* ks = nullptr;

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 namespace lbm {
 
 // Device-side geometry of one case.  Populations are SoA planes of
@@ -143,5 +145,8 @@ inline dim3 step_grid(const Geom& g, Variant v, int sms, int elem_bytes) {
 // (ind = (x+1)*(ny+2)+(y+1)) order; device SoA [ncomp][plane].
 cudaError_t reorder(const Geom& g, const double* in, double* out, int ncomp,
                     int layout, int to_device, cudaStream_t s);
+
+// Sets the message lbm_last_error() returns on this thread.
+void record_error(const std::string& msg);
 
 }  // namespace lbm

@@ -96,7 +96,9 @@ typedef struct {
   int64_t aux[9];          /* ABB: node x+n (inner index; must be listed)   */
   double param[9];         /* MBB: c_ibar . u ; ABB: rho_w                  */
   int8_t type[9];          /* LBM_LINK_*                                    */
-  int8_t reserved[7];
+  int8_t wall;             /* 1: the MBB links come from a fixed_velocity
+                              boundary (their u_w gets a gradient)          */
+  int8_t reserved[6];
 } LbmNodeLinks;
 
 /* Creates a case on the GPU: geometry, link table and parameters.  Replaces
@@ -155,6 +157,25 @@ int lbm_get_populations(LbmHandle* h, double* pop);
 /* Sets the populations entering the next step (the reference's pop_fluid_new)
  * from the padded AoS layout; the next step starts from them directly. */
 int lbm_set_populations(LbmHandle* h, const double* pop_new);
+
+/* Forward pass that keeps what lbm_adjoint_backward needs (extension: the
+ * reference has no adjoint).  Starts from the fields of the last
+ * lbm_init_fields, runs nsteps steps, stores the state every `interval`
+ * steps (1 = every step; states in between are recomputed by the backward
+ * pass) and records the moments of the last step (lbm_get_moments).
+ * Supported: BGK with Guo forcing none/linear/second order; links PULL,
+ * ZERO, BB, MBB (no anti-bounce-back, no zero_gradient); FP64 or FP32
+ * shifted storage. */
+int lbm_adjoint_forward(LbmHandle* h, int64_t nsteps, int interval);
+
+/* Reverse pass of the last lbm_adjoint_forward.  grad_u: dL/du of the last
+ * step's velocity, [nx*ny][2] inner layout (FP64).  Outputs (NULL to skip):
+ * grad_force [nx*ny][2] = dL/dF of the body-force field, *grad_tau = dL/dtau,
+ * grad_uwall[2] = dL/du_w of the fixed_velocity links marked `wall`.  The
+ * discrete adjoint of the step kernels' own arithmetic, with
+ * checkpoint-and-recompute between stored states. */
+int lbm_adjoint_backward(LbmHandle* h, const double* grad_u, double* grad_force,
+                         double* grad_tau, double* grad_uwall);
 
 /* Number of completed steps since the last init. */
 int lbm_time(LbmHandle* h, int64_t* t);

@@ -57,9 +57,9 @@ NOALLOC_MAX_ROWS = 8192
 
 # numpy mirror of LbmNodeLinks (must match the C struct byte for byte)
 NODE_LINKS_DTYPE = np.dtype([("node", "<i8"), ("src", "<i8", 9), ("aux", "<i8", 9),
-                             ("param", "<f8", 9), ("type", "i1", 9),
-                             ("reserved", "i1", 7)])
-assert NODE_LINKS_DTYPE.itemsize == 8 + 72 + 72 + 72 + 9 + 7
+                             ("param", "<f8", 9), ("type", "i1", 9), ("wall", "i1"),
+                             ("reserved", "i1", 6)])
+assert NODE_LINKS_DTYPE.itemsize == 8 + 72 + 72 + 72 + 9 + 1 + 6
 
 _LIB = None
 
@@ -68,7 +68,8 @@ EXPORTS = ["lbm_create", "lbm_init_fields", "lbm_set_body_force", "lbm_step",
            "lbm_step_ex", "lbm_get_moments", "lbm_residual", "lbm_conservation",
            "lbm_get_populations", "lbm_set_populations", "lbm_time",
            "lbm_kernel_launches", "lbm_kernel_variant", "lbm_tuning", "lbm_device_bytes", "lbm_time_steps",
-           "lbm_synchronize", "lbm_last_error", "lbm_destroy", "lbm_conservation_noalloc"]
+           "lbm_synchronize", "lbm_last_error", "lbm_destroy", "lbm_conservation_noalloc",
+           "lbm_adjoint_forward", "lbm_adjoint_backward"]
 
 
 def lib_path():
@@ -107,6 +108,8 @@ def load(build=True):
         "lbm_synchronize": [P, ctypes.c_double],
         "lbm_destroy": [P],
         "lbm_conservation_noalloc": [ctypes.POINTER(LbmPopView), P, P],
+        "lbm_adjoint_forward": [P, i64, ctypes.c_int],
+        "lbm_adjoint_backward": [P, P, P, dbl, P],
     }
     for name, argtypes in sig.items():
         fn = getattr(lib, name)

@@ -1,7 +1,7 @@
 // Auxiliary kernels of one storage precision (conversions, conservation sums)
 // and the KernelSet that bundles them with the fused step kernel.
 #pragma once
-#include "lbm_kernels.cuh"
+#include "lbm_adjoint.cuh"
 
 namespace lbm {
 
@@ -166,6 +166,17 @@ struct Kernels {
     conservation_kernel<S><<<g.ny, 256, 0, s>>>(g, p, static_cast<const S*>(f), partials);
     return cudaGetLastError();
   }
+  template <class U = S>
+  static cudaError_t adjoint(int forc, const AdjArgs& a, cudaStream_t s) {
+    const dim3 grid = node_grid(a.g);
+    if (forc == 0)
+      adjoint_kernel<S, 0><<<grid, kStepBlock, 0, s>>>(a);
+    else if (forc == 1)
+      adjoint_kernel<S, 1><<<grid, kStepBlock, 0, s>>>(a);
+    else
+      adjoint_kernel<S, 2><<<grid, kStepBlock, 0, s>>>(a);
+    return cudaGetLastError();
+  }
   static KernelSet make() {
     KernelSet k;
     k.elem_bytes = sizeof(S);
@@ -191,6 +202,10 @@ struct Kernels {
     k.moments_to_f64 = &moments_to_f64;
     k.body_from_f64 = &body_from_f64;
     k.conservation = &conservation;
+    if constexpr (sizeof(S) >= 4)
+      k.adjoint = &adjoint<S>;
+    else
+      k.adjoint = nullptr;
     return k;
   }
 };

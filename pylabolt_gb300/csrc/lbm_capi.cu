@@ -78,6 +78,26 @@ struct LbmHandle {
   bool tuned = false;
   double tune_ms[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   double timeout_s = 600.0;
+  // host copies kept for the adjoint set-up
+  std::vector<uint8_t> h_cls;
+  std::vector<LbmNodeLinks> h_links;
+  // adjoint workspace (allocated by the first lbm_adjoint_forward)
+  struct Adj {
+    bool tables = false;
+    std::string unsupported;       // non-empty: why the adjoint is unavailable
+    int* tr_reader = nullptr;
+    int8_t* tr_self = nullptr;
+    int8_t* wall_rec = nullptr;
+    int64_t T = 0;
+    int interval = 0;
+    std::vector<void*> ckpt, ckpt_side, seg, seg_side;
+    void* a[2] = {nullptr, nullptr};
+    void* gF = nullptr;
+    double* gpart = nullptr;
+    double* grad_u = nullptr;      // [2][plane]
+    long long nparts = 0;
+    bool ready = false;
+  } adj;
 
   ~LbmHandle() {
     if (gexec) cudaGraphExecDestroy(gexec);
@@ -152,13 +172,21 @@ struct LbmHandle {
   int launch(int flags, bool advance = true) { return launch_v(flags, variant, advance); }
 
   int launch_v(int flags, lbm::Variant v, bool advance) {
+    const int rc = launch_bufs(flags, v, pop[cur], pop[cur ^ 1], side[cur], side[cur ^ 1]);
+    if (rc == LBM_OK && advance) cur ^= 1;
+    return rc;
+  }
+
+  // One fused step from `fin` / `side_in` into `fout` / `side_out`.
+  int launch_bufs(int flags, lbm::Variant v, const void* fin, void* fout, const void* sin,
+                  void* sout) {
     lbm::StepArgs a;
     a.g = g;
     a.p = p;
-    a.fin = pop[cur];
-    a.fout = pop[cur ^ 1];
-    a.side_in = side[cur];
-    a.side_out = side[cur ^ 1];
+    a.fin = fin;
+    a.fout = fout;
+    a.side_in = sin;
+    a.side_out = sout;
     a.rho = mom[0];
     a.ux = mom[1];
     a.uy = mom[2];
@@ -170,9 +198,86 @@ struct LbmHandle {
     a.err = err_dev;
     a.flags = flags;
     LBM_CUDA(ks->step(cfg.collision, cfg.forcing, a, v, sms, stream));
-    if (advance) cur ^= 1;
     return LBM_OK;
   }
+
+  // Transpose of the link table: for every boundary node s and direction m,
+  // the node that pulls p(s)_m (or -1) and whether s itself bounces it back.
+  int build_adjoint_tables() {
+    if (adj.tables) return adj.unsupported.empty() ? LBM_OK : fail(LBM_ERR_ARG, adj.unsupported);
+    adj.tables = true;
+    if (cfg.collision != LBM_BGK) adj.unsupported = "adjoint: only BGK collision is supported";
+    if (!ks->adjoint) adj.unsupported = "adjoint: FP64 or FP32-shifted storage is required";
+    const int nx = g.nx, ny = g.ny, pitch = g.pitch;
+    auto dev = [&](int64_t node) { return (long long)(node % ny + 1) * pitch + node / ny; };
+    const int64_t nrec = (int64_t)h_links.size();
+    std::unordered_map<long long, int> rec_of;   // device node -> record
+    for (int64_t r = 0; r < nrec; ++r) rec_of[dev(h_links[r].node)] = (int)r;
+    std::unordered_map<long long, long long> reader;   // (src dev)*9+k -> reader dev
+    for (int64_t r = 0; r < nrec && adj.unsupported.empty(); ++r) {
+      const LbmNodeLinks& L = h_links[r];
+      const long long y = dev(L.node);
+      for (int k = 1; k < 9; ++k) {
+        if (L.type[k] == LBM_LINK_ABB) {
+          adj.unsupported = "adjoint: anti-bounce-back (fixed_pressure) links are not supported";
+          break;
+        }
+        if (L.type[k] != LBM_LINK_PULL) continue;
+        const long long key = dev(L.src[k]) * 9 + k;
+        if (!reader.emplace(key, y).second) {
+          adj.unsupported = "adjoint: a population is pulled by two nodes (zero_gradient) - not supported";
+          break;
+        }
+        // a plain in-grid neighbour must be the standard source
+        const long long yx = L.node / ny, yy = L.node % ny;
+        const long long sx = yx - kCX[k], sy = yy - kCY[k];
+        if (sx >= 0 && sx < nx && sy >= 0 && sy < ny && dev(L.src[k]) != (sy + 1) * pitch + sx) {
+          adj.unsupported = "adjoint: a link pulls from a node other than its neighbour - not supported";
+          break;
+        }
+      }
+    }
+    if (!adj.unsupported.empty()) return fail(LBM_ERR_ARG, adj.unsupported);
+    const size_t n9 = 9 * std::max<int64_t>(nrec, 1);
+    std::vector<int> trr(n9, -1);
+    std::vector<int8_t> trs(n9, 0), wr(std::max<int64_t>(nrec, 1), 0);
+    static const int inv[9] = {0, 3, 4, 1, 2, 7, 8, 5, 6};
+    for (int64_t r = 0; r < nrec; ++r) {
+      const LbmNodeLinks& L = h_links[r];
+      const long long s = dev(L.node);
+      const long long sx = L.node / ny, sy = L.node % ny;
+      wr[r] = L.wall;
+      trr[9 * r] = (int)s;   // the rest population stays at the node
+      for (int m = 1; m < 9; ++m) {
+        const long long yx = sx + kCX[m], yy = sy + kCY[m];
+        long long rd = -1;
+        if (yx >= 0 && yx < nx && yy >= 0 && yy < ny && h_cls[(yy + 1) * pitch + yx] == 0) {
+          rd = (yy + 1) * pitch + yx;   // bulk neighbour
+        } else {
+          auto it = reader.find(s * 9 + m);
+          if (it != reader.end()) rd = it->second;
+        }
+        trr[9 * r + m] = (int)rd;
+        const int tb = L.type[inv[m]];
+        trs[9 * r + m] = (tb == LBM_LINK_BB || tb == LBM_LINK_MBB) ? 1 : 0;
+      }
+    }
+    int rc;
+    if ((rc = alloc(reinterpret_cast<void**>(&adj.tr_reader), n9 * sizeof(int))) ||
+        (rc = alloc(reinterpret_cast<void**>(&adj.tr_self), n9)) ||
+        (rc = alloc(reinterpret_cast<void**>(&adj.wall_rec), wr.size())))
+      return rc;
+    LBM_CUDA(cudaMemcpyAsync(adj.tr_reader, trr.data(), n9 * sizeof(int), cudaMemcpyHostToDevice, stream));
+    LBM_CUDA(cudaMemcpyAsync(adj.tr_self, trs.data(), n9, cudaMemcpyHostToDevice, stream));
+    LBM_CUDA(cudaMemcpyAsync(adj.wall_rec, wr.data(), wr.size(), cudaMemcpyHostToDevice, stream));
+    return wait();
+  }
+
+  size_t state_bytes() const { return (9 * g.plane + 2 * g.pitch) * (size_t)ks->elem_bytes; }
+  size_t side_bytes() const { return 3 * (size_t)std::max(g.nrec, 1) * ks->compute_bytes; }
+
+  // state buffers hold a guard row before plane 0, like pop_raw
+  void* state_base(void* raw) const { return static_cast<char*>(raw) + g.pitch * ks->elem_bytes; }
 
   long long nparts_of(lbm::Variant v) const {
     const dim3 gr = lbm::step_grid(g, v, sms, ks->elem_bytes);
@@ -357,6 +462,8 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   LbmHandle* h = new LbmHandle();
   h->cfg = c;
   h->ks = ks;
+  h->h_cls = cls;
+  h->h_links.assign(links, links + nlinks);
   auto bail = [&](int rc) {
     delete h;
     return rc;
@@ -582,6 +689,148 @@ int lbm_step_ex(LbmHandle* h, int64_t nsteps, int flags) {
 }
 
 int lbm_step(LbmHandle* h, int64_t nsteps) { return lbm_step_ex(h, nsteps, 0); }
+
+int lbm_adjoint_forward(LbmHandle* h, int64_t nsteps, int interval) {
+  if (!h) return fail(LBM_ERR_ARG, "lbm_adjoint_forward: null handle");
+  if (nsteps < 1 || interval < 1) return fail(LBM_ERR_ARG, "lbm_adjoint_forward: need nsteps >= 1, interval >= 1");
+  if (!h->initialized || !h->nopull || h->t != 0)
+    return fail(LBM_ERR_STATE, "lbm_adjoint_forward: call lbm_init_fields first (the pass starts at t = 0)");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  int rc = h->build_adjoint_tables();
+  if (rc) return rc;
+  auto& A = h->adj;
+  const int64_t nck = (nsteps + interval - 1) / interval;   // states at t = 0, I, 2I, ...
+  // (re)allocate the workspace when the plan changes
+  if (!A.ready || A.interval != interval || (int64_t)A.ckpt.size() < nck) {
+    for (auto* v : {&A.ckpt, &A.ckpt_side, &A.seg, &A.seg_side})
+      for (void* q : *v)
+        for (auto it = h->allocs.begin(); it != h->allocs.end(); ++it)
+          if (*it == q) {
+            cudaFree(q);
+            h->allocs.erase(it);
+            break;
+          }
+    A.ckpt.assign(nck, nullptr);
+    A.ckpt_side.assign(nck, nullptr);
+    A.seg.assign(interval > 1 ? interval - 1 : 0, nullptr);
+    A.seg_side.assign(A.seg.size(), nullptr);
+    for (size_t i = 0; i < A.ckpt.size(); ++i)
+      if ((rc = h->alloc(&A.ckpt[i], h->state_bytes())) || (rc = h->alloc(&A.ckpt_side[i], h->side_bytes())))
+        return rc;
+    for (size_t i = 0; i < A.seg.size(); ++i)
+      if ((rc = h->alloc(&A.seg[i], h->state_bytes())) || (rc = h->alloc(&A.seg_side[i], h->side_bytes())))
+        return rc;
+    if (!A.a[0]) {
+      const size_t ab = 9 * h->g.plane * (size_t)h->ks->compute_bytes;
+      A.nparts = h->nparts_of(lbm::Variant{0, 1, 256, 0});
+      if ((rc = h->alloc(&A.a[0], ab)) || (rc = h->alloc(&A.a[1], ab)) ||
+          (rc = h->alloc(&A.gF, 2 * h->g.plane * (size_t)h->ks->compute_bytes)) ||
+          (rc = h->alloc(reinterpret_cast<void**>(&A.gpart), A.nparts * 4 * sizeof(double))) ||
+          (rc = h->alloc(reinterpret_cast<void**>(&A.grad_u), 2 * h->g.plane * sizeof(double))))
+        return rc;
+      LBM_CUDA(cudaMemsetAsync(A.a[0], 0, ab, h->stream));
+      LBM_CUDA(cudaMemsetAsync(A.a[1], 0, ab, h->stream));
+      LBM_CUDA(cudaMemsetAsync(A.grad_u, 0, 2 * h->g.plane * sizeof(double), h->stream));
+    }
+    A.interval = interval;
+    A.ready = true;
+  }
+  if (!h->tuned && (rc = h->autotune())) return rc;
+  // t = 0: the initial populations (read without pulling)
+  LBM_CUDA(cudaMemcpyAsync(h->state_base(A.ckpt[0]), h->pop[h->cur], 9 * h->g.plane * h->ks->elem_bytes,
+                           cudaMemcpyDeviceToDevice, h->stream));
+  for (int64_t t = 1; t <= nsteps; ++t) {
+    const int fl = (t == 1 ? lbm::F_NOPULL : 0) | (t == nsteps ? lbm::F_MOMENTS : 0);
+    if ((rc = h->launch(fl))) return rc;
+    if (t % interval == 0 && t < nsteps) {
+      const int64_t c = t / interval;
+      LBM_CUDA(cudaMemcpyAsync(h->state_base(A.ckpt[c]), h->pop[h->cur], 9 * h->g.plane * h->ks->elem_bytes,
+                               cudaMemcpyDeviceToDevice, h->stream));
+      LBM_CUDA(cudaMemcpyAsync(A.ckpt_side[c], h->side[h->cur], h->side_bytes(), cudaMemcpyDeviceToDevice, h->stream));
+    }
+  }
+  h->nopull = false;
+  h->t = nsteps;
+  h->launches += nsteps;
+  h->has_moments = true;
+  A.T = nsteps;
+  return h->wait();
+}
+
+int lbm_adjoint_backward(LbmHandle* h, const double* grad_u, double* grad_force,
+                         double* grad_tau, double* grad_uwall) {
+  if (!h || !grad_u) return fail(LBM_ERR_ARG, "lbm_adjoint_backward: null argument");
+  auto& A = h->adj;
+  if (!A.ready || A.T < 1) return fail(LBM_ERR_STATE, "lbm_adjoint_backward: run lbm_adjoint_forward first");
+  if (grad_force && !h->body) return fail(LBM_ERR_STATE, "lbm_adjoint_backward: no body-force field to differentiate");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  const lbm::Geom& g = h->g;
+  const long long nh = (long long)g.nx * g.ny;
+  int rc = h->ensure_stage(2 * nh);
+  if (rc) return rc;
+  LBM_CUDA(cudaMemcpyAsync(h->stage, grad_u, 2 * nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  LBM_CUDA(lbm::reorder(g, h->stage, A.grad_u, 2, LBM_LAYOUT_INNER, 1, h->stream));
+  LBM_CUDA(cudaMemsetAsync(A.gF, 0, 2 * g.plane * (size_t)h->ks->compute_bytes, h->stream));
+  LBM_CUDA(cudaMemsetAsync(A.gpart, 0, A.nparts * 4 * sizeof(double), h->stream));
+  const int I = A.interval;
+  const int64_t T = A.T;
+  const lbm::Variant plain = h->variant;
+  int cur_a = 0;
+  bool have_next = false;
+  for (int64_t c = (T - 1) / I; c >= 0; --c) {
+    const int64_t t0 = c * I, t1 = std::min<int64_t>(t0 + I, T);
+    // recompute p_{t0+1} .. p_{t1-1} into the segment buffers
+    for (int64_t t = t0 + 1; t < t1; ++t) {
+      const void* fin = t == t0 + 1 ? h->state_base(A.ckpt[c]) : h->state_base(A.seg[t - t0 - 2]);
+      const void* sin = t == t0 + 1 ? A.ckpt_side[c] : A.seg_side[t - t0 - 2];
+      if ((rc = h->launch_bufs(t == 1 ? lbm::F_NOPULL : 0, plain, fin, h->state_base(A.seg[t - t0 - 1]), sin,
+                               A.seg_side[t - t0 - 1])))
+        return rc;
+    }
+    // reverse steps t1 .. t0+1
+    for (int64_t t = t1; t > t0; --t) {
+      lbm::AdjArgs a;
+      a.g = g;
+      a.p = h->p;
+      a.fprev = t - 1 == t0 ? h->state_base(A.ckpt[c]) : h->state_base(A.seg[t - t0 - 2]);
+      a.side_prev = t - 1 == t0 ? A.ckpt_side[c] : A.seg_side[t - t0 - 2];
+      a.a_next = have_next ? A.a[cur_a] : nullptr;
+      a.a_cur = A.a[cur_a ^ 1];
+      a.grad_u = t == T ? A.grad_u : nullptr;
+      a.gF = h->body ? A.gF : nullptr;
+      a.gpart = A.gpart;
+      a.tr_reader = A.tr_reader;
+      a.tr_self = A.tr_self;
+      a.wall_rec = A.wall_rec;
+      a.body = h->body;
+      a.nopull = t == 1;
+      LBM_CUDA(h->ks->adjoint(h->cfg.forcing, a, h->stream));
+      cur_a ^= 1;
+      have_next = true;
+    }
+  }
+  // parameter gradients: fixed-order sum of the per-block rows on the host
+  std::vector<double> part(A.nparts * 4);
+  LBM_CUDA(cudaMemcpyAsync(part.data(), A.gpart, part.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if ((rc = h->wait())) return rc;
+  if (grad_force) {
+    if ((rc = h->ensure_stage(2 * nh + 3 * g.plane))) return rc;
+    LBM_CUDA(h->ks->moments_to_f64(g, A.gF, static_cast<char*>(A.gF) + g.plane * h->ks->compute_bytes,
+                                   A.gF, h->stage + 2 * nh, h->stream));
+    LBM_CUDA(lbm::reorder(g, h->stage + 2 * nh, h->stage, 2, LBM_LAYOUT_INNER, 0, h->stream));
+    LBM_CUDA(cudaMemcpyAsync(grad_force, h->stage, 2 * nh * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if ((rc = h->wait())) return rc;
+  }
+  double s[3] = {0, 0, 0};
+  for (long long b = 0; b < A.nparts; ++b)
+    for (int i = 0; i < 3; ++i) s[i] += part[b * 4 + i];
+  if (grad_tau) *grad_tau = -s[0] * h->cfg.omega * h->cfg.omega;   // d omega / d tau = -omega^2
+  if (grad_uwall) {
+    grad_uwall[0] = s[1];
+    grad_uwall[1] = s[2];
+  }
+  return LBM_OK;
+}
 
 int lbm_get_moments(LbmHandle* h, double* rho, double* u, int layout) {
   if (!h || !rho || !u) return fail(LBM_ERR_ARG, "lbm_get_moments: null argument");

@@ -68,6 +68,24 @@ struct StepArgs {
   int flags;
 };
 
+// Arguments of one reverse (adjoint) step; see lbm_adjoint.cuh.
+struct AdjArgs {
+  Geom g;
+  Params p;
+  const void* fprev;      // p_{t-1} (storage type): its pull gives f^t
+  const void* side_prev;  // rho, u of step t-1 at boundary nodes (compute type)
+  const void* a_next;     // a^{t+1} = dL/df^{t+1}, [9][plane] compute type; null at t = T
+  void* a_cur;            // a^t out
+  const double* grad_u;   // dL/du^T, [2][plane] FP64, only at t = T
+  void* gF;               // dL/dF accumulator [2][plane] (compute type) or null
+  double* gpart;          // [blocks][4]: dL/domega, dL/du_wall x, y (accumulated)
+  const int* tr_reader;   // [nrec*9] node that pulls p_t(n)_m, or -1
+  const int8_t* tr_self;  // [nrec*9] 1: n's own link mbar bounces p_t(n)_m back
+  const int8_t* wall_rec; // [nrec] 1: the record's MBB links are wall links
+  const void* body;       // body force [2][plane] or null (then F = rho g)
+  int nopull;             // t = 1: f^1 are the stored populations themselves
+};
+
 // Launch shape of the fused step.
 //   kind 0: scalar kernel, one node per thread
 //   kind 1: vector kernel, `vec` consecutive nodes per thread
@@ -109,6 +127,8 @@ struct KernelSet {
   // partial sums {sum f, sum cx f, sum cy f} per block row -> partials[ny][8]
   cudaError_t (*conservation)(const Geom& g, const Params& p, const void* f,
                               double* partials, cudaStream_t s);
+  // one reverse step (null where the storage has no adjoint)
+  cudaError_t (*adjoint)(int forcing, const AdjArgs& a, cudaStream_t s);
 };
 
 const KernelSet& kernels_fp64();

@@ -74,6 +74,7 @@ def build_links(case):
     src = np.zeros((n, 9), dtype=np.int64)
     aux = np.zeros((n, 9), dtype=np.int64)
     par = np.zeros((n, 9), dtype=np.float64)
+    wall = np.zeros(n, dtype=np.int8)
     src[:, 0] = node
     u = case.velocity
     for k in range(1, 9):
@@ -117,6 +118,7 @@ def build_links(case):
                 typ[rows, k] = LINK_BB
             elif el.type == "fixed_velocity":
                 typ[rows, k] = LINK_MBB
+                wall[rows] = 1
                 par[rows, k] = CX[kb] * np.float64(el.value[0]) + CY[kb] * np.float64(el.value[1])
             elif el.type == "fixed_pressure":
                 typ[rows, k] = LINK_ABB
@@ -142,5 +144,6 @@ def build_links(case):
     rec["src"] = src
     rec["aux"] = aux
     rec["param"] = par
+    rec["wall"] = wall
     node_solid = np.ascontiguousarray(solid.astype(np.uint8).ravel())
     return node_solid, rec

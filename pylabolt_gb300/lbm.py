@@ -134,6 +134,25 @@ class FluidLBM:
         p = np.ascontiguousarray(pop_new, dtype=np.float64)
         check(self.lib.lbm_set_populations(self.h, ptr(p)))
 
+    # -- adjoint (extension: the reference has no adjoint)
+    def adjoint_forward(self, nsteps, interval=45):
+        """Runs nsteps from the initialised fields, keeping a state every
+        `interval` steps for the reverse pass; the last step's moments are
+        recorded (:meth:`moments`)."""
+        check(self.lib.lbm_adjoint_forward(self.h, int(nsteps), int(interval)))
+
+    def adjoint_backward(self, grad_u, want_force=True):
+        """Reverse pass for dL/du of the last step ([Nx, Ny, 2]).  Returns
+        (dL/dF [Nx, Ny, 2] or None, dL/dtau, dL/du_wall [2]).  dL/du at solid
+        nodes is ignored (their velocity is the body's, not computed)."""
+        nx, ny = self.case.nx, self.case.ny
+        gu = np.ascontiguousarray(np.asarray(grad_u, dtype=np.float64).reshape(nx * ny, 2))
+        gF = np.empty((nx * ny, 2)) if (want_force and self.case.body_force_field is not None) else None
+        gtau = ctypes.c_double()
+        guw = (ctypes.c_double * 2)()
+        check(self.lib.lbm_adjoint_backward(self.h, ptr(gu), ptr(gF), ctypes.byref(gtau), guw))
+        return (gF.reshape(nx, ny, 2) if gF is not None else None), gtau.value, np.array(guw[:])
+
     @property
     def time(self):
         t = ctypes.c_int64()

@@ -107,3 +107,32 @@ def cylinder(nx=8192, ny=2048, model="BGK", storage=None, kin_visc=0.04, radius=
     u0 = rng.uniform(-amp, amp, size=(nx, ny, 2))
     c["initial_fields_dict"]["default"]["fluid"]["velocity"] = {"type": "array", "value": u0}
     return c
+
+
+def smooth_noise(nx, ny, sigma, seed):
+    """Unit-variance Gaussian-smoothed N(0,1) field (periodic FFT filter)."""
+    rng = np.random.default_rng(seed)
+    z = rng.standard_normal((nx, ny))
+    kx = np.fft.fftfreq(nx)[:, None]
+    ky = np.fft.rfftfreq(ny)[None, :]
+    filt = np.exp(-2.0 * (np.pi * sigma) ** 2 * (kx ** 2 + ky ** 2))
+    s = np.fft.irfft2(np.fft.rfft2(z) * filt, s=(nx, ny))
+    return s / s.std()
+
+
+def adjoint_channel(nx=512, ny=512, tau=0.8, mean_force=5e-6, amp=1e-6, sigma=8.0,
+                    seed=1, storage=None, forcing="guo_second_order"):
+    """Channel, periodic in x, bounce-back walls in y, BGK with Guo forcing and
+    a per-node body force F = mean_force x + amp * smoothed noise (both
+    components), tau fixed.  Returns the case dictionaries."""
+    kin_visc = (tau - 0.5) / 3.0
+    c = _base(nx, ny, kin_visc, forcing=forcing, storage=storage)
+    c["boundary_dict"]["inout"] = {"wall": False, "segments": [
+        [[0, 0], [0, ny - 1]], [[nx - 1, 0], [nx - 1, ny - 1]]], "fluid": {"type": "periodic"}}
+    c["boundary_dict"]["walls"] = {"wall": True, "segments": [
+        [[0, 0], [nx - 1, 0]], [[0, ny - 1], [nx - 1, ny - 1]]], "fluid": {"type": "bounce_back"}}
+    F = np.zeros((nx, ny, 2))
+    F[..., 0] = mean_force + amp * smooth_noise(nx, ny, sigma, seed)
+    F[..., 1] = amp * smooth_noise(nx, ny, sigma, seed + 1000)
+    c["forcing_dict"] = {"body_force_field": F}
+    return c

@@ -1,0 +1,165 @@
+"""CUDA adjoint (lbm_adjoint_forward / lbm_adjoint_backward) and the
+torch.autograd.Function against the plain-torch FP64 autograd reference and
+central finite differences of the CUDA FP64 forward."""
+import time
+
+import numpy as np
+import pytest
+import torch
+
+from _golden import load_golden
+from _torch_lbm import TorchLBM
+from pylabolt_gb300 import workloads
+from pylabolt_gb300.autograd import case_with, lbm_velocity
+from pylabolt_gb300.config import Case
+from pylabolt_gb300.lbm import FluidLBM
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-10     # CUDA FP64 adjoint vs torch FP64 autograd
+FP32_RTOL = 1e-3      # FP32-shifted forward + FP32 adjoint vs FP64 reference
+FD_RTOL = 1e-4        # against central finite differences (the benchmark spec bound)
+
+
+def _channel(forcing="guo_second_order", nx=24, ny=14, seed=5):
+    d = workloads.adjoint_channel(nx=nx, ny=ny, sigma=2.0, seed=seed, forcing=forcing)
+    return Case(d)
+
+
+def _torch_grads(case, T, gu, u_wall=None):
+    tl = TorchLBM(case)
+    F = torch.tensor(case.body_force_field.reshape(-1, 2), requires_grad=True) \
+        if case.body_force_field is not None else None
+    tau = torch.tensor(case.tau, dtype=torch.float64, requires_grad=True)
+    uw = torch.tensor(u_wall, dtype=torch.float64, requires_grad=True) if u_wall is not None else None
+    u = tl.run(T, 1.0 / tau, force=F, u_wall=uw)
+    (u * torch.tensor(gu.reshape(-1, 2))).sum().backward()
+    return (F.grad.numpy().reshape(case.nx, case.ny, 2) if F is not None else None,
+            float(tau.grad), uw.grad.numpy() if uw is not None else None)
+
+
+def _cuda_grads(case, T, gu, storage, interval):
+    with FluidLBM(case, storage=storage) as sim:
+        sim.initialize()
+        sim.adjoint_forward(T, interval)
+        return sim.adjoint_backward(gu)
+
+
+def _close(a, b, rtol):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() <= rtol * np.abs(np.asarray(b)).max()
+
+
+@pytest.mark.parametrize("forcing", ["guo_second_order", "guo_linear"])
+@pytest.mark.parametrize("interval", [1, 7, 45])
+def test_fp64_adjoint_matches_torch_autograd(forcing, interval):
+    case = _channel(forcing)
+    T = 30
+    gu = np.random.default_rng(0).standard_normal((case.nx, case.ny, 2)) * 1e-3
+    gF_ref, gtau_ref, _ = _torch_grads(case, T, gu)
+    gF, gtau, _ = _cuda_grads(case, T, gu, "fp64", interval)
+    assert _close(gF, gF_ref, FP64_RTOL)
+    assert abs(gtau - gtau_ref) <= FP64_RTOL * abs(gtau_ref)
+
+
+def test_fp64_adjoint_cavity_wall_velocity():
+    case = Case(load_golden("cavity_lid_last")[0])
+    T = 40
+    gu = np.random.default_rng(1).standard_normal((case.nx, case.ny, 2)) * 1e-3
+    _, gtau_ref, guw_ref = _torch_grads(case, T, gu, u_wall=[0.1, 0.0])
+    _, gtau, guw = _cuda_grads(case, T, gu, "fp64", 9)
+    assert _close(guw, guw_ref, FP64_RTOL)
+    assert abs(gtau - gtau_ref) <= FP64_RTOL * abs(gtau_ref)
+
+
+def test_fp32_adjoint_close_to_fp64_reference():
+    case = _channel()
+    T = 60
+    gu = np.random.default_rng(2).standard_normal((case.nx, case.ny, 2)) * 1e-3
+    gF_ref, gtau_ref, _ = _torch_grads(case, T, gu)
+    gF, gtau, _ = _cuda_grads(case, T, gu, "fp32_shifted", 10)
+    assert _close(gF, gF_ref, FP32_RTOL)
+    assert abs(gtau - gtau_ref) <= FP32_RTOL * abs(gtau_ref)
+
+
+def test_autograd_function_end_to_end():
+    case = _channel()
+    F = torch.tensor(case.body_force_field, requires_grad=True)
+    tau = torch.tensor(case.tau, dtype=torch.float64, requires_grad=True)
+    target = torch.zeros(case.nx, case.ny, 2, dtype=torch.float64)
+    u = lbm_velocity(case, force=F, tau=tau, nsteps=50, interval=8, storage="fp64")
+    loss = ((u - target) ** 2).mean()
+    loss.backward()
+    gu = (2.0 * u.detach().numpy() / u.numel())
+    gF_ref, gtau_ref, _ = _torch_grads(case, 50, gu)
+    assert _close(F.grad.numpy(), gF_ref, FP64_RTOL)
+    assert abs(float(tau.grad) - gtau_ref) <= FP64_RTOL * abs(gtau_ref)
+
+
+def _loss(case, F, tau, target, T, storage="fp64"):
+    c = case_with(case, tau=tau, force=F)
+    with FluidLBM(c, storage=storage) as sim:
+        sim.initialize()
+        sim.step(T, moments=True)
+        _, u = sim.moments()
+    return float(((u - target) ** 2).mean()), u
+
+
+def test_adjoint_channel_512_against_finite_differences_and_timing():
+    """The adjoint case at full size: 512x512 channel, tau 0.8, T = 2000,
+    checkpoint every 45 steps, FP32-shifted forward.  Gradients wrt F (one
+    random direction) and tau against central differences of the FP64 forward;
+    backward time within 3x the forward time."""
+    case = Case(workloads.adjoint_channel(seed=1))
+    tgt_case = Case(workloads.adjoint_channel(seed=2))
+    T = 2000
+    _, target = _loss(tgt_case, tgt_case.body_force_field, tgt_case.tau, 0.0, T)
+    with FluidLBM(case, storage="fp32_shifted") as sim:
+        sim.initialize()
+        sim.step(3)                      # autotune outside the timed region
+        sim.initialize()
+        sim.synchronize()
+        t0 = time.perf_counter()
+        sim.adjoint_forward(T, 45)
+        sim.synchronize()
+        t_fwd = time.perf_counter() - t0
+        _, u = sim.moments()
+        gu = 2.0 * (u - target) / u.size
+        t0 = time.perf_counter()
+        gF, gtau, _ = sim.adjoint_backward(gu)
+        t_bwd = time.perf_counter() - t0
+    rng = np.random.default_rng(7)
+    d = rng.standard_normal(case.body_force_field.shape)
+    h = 1e-8
+    lp, _ = _loss(case, case.body_force_field + h * d, case.tau, target, T)
+    lm, _ = _loss(case, case.body_force_field - h * d, case.tau, target, T)
+    fd = (lp - lm) / (2 * h)
+    assert abs(float((gF * d).sum()) - fd) <= FD_RTOL * abs(fd)
+    ht = 1e-5
+    lp, _ = _loss(case, case.body_force_field, case.tau + ht, target, T)
+    lm, _ = _loss(case, case.body_force_field, case.tau - ht, target, T)
+    fdt = (lp - lm) / (2 * ht)
+    assert abs(gtau - fdt) <= FD_RTOL * abs(fdt)
+    assert t_bwd <= 3.0 * t_fwd, (t_bwd, t_fwd)
+
+
+def test_adjoint_cavity_256_lid_velocity_against_finite_differences():
+    case = Case(workloads.cavity(256, re=400.0))
+    T = 1000
+    target = np.zeros((256, 256, 2))
+    with FluidLBM(case, storage="fp32_shifted") as sim:
+        sim.initialize()
+        sim.adjoint_forward(T, 45)
+        _, u = sim.moments()
+        _, _, guw = sim.adjoint_backward(2.0 * (u - target) / u.size)
+
+    def loss(U):
+        c = case_with(case, u_wall=[U, 0.0])
+        with FluidLBM(c, storage="fp64") as s:
+            s.initialize()
+            s.step(T, moments=True)
+            _, uu = s.moments()
+        return float(((uu - target) ** 2).mean())
+
+    U, h = case.elements[-1].value[0], 1e-6
+    fd = (loss(U + h) - loss(U - h)) / (2 * h)
+    assert abs(guw[0] - fd) <= FD_RTOL * abs(fd)

@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjArgs a) {
   const Params& p = a.p;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
-  double red[3] = {0, 0, 0};
+  T red[3] = {0, 0, 0};
   if (x < g.nx) {
     const long long n = g.node(x, y);
     const int cls = g.cls[n];
@@ -172,9 +172,9 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjArgs a) {
         gF[n] += adj_Fx;
         gF[g.plane + n] += adj_Fy;
       }
-      red[0] = double(g_om);
-      red[1] = double(guw_x);
-      red[2] = double(guw_y);
+      red[0] = g_om;
+      red[1] = guw_x;
+      red[2] = guw_y;
     }
   }
   // block sums, accumulated into this block's slot across reverse steps
@@ -182,8 +182,8 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjArgs a) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    const double v = warp_sum(red[i]);
-    if (lane == 0) sh[wid][i] = v;
+    const T v = warp_sum<T>(red[i]);
+    if (lane == 0) sh[wid][i] = double(v);
   }
   __syncthreads();
   if (threadIdx.x < 3) {

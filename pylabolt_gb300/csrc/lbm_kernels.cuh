@@ -342,7 +342,8 @@ __device__ __forceinline__ typename Store<S>::T special_link(
   return -raw + T(2.0 * Wk(KB)) * (drho_w + rho_w * (T(4.5) * cu * cu - T(1.5) * u2));
 }
 
-__device__ __forceinline__ double warp_sum(double v) {
+template <class R>
+__device__ __forceinline__ R warp_sum(R v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
@@ -439,10 +440,13 @@ __device__ __forceinline__ void special_links(typename Store<S>::T f[9], const S
   }
 }
 
-// Side data, moment output and residual terms of one updated node.
+// Side data, moment output and residual terms of one updated node.  The
+// residual terms are formed in the compute type T (FP32 for shifted storage:
+// GB300's FP64 rate is a small fraction of its FP32 rate) and summed in FP64
+// per block.
 template <class T>
 __device__ __forceinline__ void node_outputs(const StepArgs& a, long long n, int r, T rho,
-                                             T ux, T uy, double red[7]) {
+                                             T ux, T uy, T red[7]) {
   if (r >= 0) {
     T* side = static_cast<T*>(a.side_out);
     side[3 * r] = rho;
@@ -459,28 +463,29 @@ __device__ __forceinline__ void node_outputs(const StepArgs& a, long long n, int
     T* ro = static_cast<T*>(a.rho_old);
     T* xo = static_cast<T*>(a.ux_old);
     T* yo = static_cast<T*>(a.uy_old);
-    const double v[3] = {double(rho), double(ux), double(uy)};
-    const double o[3] = {double(ro[n]), double(xo[n]), double(yo[n])};
+    const T v[3] = {rho, ux, uy};
+    const T o[3] = {ro[n], xo[n], yo[n]};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const double d = v[c] - o[c];
+      const T d = v[c] - o[c];
       red[2 * c] += d * d;
       red[2 * c + 1] += o[c] * o[c];
     }
-    red[6] += (isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2])) ? 0.0 : 1.0;
+    red[6] += (isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2])) ? T(0) : T(1);
     ro[n] = rho;
     xo[n] = ux;
     yo[n] = uy;
   }
 }
 
-__device__ __forceinline__ void block_residual(const StepArgs& a, double red[7]) {
+template <class T>
+__device__ __forceinline__ void block_residual(const StepArgs& a, T red[7]) {
   __shared__ double sh[32][8];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int i = 0; i < 7; ++i) {
-    const double v = warp_sum(red[i]);
-    if (lane == 0) sh[wid][i] = v;
+    const T v = warp_sum<T>(red[i]);
+    if (lane == 0) sh[wid][i] = double(v);
   }
   __syncthreads();
   if (threadIdx.x < 7) {
@@ -504,7 +509,7 @@ __global__ void __launch_bounds__(CAP ? 256 : 512, CAP ? 8 : 1) step_kernel(cons
   const Params& p = a.p;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
-  double red[7] = {0, 0, 0, 0, 0, 0, 0};
+  T red[7] = {0, 0, 0, 0, 0, 0, 0};
 
   if (x < g.nx) {
     const long long n = g.node(x, y);
@@ -534,7 +539,7 @@ __global__ void __launch_bounds__(CAP ? 256 : 512, CAP ? 8 : 1) step_kernel(cons
       node_outputs<T>(a, n, r, rho, ux, uy, red);
     }
   }
-  if (a.flags & F_RESIDUAL) block_residual(a, red);
+  if (a.flags & F_RESIDUAL) block_residual<decltype(red[0] + 0)>(a, red);
 }
 
 // ---------------------------------------------------------------------------
@@ -640,7 +645,7 @@ __global__ void __launch_bounds__(256) step_vec_kernel(const StepArgs a) {
   const int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * V;
   const int warp_x0 = x0 - lane * V;
   const int y = blockIdx.y;
-  double red[7] = {0, 0, 0, 0, 0, 0, 0};
+  float red[7] = {0, 0, 0, 0, 0, 0, 0};
 
   if (warp_x0 < g.pitch) {
     const long long n0 = g.node(x0, y);
@@ -690,7 +695,7 @@ __global__ void __launch_bounds__(256) step_vec_kernel(const StepArgs a) {
       for (int k = 0; k < 9; ++k) VecIO<S, V>::store(fout + k * g.plane + n0, f[k], p);
     }
   }
-  if (a.flags & F_RESIDUAL) block_residual(a, red);
+  if (a.flags & F_RESIDUAL) block_residual<decltype(red[0] + 0)>(a, red);
 }
 
 // ---------------------------------------------------------------------------
@@ -780,7 +785,7 @@ __global__ void __launch_bounds__(1024) step_tma_kernel(const StepArgs a, int st
   const bool nopull = (a.flags & F_NOPULL) != 0;
   const S* __restrict__ fin = static_cast<const S*>(a.fin);
   S* __restrict__ fout = static_cast<S*>(a.fout);
-  double red[7] = {0, 0, 0, 0, 0, 0, 0};
+  float red[7] = {0, 0, 0, 0, 0, 0, 0};
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < stages; ++s) mbar_init(smem_u32(&bars[s]), 1);
@@ -872,7 +877,7 @@ __global__ void __launch_bounds__(1024) step_tma_kernel(const StepArgs a, int st
     }
   }
   __syncthreads();
-  if (a.flags & F_RESIDUAL) block_residual(a, red);
+  if (a.flags & F_RESIDUAL) block_residual<decltype(red[0] + 0)>(a, red);
 }
 
 // ---------------------------------------------------------------------------

@@ -240,10 +240,12 @@ def run_gb300(args, world, rank, local):
         if key in tr and tr[key].get("nodes"):
             traffic = tr[key]["dram_bytes_per_launch"] * nodes / tr[key]["nodes"]
 
-    # ---- end to end through the Python API, host buffers ------------------
+    # ---- end to end through the Python API, pinned host buffers -----------
     e2e_steps = min(args.steps, 100)
-    rho_h = np.ascontiguousarray(case.density)
-    u_h = np.ascontiguousarray(case.velocity)
+    rho_h = torch.empty(case.density.shape, dtype=torch.float64, pin_memory=True).numpy()
+    u_h = torch.empty(case.velocity.shape, dtype=torch.float64, pin_memory=True).numpy()
+    rho_h[...] = case.density
+    u_h[...] = case.velocity
     barrier()
     t0 = time.perf_counter()
     sim.initialize(rho_h, u_h)                      # H2D of the initial fields
@@ -326,6 +328,7 @@ def side_measurements(args, case_d, sim32, nodes, peak):
             mlups = nodes * steps / (ms / 1e3) / 1e6
             res[storage] = {"mlups": mlups,
                             "roofline_frac": B_LU[storage] * nodes / (ms / steps / 1e3) / 1e9 / peak}
+    out["adjoint"] = adjoint_measurement()
     out["fp64"] = res["fp64"]
     out["fp16_shifted"] = res["fp16_shifted"]
     err_steps = 200
@@ -344,6 +347,53 @@ def side_measurements(args, case_d, sim32, nodes, peak):
             "u_rel_l2": float(np.linalg.norm(d) / np.linalg.norm(ref[fluid])),
             "u_max_abs_over_max": float(np.abs(d).max() / np.abs(ref[fluid]).max())}
     return out
+
+
+def adjoint_measurement(nsteps=2000, interval=45):
+    """Adjoint case: 512x512 channel, BGK + Guo, per-node body force, tau 0.8,
+    FP32-shifted forward, T = 2000, state kept every 45 steps.  Reports the
+    forward time (with checkpointing), the reverse time (recompute + adjoint)
+    and a gradient check of one random body-force direction against central
+    differences of the FP64 forward."""
+    from pylabolt_gb300 import workloads
+    from pylabolt_gb300.config import Case
+    from pylabolt_gb300.lbm import FluidLBM
+    from pylabolt_gb300.autograd import case_with
+    case = Case(workloads.adjoint_channel(seed=1))
+    tgt = Case(workloads.adjoint_channel(seed=2))
+
+    def run64(c):
+        with FluidLBM(c, storage="fp64") as s:
+            s.initialize()
+            s.step(nsteps, moments=True)
+            return s.moments()[1]
+
+    target = run64(tgt)
+    with FluidLBM(case, storage="fp32_shifted") as sim:
+        sim.initialize()
+        sim.step(3)
+        sim.initialize()
+        sim.synchronize()
+        t0 = time.perf_counter()
+        sim.adjoint_forward(nsteps, interval)
+        sim.synchronize()
+        t_fwd = time.perf_counter() - t0
+        _, u = sim.moments()
+        t0 = time.perf_counter()
+        gF, gtau, _ = sim.adjoint_backward(2.0 * (u - target) / u.size)
+        t_bwd = time.perf_counter() - t0
+        sim.initialize()
+        ms_plain = sim.time_steps(nsteps)
+    d = np.random.default_rng(7).standard_normal(case.body_force_field.shape)
+    h = 1e-8
+    lp = float(((run64(case_with(case, force=case.body_force_field + h * d)) - target) ** 2).mean())
+    lm = float(((run64(case_with(case, force=case.body_force_field - h * d)) - target) ** 2).mean())
+    fd = (lp - lm) / (2 * h)
+    ad = float((gF * d).sum())
+    return {"workload": "channel_512x512_bgk_guo2_body_force_fp32_shifted", "steps": nsteps,
+            "checkpoint_interval": interval, "forward_s": t_fwd, "backward_s": t_bwd,
+            "plain_forward_s": ms_plain / 1e3, "adjoint_over_forward": t_bwd / t_fwd,
+            "grad_dir_vs_central_fd_rel": abs(ad - fd) / abs(fd), "grad_tau": gtau}
 
 
 def main():

@@ -329,6 +329,7 @@ def side_measurements(args, case_d, sim32, nodes, peak):
             res[storage] = {"mlups": mlups,
                             "roofline_frac": B_LU[storage] * nodes / (ms / steps / 1e3) / 1e9 / peak}
     out["adjoint"] = adjoint_measurement()
+    out["batch"] = batch_measurement()
     out["fp64"] = res["fp64"]
     out["fp16_shifted"] = res["fp16_shifted"]
     err_steps = 200
@@ -394,6 +395,61 @@ def adjoint_measurement(nsteps=2000, interval=45):
             "checkpoint_interval": interval, "forward_s": t_fwd, "backward_s": t_bwd,
             "plain_forward_s": ms_plain / 1e3, "adjoint_over_forward": t_bwd / t_fwd,
             "grad_dir_vs_central_fd_rel": abs(ad - fd) / abs(fd), "grad_tau": gtau}
+
+
+def batch_measurement(nsteps=5000, n_check=16, seq_steps=50):
+    """256 lid-driven cavities (sides U{64..512}, Re U[50,1000], lid
+    U[0.05,0.1], default_rng(0)) advanced together, FP32 shifted, nsteps steps
+    replayed from CUDA graphs; against one launch stream per cavity run one
+    after the other, and against FP64 runs of a sample of cavities."""
+    from pylabolt_gb300 import workloads
+    from pylabolt_gb300.batch import CavityBatch, draw_cavities
+    from pylabolt_gb300.config import Case
+    from pylabolt_gb300.lbm import FluidLBM
+    sides, res, lids = draw_cavities()
+    with CavityBatch(sides, res, lids) as b:
+        b.initialize()
+        b.step(3)
+        b.initialize()
+        b.step(1)
+        ms = b.time_steps(nsteps - 2)
+        b.step(1, moments=True)
+        ub = b.velocities()
+        variant = b.kernel_variant
+        nodes = b.fluid_nodes
+    batched = nodes * (nsteps - 2) / (ms / 1e3) / 1e6
+    # sequential: every cavity its own handle, stepped one after the other
+    sims = []
+    for i in range(len(sides)):
+        c = Case(workloads.cavity(int(sides[i]), re=float(res[i]), lid=float(lids[i])))
+        s = FluidLBM(c, storage="fp32_shifted")
+        s.initialize()
+        s.step(2)
+        s.synchronize()
+        sims.append(s)
+    t0 = time.perf_counter()
+    for s in sims:
+        s.step(seq_steps)
+    for s in sims:
+        s.synchronize()
+    t_seq = time.perf_counter() - t0
+    for s in sims:
+        s.close()
+    sequential = nodes * seq_steps / t_seq / 1e6
+    # FP64 per-cavity runs of a sample
+    rng = np.random.default_rng(1)
+    errs = []
+    for i in rng.choice(len(sides), size=n_check, replace=False):
+        c = Case(workloads.cavity(int(sides[i]), re=float(res[i]), lid=float(lids[i])))
+        with FluidLBM(c, storage="fp64") as s:
+            s.initialize()
+            s.step(nsteps, moments=True)
+            _, u = s.moments()
+        errs.append(float(np.abs(ub[i] - u).max() / np.abs(u).max()))
+    return {"workload": "256_cavities_U64-512_fp32_shifted", "steps": nsteps,
+            "fluid_nodes": nodes, "batched_mlups": batched,
+            "sequential_per_instance_mlups": sequential, "speedup": batched / sequential,
+            "kernel": list(variant), "max_err_vs_fp64": max(errs), "fp64_checked": n_check}
 
 
 def main():

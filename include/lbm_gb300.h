@@ -120,6 +120,13 @@ int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout
  * rho*g when cfg.body_force_field == 1 (extension: no reference key). */
 int lbm_set_body_force(LbmHandle* h, const double* force);
 
+/* Per-node relaxation rate omega [nx*ny] (inner layout), constant inside
+ * every 32-node row segment (x / 32) of fluid nodes; replaces cfg.omega for
+ * BGK with shifted storage.  Used to advance many cases of different
+ * viscosity in one grid (extension: the reference has one omega per run,
+ * collision_operator.py:89-91). */
+int lbm_set_omega_map(LbmHandle* h, const double* omega);
+
 /* Advances nsteps time steps, each one Solver.single_time_step
  * (pylabolt/solvers/fluidLB.py:206-253: density, force, velocity, collide,
  * periodic wrap, stream, boundaries) as one fused kernel launch.  Long runs

@@ -69,7 +69,7 @@ EXPORTS = ["lbm_create", "lbm_init_fields", "lbm_set_body_force", "lbm_step",
            "lbm_get_populations", "lbm_set_populations", "lbm_time",
            "lbm_kernel_launches", "lbm_kernel_variant", "lbm_tuning", "lbm_device_bytes", "lbm_time_steps",
            "lbm_synchronize", "lbm_last_error", "lbm_destroy", "lbm_conservation_noalloc",
-           "lbm_adjoint_forward", "lbm_adjoint_backward"]
+           "lbm_adjoint_forward", "lbm_adjoint_backward", "lbm_set_omega_map"]
 
 
 def lib_path():
@@ -109,6 +109,7 @@ def load(build=True):
         "lbm_destroy": [P],
         "lbm_conservation_noalloc": [ctypes.POINTER(LbmPopView), P, P],
         "lbm_adjoint_forward": [P, i64, ctypes.c_int],
+        "lbm_set_omega_map": [P, P],
         "lbm_adjoint_backward": [P, P, P, dbl, P],
     }
     for name, argtypes in sig.items():

@@ -60,6 +60,7 @@ struct LbmHandle {
   void* mom[3] = {nullptr, nullptr, nullptr};
   void* old[3] = {nullptr, nullptr, nullptr};
   void* body = nullptr;
+  float* omega_seg = nullptr;  // optional per-segment relaxation rate
   double* partials = nullptr;
   double* red = nullptr;       // device [16]: residual sums, conservation sums
   double* scratch = nullptr;   // device [kFinishBlocks*8]: first reduction stage
@@ -196,6 +197,7 @@ struct LbmHandle {
     a.partials = partials;
     a.body = body;
     a.err = err_dev;
+    a.omega_seg = omega_seg;
     a.flags = flags;
     LBM_CUDA(ks->step(cfg.collision, cfg.forcing, a, v, sms, stream));
     return LBM_OK;
@@ -633,6 +635,40 @@ int lbm_set_body_force(LbmHandle* h, const double* force) {
   LBM_CUDA(cudaMemsetAsync(ds, 0, 2 * plane * sizeof(double), h->stream));
   LBM_CUDA(lbm::reorder(h->g, hs, ds, 2, LBM_LAYOUT_INNER, 1, h->stream));
   LBM_CUDA(h->ks->body_from_f64(h->g, ds, h->body, h->stream));
+  return h->wait();
+}
+
+int lbm_set_omega_map(LbmHandle* h, const double* omega) {
+  if (!h || !omega) return fail(LBM_ERR_ARG, "lbm_set_omega_map: null argument");
+  if (h->cfg.precision == LBM_FP64 || h->cfg.collision != LBM_BGK)
+    return fail(LBM_ERR_ARG, "lbm_set_omega_map: needs BGK with shifted (FP32/FP16) storage");
+  const lbm::Geom& g = h->g;
+  const int nx = g.nx, ny = g.ny;
+  std::vector<float> seg((size_t)ny * g.nseg, (float)h->cfg.omega);
+  std::vector<uint8_t> set((size_t)ny * g.nseg, 0);
+  for (int x = 0; x < nx; ++x)
+    for (int y = 0; y < ny; ++y) {
+      if (h->h_cls[(long long)(y + 1) * g.pitch + x] >= 2) continue;   // solid
+      const double w = omega[(long long)x * ny + y];
+      if (!(w > 0.0 && w < 2.0)) return fail(LBM_ERR_ARG, "lbm_set_omega_map: omega must lie in (0, 2)");
+      const size_t i = (size_t)y * g.nseg + x / 32;
+      if (set[i] && seg[i] != (float)w)
+        return fail(LBM_ERR_ARG, "lbm_set_omega_map: omega differs inside the 32-node segment of node (" +
+                                     std::to_string(x) + "," + std::to_string(y) + ")");
+      seg[i] = (float)w;
+      set[i] = 1;
+    }
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  if (!h->omega_seg) {
+    int rc = h->alloc(reinterpret_cast<void**>(&h->omega_seg), seg.size() * sizeof(float));
+    if (rc) return rc;
+  }
+  LBM_CUDA(cudaMemcpyAsync(h->omega_seg, seg.data(), seg.size() * sizeof(float), cudaMemcpyHostToDevice,
+                           h->stream));
+  if (h->gexec) {   // graphs captured earlier hold the old argument
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
   return h->wait();
 }
 

@@ -65,6 +65,7 @@ struct StepArgs {
   double* partials;      // [nblocks*8] residual partial sums
   const void* body;      // [2*plane] body force or null
   int* err;              // device-visible error word (bounded waits)
+  const float* omega_seg;  // [ny*nseg] relaxation rate per 32-node segment, or null
   int flags;
 };
 

@@ -193,8 +193,8 @@ __device__ __forceinline__ T bgk_shift_k(T gk, T rho, T drho, T ux, T uy,
 // split the same way into its even and odd parts.
 template <int FORC>
 __device__ __forceinline__ void bgk_shift_pairs(float G[9], float rho, float drho, float ux,
-                                                float uy, float Fx, float Fy, const Params& p) {
-  const float om = p.f_omega;
+                                                float uy, float Fx, float Fy, const Params& p,
+                                                float om) {
   const float A = drho - 1.5f * rho * (ux * ux + uy * uy);
   const float r3 = 3.f * rho;
   G[0] += om * (p.f_wsc[0] * A - G[0]);
@@ -212,10 +212,12 @@ __device__ __forceinline__ void bgk_shift_pairs(float G[9], float rho, float drh
   if (FORC != 0) {
     const float cfs[4] = {Fx, Fy, Fx + Fy, Fy - Fx};
     const float uF = ux * Fx + uy * Fy;
-    if (FORC == 2) G[0] += p.f_omh[0] * (-3.f * uF);
+    // (1 - omega/2) w scale; recomputed when omega comes from a map
+    const float hs = om == p.f_omega ? 1.f : (1.f - 0.5f * om) / (1.f - 0.5f * p.f_omega);
+    if (FORC == 2) G[0] += hs * p.f_omh[0] * (-3.f * uF);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const float h = p.f_omh[j < 2 ? 1 : 2];
+      const float h = hs * p.f_omh[j < 2 ? 1 : 2];
       const float O = 3.f * cfs[j];
       const float E = FORC == 2 ? 9.f * cus[j] * cfs[j] - 3.f * uF : 0.f;
       G[ks[j]] += h * (E + O);
@@ -353,11 +355,13 @@ __device__ __forceinline__ R warp_sum(R v) {
 // Moments, force, velocity and collision of one node: f holds the incoming
 // populations (f, or g = f - w when shifted) and receives the post-collision
 // ones.
+// `seg` is the node's 32-node row segment (y * nseg + x / 32), used to read a
+// per-segment relaxation rate when the case has one (batched cases).
 template <class S, int COLL, int FORC>
 __device__ __forceinline__ void node_update(typename Store<S>::T f[9], const StepArgs& a,
                                             long long n, typename Store<S>::T& rho,
                                             typename Store<S>::T& ux,
-                                            typename Store<S>::T& uy) {
+                                            typename Store<S>::T& uy, int seg) {
   using T = typename Store<S>::T;
   constexpr bool SH = Store<S>::shifted;
   const Params& p = a.p;
@@ -416,7 +420,8 @@ __device__ __forceinline__ void node_update(typename Store<S>::T f[9], const Ste
     f[7] = bgk_ref_k<7, FORC>(f[7], rho, ux, uy, hu2, Fx, Fy, p);
     f[8] = bgk_ref_k<8, FORC>(f[8], rho, ux, uy, hu2, Fx, Fy, p);
   } else {
-    bgk_shift_pairs<FORC>(f, rho, drho, ux, uy, Fx, Fy, p);
+    const float om = a.omega_seg ? a.omega_seg[seg] : p.f_omega;
+    bgk_shift_pairs<FORC>(f, rho, drho, ux, uy, Fx, Fy, p, om);
   }
 }
 
@@ -533,7 +538,7 @@ __global__ void __launch_bounds__(CAP ? 256 : 512, CAP ? 8 : 1) step_kernel(cons
         special_links<S>(f, a, fin, n, r);
       }
       T rho, ux, uy;
-      node_update<S, COLL, FORC>(f, a, n, rho, ux, uy);
+      node_update<S, COLL, FORC>(f, a, n, rho, ux, uy, y * g.nseg + (x >> 5));
 #pragma unroll
       for (int k = 0; k < 9; ++k) Store<S>::str(fout, k * g.plane + n, f[k]);
       node_outputs<T>(a, n, r, rho, ux, uy, red);
@@ -686,7 +691,7 @@ __global__ void __launch_bounds__(256) step_vec_kernel(const StepArgs a) {
           if (!nopull) special_links<S>(fn, a, fin, n0 + v, r);
         }
         float rho, ux, uy;
-        node_update<S, COLL, FORC>(fn, a, n0 + v, rho, ux, uy);
+        node_update<S, COLL, FORC>(fn, a, n0 + v, rho, ux, uy, y * g.nseg + ((x0 + v) >> 5));
 #pragma unroll
         for (int k = 0; k < 9; ++k) f[k][v] = fn[k];
         node_outputs<float>(a, n0 + v, r, rho, ux, uy, red);
@@ -851,7 +856,7 @@ __global__ void __launch_bounds__(1024) step_tma_kernel(const StepArgs a, int st
         if (!nopull) special_links<S>(f, a, fin, n, r);
       }
       float rho, ux, uy;
-      node_update<S, COLL, FORC>(f, a, n, rho, ux, uy);
+      node_update<S, COLL, FORC>(f, a, n, rho, ux, uy, y * g.nseg + (x >> 5));
 #pragma unroll
       for (int k = 0; k < 9; ++k) Store<S>::str(fout, k * g.plane + n, f[k]);
       node_outputs<float>(a, n, r, rho, ux, uy, red);

@@ -29,7 +29,8 @@ def test_batch_equals_single_cavities():
             s.initialize()
             s.step(steps, moments=True)
             _, u64 = s.moments()
-        assert np.abs(ub[i] - u64).max() <= 1e-5 * np.abs(u64).max()
+        # FP32 storage vs FP64: worst node at the singular lid corners
+        assert np.abs(ub[i] - u64).max() <= 3e-5 * np.abs(u64).max()
 
 
 def test_omega_map_rejects_mixed_segment():

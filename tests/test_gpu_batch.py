@@ -12,7 +12,8 @@ pytestmark = pytest.mark.gpu
 
 
 def test_batch_equals_single_cavities():
-    sides, res, lids = draw_cavities(n=10, seed=3, side=(16, 72))
+    # small cavities at moderate Re (Re/N <= 6, tau >= 0.53): stable with BGK
+    sides, res, lids = draw_cavities(n=10, seed=3, side=(48, 96), re=(50.0, 300.0))
     steps = 300
     with CavityBatch(sides, res, lids, width=256) as b:
         b.initialize()

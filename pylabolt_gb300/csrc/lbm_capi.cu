@@ -98,10 +98,16 @@ struct LbmHandle {
     double* grad_u = nullptr;      // [2][plane]
     long long nparts = 0;
     bool ready = false;
+    // both passes are captured once per (T, interval) plan and replayed
+    cudaGraphExec_t fwd_graph = nullptr, bwd_graph = nullptr;
+    int64_t graph_T = -1;
+    int graph_interval = -1;
   } adj;
 
   ~LbmHandle() {
     if (gexec) cudaGraphExecDestroy(gexec);
+    if (adj.fwd_graph) cudaGraphExecDestroy(adj.fwd_graph);
+    if (adj.bwd_graph) cudaGraphExecDestroy(adj.bwd_graph);
     for (void* a : allocs) cudaFree(a);
     if (host_red) cudaFreeHost(host_red);
     if (err_host) cudaFreeHost(err_host);
@@ -280,6 +286,27 @@ struct LbmHandle {
 
   // state buffers hold a guard row before plane 0, like pop_raw
   void* state_base(void* raw) const { return static_cast<char*>(raw) + g.pitch * ks->elem_bytes; }
+
+  // Captures the work `enqueue` puts on the stream into an executable graph.
+  template <class F>
+  int capture(cudaGraphExec_t* out, F&& enqueue) {
+    cudaGraph_t graph = nullptr;
+    LBM_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue();
+    cudaError_t e = cudaStreamEndCapture(stream, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      *out = nullptr;
+      return fail(LBM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+    return LBM_OK;
+  }
 
   long long nparts_of(lbm::Variant v) const {
     const dim3 gr = lbm::step_grid(g, v, sms, ks->elem_bytes);
@@ -772,18 +799,48 @@ int lbm_adjoint_forward(LbmHandle* h, int64_t nsteps, int interval) {
     A.ready = true;
   }
   if (!h->tuned && (rc = h->autotune())) return rc;
-  // t = 0: the initial populations (read without pulling)
-  LBM_CUDA(cudaMemcpyAsync(h->state_base(A.ckpt[0]), h->pop[h->cur], 9 * h->g.plane * h->ks->elem_bytes,
-                           cudaMemcpyDeviceToDevice, h->stream));
-  for (int64_t t = 1; t <= nsteps; ++t) {
-    const int fl = (t == 1 ? lbm::F_NOPULL : 0) | (t == nsteps ? lbm::F_MOMENTS : 0);
-    if ((rc = h->launch(fl))) return rc;
-    if (t % interval == 0 && t < nsteps) {
-      const int64_t c = t / interval;
-      LBM_CUDA(cudaMemcpyAsync(h->state_base(A.ckpt[c]), h->pop[h->cur], 9 * h->g.plane * h->ks->elem_bytes,
-                               cudaMemcpyDeviceToDevice, h->stream));
-      LBM_CUDA(cudaMemcpyAsync(A.ckpt_side[c], h->side[h->cur], h->side_bytes(), cudaMemcpyDeviceToDevice, h->stream));
+  const bool use_graph = !std::getenv("LBM_NO_GRAPH");
+  if (use_graph && (A.graph_T != nsteps || A.graph_interval != interval)) {
+    if (A.fwd_graph) cudaGraphExecDestroy(A.fwd_graph);
+    if (A.bwd_graph) cudaGraphExecDestroy(A.bwd_graph);
+    A.fwd_graph = A.bwd_graph = nullptr;
+    A.graph_T = nsteps;
+    A.graph_interval = interval;
+  }
+  // the pass starts from buffer 0 so that one captured graph fits every call
+  if (h->cur != 0) {
+    LBM_CUDA(cudaMemcpyAsync(h->pop[0], h->pop[1], 9 * h->g.plane * h->ks->elem_bytes,
+                             cudaMemcpyDeviceToDevice, h->stream));
+    h->cur = 0;
+  }
+  auto enqueue = [&]() -> int {
+    // t = 0: the initial populations (read without pulling)
+    LBM_CUDA(cudaMemcpyAsync(h->state_base(A.ckpt[0]), h->pop[h->cur], 9 * h->g.plane * h->ks->elem_bytes,
+                             cudaMemcpyDeviceToDevice, h->stream));
+    for (int64_t t = 1; t <= nsteps; ++t) {
+      const int fl = (t == 1 ? lbm::F_NOPULL : 0) | (t == nsteps ? lbm::F_MOMENTS : 0);
+      int r = h->launch(fl);
+      if (r) return r;
+      if (t % interval == 0 && t < nsteps) {
+        const int64_t c = t / interval;
+        LBM_CUDA(cudaMemcpyAsync(h->state_base(A.ckpt[c]), h->pop[h->cur], 9 * h->g.plane * h->ks->elem_bytes,
+                                 cudaMemcpyDeviceToDevice, h->stream));
+        LBM_CUDA(cudaMemcpyAsync(A.ckpt_side[c], h->side[h->cur], h->side_bytes(), cudaMemcpyDeviceToDevice,
+                                 h->stream));
+      }
     }
+    return LBM_OK;
+  };
+  if (use_graph) {
+    if (!A.fwd_graph) {
+      rc = h->capture(&A.fwd_graph, enqueue);
+      h->cur = 0;   // capture only recorded the launches
+      if (rc) return rc;
+    }
+    LBM_CUDA(cudaGraphLaunch(A.fwd_graph, h->stream));
+    h->cur = (int)(nsteps & 1);
+  } else if ((rc = enqueue())) {
+    return rc;
   }
   h->nopull = false;
   h->t = nsteps;
@@ -806,44 +863,53 @@ int lbm_adjoint_backward(LbmHandle* h, const double* grad_u, double* grad_force,
   if (rc) return rc;
   LBM_CUDA(cudaMemcpyAsync(h->stage, grad_u, 2 * nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   LBM_CUDA(lbm::reorder(g, h->stage, A.grad_u, 2, LBM_LAYOUT_INNER, 1, h->stream));
-  LBM_CUDA(cudaMemsetAsync(A.gF, 0, 2 * g.plane * (size_t)h->ks->compute_bytes, h->stream));
-  LBM_CUDA(cudaMemsetAsync(A.gpart, 0, A.nparts * 4 * sizeof(double), h->stream));
   const int I = A.interval;
   const int64_t T = A.T;
   const lbm::Variant plain = h->variant;
-  int cur_a = 0;
-  bool have_next = false;
-  for (int64_t c = (T - 1) / I; c >= 0; --c) {
-    const int64_t t0 = c * I, t1 = std::min<int64_t>(t0 + I, T);
-    // recompute p_{t0+1} .. p_{t1-1} into the segment buffers
-    for (int64_t t = t0 + 1; t < t1; ++t) {
-      const void* fin = t == t0 + 1 ? h->state_base(A.ckpt[c]) : h->state_base(A.seg[t - t0 - 2]);
-      const void* sin = t == t0 + 1 ? A.ckpt_side[c] : A.seg_side[t - t0 - 2];
-      if ((rc = h->launch_bufs(t == 1 ? lbm::F_NOPULL : 0, plain, fin, h->state_base(A.seg[t - t0 - 1]), sin,
-                               A.seg_side[t - t0 - 1])))
-        return rc;
+  auto enqueue = [&]() -> int {
+    LBM_CUDA(cudaMemsetAsync(A.gF, 0, 2 * g.plane * (size_t)h->ks->compute_bytes, h->stream));
+    LBM_CUDA(cudaMemsetAsync(A.gpart, 0, A.nparts * 4 * sizeof(double), h->stream));
+    int cur_a = 0;
+    bool have_next = false;
+    for (int64_t c = (T - 1) / I; c >= 0; --c) {
+      const int64_t t0 = c * I, t1 = std::min<int64_t>(t0 + I, T);
+      // recompute p_{t0+1} .. p_{t1-1} into the segment buffers
+      for (int64_t t = t0 + 1; t < t1; ++t) {
+        const void* fin = t == t0 + 1 ? h->state_base(A.ckpt[c]) : h->state_base(A.seg[t - t0 - 2]);
+        const void* sin = t == t0 + 1 ? A.ckpt_side[c] : A.seg_side[t - t0 - 2];
+        int r = h->launch_bufs(t == 1 ? lbm::F_NOPULL : 0, plain, fin, h->state_base(A.seg[t - t0 - 1]), sin,
+                               A.seg_side[t - t0 - 1]);
+        if (r) return r;
+      }
+      // reverse steps t1 .. t0+1
+      for (int64_t t = t1; t > t0; --t) {
+        lbm::AdjArgs a;
+        a.g = g;
+        a.p = h->p;
+        a.fprev = t - 1 == t0 ? h->state_base(A.ckpt[c]) : h->state_base(A.seg[t - t0 - 2]);
+        a.side_prev = t - 1 == t0 ? A.ckpt_side[c] : A.seg_side[t - t0 - 2];
+        a.a_next = have_next ? A.a[cur_a] : nullptr;
+        a.a_cur = A.a[cur_a ^ 1];
+        a.grad_u = t == T ? A.grad_u : nullptr;
+        a.gF = h->body ? A.gF : nullptr;
+        a.gpart = A.gpart;
+        a.tr_reader = A.tr_reader;
+        a.tr_self = A.tr_self;
+        a.wall_rec = A.wall_rec;
+        a.body = h->body;
+        a.nopull = t == 1;
+        LBM_CUDA(h->ks->adjoint(h->cfg.forcing, a, h->stream));
+        cur_a ^= 1;
+        have_next = true;
+      }
     }
-    // reverse steps t1 .. t0+1
-    for (int64_t t = t1; t > t0; --t) {
-      lbm::AdjArgs a;
-      a.g = g;
-      a.p = h->p;
-      a.fprev = t - 1 == t0 ? h->state_base(A.ckpt[c]) : h->state_base(A.seg[t - t0 - 2]);
-      a.side_prev = t - 1 == t0 ? A.ckpt_side[c] : A.seg_side[t - t0 - 2];
-      a.a_next = have_next ? A.a[cur_a] : nullptr;
-      a.a_cur = A.a[cur_a ^ 1];
-      a.grad_u = t == T ? A.grad_u : nullptr;
-      a.gF = h->body ? A.gF : nullptr;
-      a.gpart = A.gpart;
-      a.tr_reader = A.tr_reader;
-      a.tr_self = A.tr_self;
-      a.wall_rec = A.wall_rec;
-      a.body = h->body;
-      a.nopull = t == 1;
-      LBM_CUDA(h->ks->adjoint(h->cfg.forcing, a, h->stream));
-      cur_a ^= 1;
-      have_next = true;
-    }
+    return LBM_OK;
+  };
+  if (!std::getenv("LBM_NO_GRAPH")) {
+    if (!A.bwd_graph && (rc = h->capture(&A.bwd_graph, enqueue))) return rc;
+    LBM_CUDA(cudaGraphLaunch(A.bwd_graph, h->stream));
+  } else if ((rc = enqueue())) {
+    return rc;
   }
   // parameter gradients: fixed-order sum of the per-block rows on the host
   std::vector<double> part(A.nparts * 4);

@@ -99,41 +99,48 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjArgs a) {
           }
         }
       }
-      // ---- 3. reverse mode through the collision
-      T adj_rho = T(0), adj_ux = T(0), adj_uy = T(0), adj_Fx = T(0), adj_Fy = T(0);
-      T g_om = T(0);
+      // ---- 3. reverse mode through the collision, through the moments of A:
+      // every sum over k below is sum_k A_k w_k P(c_k) with P of degree <= 2,
+      // i.e. a combination of M0 = sum A w, Mc = sum A w c, Mcc = sum A w c c.
+      const T w1 = T(1.0 / 9.0), w2 = T(1.0 / 36.0);
+      const T d13 = A[1] - A[3], d24 = A[2] - A[4];
+      const T s13 = A[1] + A[3], s24 = A[2] + A[4];
+      const T s5678 = (A[5] + A[7]) + (A[6] + A[8]);
+      const T M0 = T(4.0 / 9.0) * A[0] + w1 * (s13 + s24) + w2 * s5678;
+      const T Mx = w1 * d13 + w2 * ((A[5] - A[7]) + (A[8] - A[6]));
+      const T My = w1 * d24 + w2 * ((A[5] - A[7]) + (A[6] - A[8]));
+      const T Mxx = w1 * s13 + w2 * s5678;
+      const T Myy = w1 * s24 + w2 * s5678;
+      const T Mxy = w2 * ((A[5] + A[7]) - (A[6] + A[8]));
+      const T uMc = ux * Mx + uy * My;
+      const T Mccux = Mxx * ux + Mxy * uy, Mccuy = Mxy * ux + Myy * uy;   // Mcc u
+      const T uMccu = ux * Mccux + uy * Mccuy;
+      // sum_k A_k f_eq,k = rho B,  B = sum_k A_k w_k E_k
+      const T Bm1 = -T(0.5) * i2 * u2 * M0 + i2 * uMc + T(0.5) * i4 * uMccu;   // B - M0
+      T adj_rho = om * (M0 + Bm1);
+      T adj_ux = om * rho * (i2 * Mx + i4 * Mccux - i2 * ux * M0);
+      T adj_uy = om * rho * (i2 * My + i4 * Mccuy - i2 * uy * M0);
+      T adj_Fx = T(0), adj_Fy = T(0);
+      // sum_k A_k (f_eq,k - f_k): in shifted storage f = g + w, so
+      // rho B - sum A f = M0 drho + rho (B - M0) - sum A g (no cancellation)
+      T sAf = T(0);
 #pragma unroll
-      for (int k = 0; k < 9; ++k) {
-        const T cx = T(CXk(k)), cy = T(CYk(k)), w = T(Wk(k));
-        const T cu = cx * ux + cy * uy;
-        const T E = T(1) + i2 * cu + T(0.5) * i4 * cu * cu - T(0.5) * i2 * u2;
-        const T Ak = A[k];
-        // f_eq_k = w rho E ; p_k = f_k + om (f_eq_k - f_k) + omh Fbar_k
-        adj_rho += om * Ak * w * E;
-        const T dEx = i2 * cx + i4 * cu * cx - i2 * ux;
-        const T dEy = i2 * cy + i4 * cu * cy - i2 * uy;
-        adj_ux += om * Ak * w * rho * dEx;
-        adj_uy += om * Ak * w * rho * dEy;
-        // f_eq - f in the stored representation (g_eq - g when shifted)
-        const T feq_minus_f = SH ? w * (drho + rho * (E - T(1))) - f[k] : w * rho * E - f[k];
-        T Fbar = T(0);
-        if (FORC == 1) {
-          const T cF = cx * Fx + cy * Fy;
-          Fbar = w * i2 * cF;
-          adj_Fx += omh * Ak * w * i2 * cx;
-          adj_Fy += omh * Ak * w * i2 * cy;
-        } else if (FORC == 2) {
-          const T cF = cx * Fx + cy * Fy;
-          const T ex = (cx - ux) * i2 + cu * cx * i4;
-          const T ey = (cy - uy) * i2 + cu * cy * i4;
-          Fbar = w * (ex * Fx + ey * Fy);
-          adj_Fx += omh * Ak * w * ex;
-          adj_Fy += omh * Ak * w * ey;
-          // d Fbar / du = w (-i2 F + i4 (c.F) c)
-          adj_ux += omh * Ak * w * (-i2 * Fx + i4 * cF * cx);
-          adj_uy += omh * Ak * w * (-i2 * Fy + i4 * cF * cy);
-        }
-        g_om += Ak * (feq_minus_f - T(0.5) * Fbar);
+      for (int k = 0; k < 9; ++k) sAf += A[k] * f[k];
+      T g_om = SH ? M0 * drho + rho * Bm1 - sAf : rho * (M0 + Bm1) - sAf;
+      if (FORC == 1) {
+        const T sAF = i2 * (Mx * Fx + My * Fy);          // sum A Fbar
+        g_om -= T(0.5) * sAF;
+        adj_Fx += omh * i2 * Mx;
+        adj_Fy += omh * i2 * My;
+      } else if (FORC == 2) {
+        const T uF = ux * Fx + uy * Fy;
+        const T MccFx = Mxx * Fx + Mxy * Fy, MccFy = Mxy * Fx + Myy * Fy;
+        const T sAF = i2 * (Mx * Fx + My * Fy) - i2 * M0 * uF + i4 * (ux * MccFx + uy * MccFy);
+        g_om -= T(0.5) * sAF;
+        adj_Fx += omh * (i2 * Mx - i2 * M0 * ux + i4 * Mccux);
+        adj_Fy += omh * (i2 * My - i2 * M0 * uy + i4 * Mccuy);
+        adj_ux += omh * (-i2 * M0 * Fx + i4 * MccFx);
+        adj_uy += omh * (-i2 * M0 * Fy + i4 * MccFy);
       }
       if (a.grad_u) {  // loss term: dL/du^T of this node
         adj_ux += T(a.grad_u[n]);

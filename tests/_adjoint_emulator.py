@@ -94,28 +94,31 @@ def adjoint(case, nsteps, grad_u, force=None):
                         rd = tr_reader[r, m]
                         A[m] = (a_next[rd, m] if rd >= 0 else 0.0) + \
                             (a_next[s, INV[m]] if tr_self[r, m] else 0.0)
-            adj_rho = adj_ux = adj_uy = adj_Fx = adj_Fy = 0.0
-            for k in range(9):
-                cu = CX[k] * ux + CY[k] * uy
-                E = 1 + i2 * cu + 0.5 * i4 * cu * cu - 0.5 * i2 * u2
-                adj_rho += om * A[k] * W[k] * E
-                adj_ux += om * A[k] * W[k] * rho * (i2 * CX[k] + i4 * cu * CX[k] - i2 * ux)
-                adj_uy += om * A[k] * W[k] * rho * (i2 * CY[k] + i4 * cu * CY[k] - i2 * uy)
-                fbar = 0.0
-                if forc == 1:
-                    fbar = W[k] * i2 * (CX[k] * Fx + CY[k] * Fy)
-                    adj_Fx += omh * A[k] * W[k] * i2 * CX[k]
-                    adj_Fy += omh * A[k] * W[k] * i2 * CY[k]
-                elif forc == 2:
-                    cF = CX[k] * Fx + CY[k] * Fy
-                    ex = (CX[k] - ux) * i2 + cu * CX[k] * i4
-                    ey = (CY[k] - uy) * i2 + cu * CY[k] * i4
-                    fbar = W[k] * (ex * Fx + ey * Fy)
-                    adj_Fx += omh * A[k] * W[k] * ex
-                    adj_Fy += omh * A[k] * W[k] * ey
-                    adj_ux += omh * A[k] * W[k] * (-i2 * Fx + i4 * cF * CX[k])
-                    adj_uy += omh * A[k] * W[k] * (-i2 * Fy + i4 * cF * CY[k])
-                g_om += A[k] * (W[k] * rho * E - f[k] - 0.5 * fbar)
+            # moments of A (lbm_adjoint.cuh step 3)
+            M0 = (W * A).sum()
+            Mx, My = (W * CX * A).sum(), (W * CY * A).sum()
+            Mxx, Myy, Mxy = (W * CX * CX * A).sum(), (W * CY * CY * A).sum(), (W * CX * CY * A).sum()
+            uMc = ux * Mx + uy * My
+            Mccux, Mccuy = Mxx * ux + Mxy * uy, Mxy * ux + Myy * uy
+            uMccu = ux * Mccux + uy * Mccuy
+            Bm1 = -0.5 * i2 * u2 * M0 + i2 * uMc + 0.5 * i4 * uMccu
+            adj_rho = om * (M0 + Bm1)
+            adj_ux = om * rho * (i2 * Mx + i4 * Mccux - i2 * ux * M0)
+            adj_uy = om * rho * (i2 * My + i4 * Mccuy - i2 * uy * M0)
+            adj_Fx = adj_Fy = 0.0
+            g_om += rho * (M0 + Bm1) - (A * f).sum()
+            if forc == 1:
+                g_om -= 0.5 * i2 * (Mx * Fx + My * Fy)
+                adj_Fx += omh * i2 * Mx
+                adj_Fy += omh * i2 * My
+            elif forc == 2:
+                uF = ux * Fx + uy * Fy
+                MccFx, MccFy = Mxx * Fx + Mxy * Fy, Mxy * Fx + Myy * Fy
+                g_om -= 0.5 * (i2 * (Mx * Fx + My * Fy) - i2 * M0 * uF + i4 * (ux * MccFx + uy * MccFy))
+                adj_Fx += omh * (i2 * Mx - i2 * M0 * ux + i4 * Mccux)
+                adj_Fy += omh * (i2 * My - i2 * M0 * uy + i4 * Mccuy)
+                adj_ux += omh * (-i2 * M0 * Fx + i4 * MccFx)
+                adj_uy += omh * (-i2 * M0 * Fy + i4 * MccFy)
             if t == nsteps:
                 adj_ux += grad_u[s, 0]
                 adj_uy += grad_u[s, 1]

@@ -18,10 +18,18 @@
 #pragma once
 #include "lbm_kernels.cuh"
 
+// Resident 256-thread blocks per SM asked of ptxas.  The kernel is latency
+// bound: 4 blocks (64 registers, no spills) for the FP32 adjoint; the FP64
+// adjoint spills below 128 registers, so 2.
+#ifndef LBM_ADJ_MIN_BLOCKS
+#define LBM_ADJ_MIN_BLOCKS 4
+#endif
+
 namespace lbm {
 
 template <class S, int FORC>
-__global__ void __launch_bounds__(256) adjoint_kernel(const AdjArgs a) {
+__global__ void __launch_bounds__(256, sizeof(typename Store<S>::T) == 4 ? LBM_ADJ_MIN_BLOCKS : 2)
+    adjoint_kernel(const AdjArgs a) {
   using T = typename Store<S>::T;
   constexpr bool SH = Store<S>::shifted;
   const Geom& g = a.g;
@@ -29,6 +37,16 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   T red[3] = {0, 0, 0};
+  // this warp's running sums, fetched before the node's loads so that the
+  // read-modify-write at the end costs no extra memory round trip
+  const int lane = threadIdx.x & 31;
+  const long long slot = ((long long)blockIdx.y * gridDim.x + blockIdx.x) * (blockDim.x >> 5) +
+                         (threadIdx.x >> 5);
+  double run[3] = {0, 0, 0};
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) run[i] = a.gpart[slot * 4 + i];
+  }
   if (x < g.nx) {
     const long long n = g.node(x, y);
     const int cls = g.cls[n];
@@ -37,6 +55,12 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjArgs a) {
       const T* __restrict__ an = static_cast<const T*>(a.a_next);
       T* __restrict__ ac = static_cast<T*>(a.a_cur);
       const int r = cls == 1 ? g.recmap[n] : -1;
+      T gF0 = T(0), gF1 = T(0);   // running dL/dF of this node, fetched early
+      if (a.gF) {
+        const T* gF = static_cast<const T*>(a.gF);
+        gF0 = gF[n];
+        gF1 = gF[g.plane + n];
+      }
       // ---- 1. f^t(n): physical deviations g (shifted) or f (FP64)
       T f[9];
       if (a.nopull) {
@@ -61,8 +85,10 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjArgs a) {
       // ---- forward quantities
       T rho, drho, jx, jy;
       moments<SH>(f, rho, drho, jx, jy);
-      const T i2 = T(p.inv_cs_2), i4 = T(p.inv_cs_4);
-      const T om = T(p.omega), omh = T(p.one_m_half_omega);
+      // FP32 constants come pre-converted (an FP64 -> FP32 conversion per
+      // thread would run on GB300's slow FP64 pipe)
+      const T i2 = SH ? T(p.f_i2) : T(p.inv_cs_2), i4 = SH ? T(p.f_i4) : T(p.inv_cs_4);
+      const T om = SH ? T(p.f_omega) : T(p.omega), omh = SH ? T(p.f_homh) : T(p.one_m_half_omega);
       T Fx = T(0), Fy = T(0), dFx = T(0), dFy = T(0);  // dF = dF/drho
       if (FORC != 0) {
         if (a.body) {
@@ -70,8 +96,8 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjArgs a) {
           Fx = body[n];
           Fy = body[g.plane + n];
         } else {
-          dFx = T(p.gx);
-          dFy = T(p.gy);
+          dFx = SH ? T(p.f_gx) : T(p.gx);
+          dFy = SH ? T(p.f_gy) : T(p.gy);
           Fx = rho * dFx;
           Fy = rho * dFy;
         }
@@ -176,27 +202,20 @@ __global__ void __launch_bounds__(256) adjoint_kernel(const AdjArgs a) {
       }
       if (a.gF) {
         T* gF = static_cast<T*>(a.gF);
-        gF[n] += adj_Fx;
-        gF[g.plane + n] += adj_Fy;
+        gF[n] = gF0 + adj_Fx;
+        gF[g.plane + n] = gF1 + adj_Fy;
       }
       red[0] = g_om;
       red[1] = guw_x;
       red[2] = guw_y;
     }
   }
-  // block sums, accumulated into this block's slot across reverse steps
-  __shared__ double sh[32][3];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // warp sums, accumulated into this warp's slot across reverse steps (fixed
+  // slots, so the final sum is deterministic; no block barrier)
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     const T v = warp_sum<T>(red[i]);
-    if (lane == 0) sh[wid][i] = double(v);
-  }
-  __syncthreads();
-  if (threadIdx.x < 3) {
-    double s = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh[w][threadIdx.x];
-    a.gpart[((long long)blockIdx.y * gridDim.x + blockIdx.x) * 4 + threadIdx.x] += s;
+    if (lane == 0) a.gpart[slot * 4 + i] = run[i] + double(v);
   }
 }
 

@@ -91,7 +91,12 @@ struct LbmHandle {
     int8_t* wall_rec = nullptr;
     int64_t T = 0;
     int interval = 0;
-    std::vector<void*> ckpt, ckpt_side, seg, seg_side;
+    std::vector<void*> ckpt, ckpt_side;
+    // two sets of interval-1 recomputed states: the backward recomputes the
+    // next segment into one set (on `aux`) while the reverse steps read the other
+    std::vector<void*> seg, seg_side;
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // fork, join, R[2], A[2]
     void* a[2] = {nullptr, nullptr};
     void* gF = nullptr;
     double* gpart = nullptr;
@@ -108,6 +113,9 @@ struct LbmHandle {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (adj.fwd_graph) cudaGraphExecDestroy(adj.fwd_graph);
     if (adj.bwd_graph) cudaGraphExecDestroy(adj.bwd_graph);
+    for (cudaEvent_t e : adj.ev)
+      if (e) cudaEventDestroy(e);
+    if (adj.aux) cudaStreamDestroy(adj.aux);
     for (void* a : allocs) cudaFree(a);
     if (host_red) cudaFreeHost(host_red);
     if (err_host) cudaFreeHost(err_host);
@@ -186,7 +194,7 @@ struct LbmHandle {
 
   // One fused step from `fin` / `side_in` into `fout` / `side_out`.
   int launch_bufs(int flags, lbm::Variant v, const void* fin, void* fout, const void* sin,
-                  void* sout) {
+                  void* sout, cudaStream_t on = nullptr) {
     lbm::StepArgs a;
     a.g = g;
     a.p = p;
@@ -205,7 +213,7 @@ struct LbmHandle {
     a.err = err_dev;
     a.omega_seg = omega_seg;
     a.flags = flags;
-    LBM_CUDA(ks->step(cfg.collision, cfg.forcing, a, v, sms, stream));
+    LBM_CUDA(ks->step(cfg.collision, cfg.forcing, a, v, sms, on ? on : stream));
     return LBM_OK;
   }
 
@@ -500,7 +508,11 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   if (std::getenv("LBM_FAIL_ALLOC")) return bail(fail(LBM_ERR_ALLOC, "device allocation refused (LBM_FAIL_ALLOC is set)"));
   cudaError_t e = cudaSetDevice(c.device);
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e)));
-  e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  // the handle's stream at the highest priority (the adjoint's recompute
+  // stream runs below it)
+  int prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  e = cudaStreamCreateWithPriority(&h->stream, cudaStreamNonBlocking, prio_hi);
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
 
   lbm::Geom& g = h->g;
@@ -601,6 +613,9 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
     p.f_gy = (float)p.gy;
     p.f_scale = (float)p.scale;
     p.f_inv_scale = (float)p.inv_scale;
+    p.f_i2 = (float)p.inv_cs_2;
+    p.f_i4 = (float)p.inv_cs_4;
+    p.f_homh = (float)p.one_m_half_omega;
   }
   if (c.body_force_field) {
     if ((rc = h->alloc(&h->body, 2 * plane * cb))) return bail(rc);
@@ -775,7 +790,7 @@ int lbm_adjoint_forward(LbmHandle* h, int64_t nsteps, int interval) {
           }
     A.ckpt.assign(nck, nullptr);
     A.ckpt_side.assign(nck, nullptr);
-    A.seg.assign(interval > 1 ? interval - 1 : 0, nullptr);
+    A.seg.assign(interval > 1 ? 2 * (interval - 1) : 0, nullptr);
     A.seg_side.assign(A.seg.size(), nullptr);
     for (size_t i = 0; i < A.ckpt.size(); ++i)
       if ((rc = h->alloc(&A.ckpt[i], h->state_bytes())) || (rc = h->alloc(&A.ckpt_side[i], h->side_bytes())))
@@ -785,7 +800,7 @@ int lbm_adjoint_forward(LbmHandle* h, int64_t nsteps, int interval) {
         return rc;
     if (!A.a[0]) {
       const size_t ab = 9 * h->g.plane * (size_t)h->ks->compute_bytes;
-      A.nparts = h->nparts_of(lbm::Variant{0, 1, 256, 0});
+      A.nparts = h->nparts_of(lbm::Variant{0, 1, 256, 0}) * 8;   // one row per warp
       if ((rc = h->alloc(&A.a[0], ab)) || (rc = h->alloc(&A.a[1], ab)) ||
           (rc = h->alloc(&A.gF, 2 * h->g.plane * (size_t)h->ks->compute_bytes)) ||
           (rc = h->alloc(reinterpret_cast<void**>(&A.gpart), A.nparts * 4 * sizeof(double))) ||
@@ -794,6 +809,14 @@ int lbm_adjoint_forward(LbmHandle* h, int64_t nsteps, int interval) {
       LBM_CUDA(cudaMemsetAsync(A.a[0], 0, ab, h->stream));
       LBM_CUDA(cudaMemsetAsync(A.a[1], 0, ab, h->stream));
       LBM_CUDA(cudaMemsetAsync(A.grad_u, 0, 2 * h->g.plane * sizeof(double), h->stream));
+    }
+    if (!A.aux) {
+      // the recompute stream runs at the lowest priority: the reverse steps on
+      // the handle's stream are the critical path
+      int lo = 0, hi = 0;
+      LBM_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+      LBM_CUDA(cudaStreamCreateWithPriority(&A.aux, cudaStreamNonBlocking, lo));
+      for (cudaEvent_t& e : A.ev) LBM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
     A.interval = interval;
     A.ready = true;
@@ -871,23 +894,35 @@ int lbm_adjoint_backward(LbmHandle* h, const double* grad_u, double* grad_force,
     LBM_CUDA(cudaMemsetAsync(A.gpart, 0, A.nparts * 4 * sizeof(double), h->stream));
     int cur_a = 0;
     bool have_next = false;
-    for (int64_t c = (T - 1) / I; c >= 0; --c) {
+    const int64_t C = (T - 1) / I;
+    cudaEvent_t* const evR = A.ev + 2;
+    cudaEvent_t* const evA = A.ev + 4;
+    LBM_CUDA(cudaEventRecord(A.ev[0], h->stream));   // fork
+    LBM_CUDA(cudaStreamWaitEvent(A.aux, A.ev[0], 0));
+    for (int64_t c = C; c >= 0; --c) {
       const int64_t t0 = c * I, t1 = std::min<int64_t>(t0 + I, T);
-      // recompute p_{t0+1} .. p_{t1-1} into the segment buffers
+      const int set = (int)(c & 1);
+      void* const* seg = A.seg.data() + set * (I - 1);
+      void* const* seg_side = A.seg_side.data() + set * (I - 1);
+      // aux: recompute p_{t0+1} .. p_{t1-1} into this segment's set, once the
+      // reverse steps of segment c+2 (same set) have read it
+      if (c + 2 <= C) LBM_CUDA(cudaStreamWaitEvent(A.aux, evA[set], 0));
       for (int64_t t = t0 + 1; t < t1; ++t) {
-        const void* fin = t == t0 + 1 ? h->state_base(A.ckpt[c]) : h->state_base(A.seg[t - t0 - 2]);
-        const void* sin = t == t0 + 1 ? A.ckpt_side[c] : A.seg_side[t - t0 - 2];
-        int r = h->launch_bufs(t == 1 ? lbm::F_NOPULL : 0, plain, fin, h->state_base(A.seg[t - t0 - 1]), sin,
-                               A.seg_side[t - t0 - 1]);
+        const void* fin = t == t0 + 1 ? h->state_base(A.ckpt[c]) : h->state_base(seg[t - t0 - 2]);
+        const void* sin = t == t0 + 1 ? A.ckpt_side[c] : seg_side[t - t0 - 2];
+        int r = h->launch_bufs(t == 1 ? lbm::F_NOPULL : 0, plain, fin, h->state_base(seg[t - t0 - 1]), sin,
+                               seg_side[t - t0 - 1], A.aux);
         if (r) return r;
       }
-      // reverse steps t1 .. t0+1
+      LBM_CUDA(cudaEventRecord(evR[set], A.aux));
+      // main: reverse steps t1 .. t0+1 (overlap the recompute of segment c-1)
+      LBM_CUDA(cudaStreamWaitEvent(h->stream, evR[set], 0));
       for (int64_t t = t1; t > t0; --t) {
         lbm::AdjArgs a;
         a.g = g;
         a.p = h->p;
-        a.fprev = t - 1 == t0 ? h->state_base(A.ckpt[c]) : h->state_base(A.seg[t - t0 - 2]);
-        a.side_prev = t - 1 == t0 ? A.ckpt_side[c] : A.seg_side[t - t0 - 2];
+        a.fprev = t - 1 == t0 ? h->state_base(A.ckpt[c]) : h->state_base(seg[t - t0 - 2]);
+        a.side_prev = t - 1 == t0 ? A.ckpt_side[c] : seg_side[t - t0 - 2];
         a.a_next = have_next ? A.a[cur_a] : nullptr;
         a.a_cur = A.a[cur_a ^ 1];
         a.grad_u = t == T ? A.grad_u : nullptr;
@@ -902,7 +937,10 @@ int lbm_adjoint_backward(LbmHandle* h, const double* grad_u, double* grad_force,
         cur_a ^= 1;
         have_next = true;
       }
+      LBM_CUDA(cudaEventRecord(evA[set], h->stream));
     }
+    LBM_CUDA(cudaEventRecord(A.ev[1], A.aux));   // join
+    LBM_CUDA(cudaStreamWaitEvent(h->stream, A.ev[1], 0));
     return LBM_OK;
   };
   if (!std::getenv("LBM_NO_GRAPH")) {

@@ -42,6 +42,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the FP64 / FP16 / error side measurements")
+    ap.add_argument("--only", choices=["adjoint", "batch"],
+                    help="run one side measurement alone and print it (profiling runs)")
+    ap.add_argument("--adjoint-steps", type=int, default=2000)
     return ap.parse_args()
 
 
@@ -459,6 +462,10 @@ def batch_measurement(nsteps=5000, n_check=16, seq_steps=50):
 
 def main():
     args = parse()
+    if args.only:
+        out = adjoint_measurement(args.adjoint_steps) if args.only == "adjoint" else batch_measurement()
+        print(json.dumps({"only": args.only, **out}), flush=True)
+        return
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)

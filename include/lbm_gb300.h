@@ -184,6 +184,37 @@ int lbm_adjoint_forward(LbmHandle* h, int64_t nsteps, int interval);
 int lbm_adjoint_backward(LbmHandle* h, const double* grad_u, double* grad_force,
                          double* grad_tau, double* grad_uwall);
 
+/* One momentum-exchange link: node x, the population k_out leaving x towards
+ * a solid node or a wall, and k_in, the population coming back along the
+ * opposite direction.  Its contribution to its group (an obstacle or a wall
+ * boundary element) is
+ *     v = pop[x,k_out] c_{k_out} - pop_new[x,k_in] c_{k_in}
+ *     force += v,  torque += rx v_y - ry v_x
+ * with pop the post-collision populations of the last step and pop_new the
+ * populations after its streaming and boundaries.  (rx, ry) is the lever arm
+ * from the group's reference point (minimum image on periodic axes). */
+typedef struct {
+  int64_t node;            /* inner index x*ny + y; must have a link record */
+  int32_t group;           /* 0 .. ngroups-1                                */
+  int8_t k_out, k_in;      /* D2Q9 directions, k_in = opposite of k_out     */
+  int8_t reserved[2];
+  double rx, ry;           /* lever arm (obstacles); 0 for wall elements    */
+} LbmForceLink;
+
+/* Registers the momentum-exchange links (replaces the argument set-up of
+ * ObstacleOperator / BoundaryOperator force computation,
+ * pylabolt/base/obstacle_operator.py:75-114, boundary_operator.py:362-397).
+ * A later call replaces the previous set. */
+int lbm_set_force_links(LbmHandle* h, const LbmForceLink* links, int64_t nlinks, int ngroups);
+
+/* Force and torque of every group on the current state, FP64:
+ * out[g*3 + {0,1,2}] = {fx, fy, torque}.  Replaces
+ * compute_force_torque_single_phase and compute_boundary_force_single_phase
+ * (pylabolt/parallel/cpu/force_torque_kernels.py:11-141) evaluated after a
+ * time step (fluidLB.py:249-253, :361-366); right after lbm_init_fields it
+ * gives the t = 0 values (pop = pop_new = f_eq, fluidLB.py:323-335). */
+int lbm_forces(LbmHandle* h, double* out);
+
 /* Number of completed steps since the last init. */
 int lbm_time(LbmHandle* h, int64_t* t);
 

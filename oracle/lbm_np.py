@@ -308,3 +308,60 @@ def run(st, nsteps, std_out_interval=None):
         if std_out_interval and t % std_out_interval == 0:
             hist.append((t, *res.compute(st)))
     return hist
+
+
+# ---------------------------------------------------------------------------
+# momentum exchange (evaluated after a time step)
+
+def obstacle_force_torque(pop, pop_new, solid, solid_id, fluid_boundary, nx, ny,
+                          ref_point, obstacle_id, x_periodic, y_periodic):
+    """compute_force_torque_single_phase,
+    pylabolt/parallel/cpu/force_torque_kernels.py:11-90.  Padded AoS inputs
+    ([(nx+2)*(ny+2)] flags, [.., 9] populations); sums in the serial loop
+    order (node, then direction).  Returns [fx, fy, torque]."""
+    nyp = ny + 2
+    idx = np.arange((nx + 2) * nyp)
+    x, y = idx // nyp, idx % nyp
+    ghost = (x == 0) | (x == nx + 1) | (y == 0) | (y == ny + 1)
+    sel = np.nonzero(~ghost & fluid_boundary & (solid_id == obstacle_id))[0]
+    xs, ys = sel // nyp, sel % nyp
+    rx = (xs - 1) - ref_point[0]
+    ry = (ys - 1) - ref_point[1]
+    rxm, rym = rx.astype(np.float64), ry.astype(np.float64)
+    if x_periodic:
+        a = rx + nx
+        rxm = np.where(np.abs(a) < np.abs(rxm), a, rxm)
+        b = rx - nx
+        rxm = np.where(np.abs(b) < np.abs(rxm), b, rxm)
+    if y_periodic:
+        a = ry + ny
+        rym = np.where(np.abs(a) < np.abs(rym), a, rym)
+        b = ry - ny
+        rym = np.where(np.abs(b) < np.abs(rym), b, rym)
+    vx = np.zeros((sel.size, 9))
+    vy = np.zeros((sel.size, 9))
+    tq = np.zeros((sel.size, 9))
+    for k in range(9):
+        nb = (xs + CX[k]) * nyp + ys + CY[k]
+        m = solid[nb]
+        ki = INV[k]
+        px = pop[sel, k] * CX[k] - pop_new[sel, ki] * CX[ki]
+        py = pop[sel, k] * CY[k] - pop_new[sel, ki] * CY[ki]
+        vx[m, k] = px[m]
+        vy[m, k] = py[m]
+        tq[m, k] = rxm[m] * py[m] - rym[m] * px[m]
+    return np.array([_seq_sum(vx.ravel()), _seq_sum(vy.ravel()), _seq_sum(tq.ravel())])
+
+
+def boundary_force(pop, pop_new, solid, boundary_nodes, out_list, inv_list):
+    """compute_boundary_force_single_phase,
+    pylabolt/parallel/cpu/force_torque_kernels.py:96-141 (padded node
+    indices).  Returns [fx, fy]."""
+    nodes = np.asarray(boundary_nodes)
+    nodes = nodes[~solid[nodes]]
+    vx = np.zeros((nodes.size, len(out_list)))
+    vy = np.zeros((nodes.size, len(out_list)))
+    for j, (ko, ki) in enumerate(zip(out_list, inv_list)):
+        vx[:, j] = pop[nodes, ko] * CX[ko] - pop_new[nodes, ki] * CX[ki]
+        vy[:, j] = pop[nodes, ko] * CY[ko] - pop_new[nodes, ki] * CY[ki]
+    return np.array([_seq_sum(vx.ravel()), _seq_sum(vy.ravel())])

@@ -61,6 +61,11 @@ NODE_LINKS_DTYPE = np.dtype([("node", "<i8"), ("src", "<i8", 9), ("aux", "<i8", 
                              ("reserved", "i1", 6)])
 assert NODE_LINKS_DTYPE.itemsize == 8 + 72 + 72 + 72 + 9 + 1 + 6
 
+# numpy mirror of LbmForceLink
+FORCE_LINK_DTYPE = np.dtype([("node", "<i8"), ("group", "<i4"), ("k_out", "i1"), ("k_in", "i1"),
+                             ("reserved", "i1", 2), ("rx", "<f8"), ("ry", "<f8")])
+assert FORCE_LINK_DTYPE.itemsize == 32
+
 _LIB = None
 
 # every symbol include/lbm_gb300.h declares
@@ -69,7 +74,8 @@ EXPORTS = ["lbm_create", "lbm_init_fields", "lbm_set_body_force", "lbm_step",
            "lbm_get_populations", "lbm_set_populations", "lbm_time",
            "lbm_kernel_launches", "lbm_kernel_variant", "lbm_tuning", "lbm_device_bytes", "lbm_time_steps",
            "lbm_synchronize", "lbm_last_error", "lbm_destroy", "lbm_conservation_noalloc",
-           "lbm_adjoint_forward", "lbm_adjoint_backward", "lbm_set_omega_map"]
+           "lbm_adjoint_forward", "lbm_adjoint_backward", "lbm_set_omega_map",
+           "lbm_set_force_links", "lbm_forces"]
 
 
 def lib_path():
@@ -111,6 +117,8 @@ def load(build=True):
         "lbm_adjoint_forward": [P, i64, ctypes.c_int],
         "lbm_set_omega_map": [P, P],
         "lbm_adjoint_backward": [P, P, P, dbl, P],
+        "lbm_set_force_links": [P, P, i64, ctypes.c_int],
+        "lbm_forces": [P, P],
     }
     for name, argtypes in sig.items():
         fn = getattr(lib, name)

@@ -330,6 +330,7 @@ class Case:
     def _obstacles(self, od):
         self.obstacles = []
         self.solid = np.zeros((self.nx, self.ny), dtype=bool)
+        self.solid_id = np.full((self.nx, self.ny), -1, dtype=np.int64)
         if "options" not in od:
             raise ValueError("options missing in obstacle_dict")
         opts = od["options"]
@@ -392,6 +393,7 @@ class Case:
         r = np.float64(obs.radius)
         inside = rxm * rxm + rym * rym <= r * r
         self.solid |= inside
+        self.solid_id[inside] = obs.id
         lin = obs.linear_velocity
         ang = np.float64(obs.angular_velocity)
         self.velocity[inside, 0] = lin[0] - ang * rym[inside]

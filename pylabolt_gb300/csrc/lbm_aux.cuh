@@ -2,6 +2,7 @@
 // and the KernelSet that bundles them with the fused step kernel.
 #pragma once
 #include "lbm_adjoint.cuh"
+#include "lbm_force.cuh"
 
 namespace lbm {
 
@@ -177,6 +178,10 @@ struct Kernels {
       adjoint_kernel<S, 2><<<grid, kStepBlock, 0, s>>>(a);
     return cudaGetLastError();
   }
+  static cudaError_t forces(const ForceArgs& a, int ngroups, cudaStream_t s) {
+    force_kernel<S><<<ngroups, kForceBlock, 0, s>>>(a);
+    return cudaGetLastError();
+  }
   static KernelSet make() {
     KernelSet k;
     k.elem_bytes = sizeof(S);
@@ -202,6 +207,7 @@ struct Kernels {
     k.moments_to_f64 = &moments_to_f64;
     k.body_from_f64 = &body_from_f64;
     k.conservation = &conservation;
+    k.forces = &forces;
     if constexpr (sizeof(S) >= 4)
       k.adjoint = &adjoint<S>;
     else

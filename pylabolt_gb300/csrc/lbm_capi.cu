@@ -7,6 +7,7 @@
 // so the fused kernel never reads outside its arrays.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -108,6 +109,28 @@ struct LbmHandle {
     int64_t graph_T = -1;
     int graph_interval = -1;
   } adj;
+  // momentum-exchange links (lbm_set_force_links)
+  struct Force {
+    long long* node = nullptr;
+    int* rec = nullptr;
+    int8_t* kk = nullptr;
+    double* arm = nullptr;
+    int* gstart = nullptr;
+    double* out = nullptr;
+    int ngroups = 0;
+    int64_t n = 0;
+  } force;
+
+  // frees one allocation of this handle
+  void release(void* q) {
+    if (!q) return;
+    for (auto it = allocs.begin(); it != allocs.end(); ++it)
+      if (*it == q) {
+        cudaFree(q);
+        allocs.erase(it);
+        return;
+      }
+  }
 
   ~LbmHandle() {
     if (gexec) cudaGraphExecDestroy(gexec);
@@ -1051,6 +1074,94 @@ int lbm_set_populations(LbmHandle* h, const double* pop_new) {
   h->initialized = true;
   h->nopull = true;
   return LBM_OK;
+}
+
+int lbm_set_force_links(LbmHandle* h, const LbmForceLink* links, int64_t nlinks, int ngroups) {
+  if (!h || (nlinks > 0 && !links)) return fail(LBM_ERR_ARG, "lbm_set_force_links: null argument");
+  if (nlinks < 0 || ngroups < 0 || (nlinks > 0 && ngroups == 0) || nlinks > (int64_t)INT32_MAX)
+    return fail(LBM_ERR_ARG, "lbm_set_force_links: bad link or group count");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  const lbm::Geom& g = h->g;
+  const int64_t nx = g.nx, ny = g.ny;
+  std::unordered_map<int64_t, int> rec_of;   // inner node -> record
+  for (size_t r = 0; r < h->h_links.size(); ++r) rec_of[h->h_links[r].node] = (int)r;
+  std::vector<int64_t> order(nlinks);
+  for (int64_t i = 0; i < nlinks; ++i) {
+    const LbmForceLink& L = links[i];
+    if (L.group < 0 || L.group >= ngroups)
+      return fail(LBM_ERR_ARG, "lbm_set_force_links: link " + std::to_string(i) + " has group out of range");
+    if (L.k_out < 0 || L.k_out > 8 || L.k_in < 0 || L.k_in > 8)
+      return fail(LBM_ERR_ARG, "lbm_set_force_links: link " + std::to_string(i) + " has a direction out of range");
+    if (L.node < 0 || L.node >= nx * ny || !rec_of.count(L.node))
+      return fail(LBM_ERR_ARG, "lbm_set_force_links: link " + std::to_string(i) +
+                                   " is not on a boundary node of the link table");
+    order[i] = i;
+  }
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int64_t a, int64_t b) { return links[a].group < links[b].group; });
+  std::vector<long long> node(nlinks);
+  std::vector<int> rec(nlinks), gstart(ngroups + 1, 0);
+  std::vector<int8_t> kk(2 * nlinks);
+  std::vector<double> arm(2 * nlinks);
+  for (int64_t j = 0; j < nlinks; ++j) {
+    const LbmForceLink& L = links[order[j]];
+    node[j] = (long long)(L.node % ny + 1) * g.pitch + L.node / ny;
+    rec[j] = rec_of[L.node];
+    kk[2 * j] = L.k_out;
+    kk[2 * j + 1] = L.k_in;
+    arm[2 * j] = L.rx;
+    arm[2 * j + 1] = L.ry;
+    ++gstart[L.group + 1];
+  }
+  for (int q = 0; q < ngroups; ++q) gstart[q + 1] += gstart[q];
+  auto& F = h->force;
+  for (void* q : {(void*)F.node, (void*)F.rec, (void*)F.kk, (void*)F.arm, (void*)F.gstart, (void*)F.out})
+    h->release(q);
+  F = LbmHandle::Force{};
+  if (ngroups == 0) return LBM_OK;
+  const size_t n1 = std::max<int64_t>(nlinks, 1);
+  int rc;
+  if ((rc = h->alloc(reinterpret_cast<void**>(&F.node), n1 * sizeof(long long))) ||
+      (rc = h->alloc(reinterpret_cast<void**>(&F.rec), n1 * sizeof(int))) ||
+      (rc = h->alloc(reinterpret_cast<void**>(&F.kk), 2 * n1)) ||
+      (rc = h->alloc(reinterpret_cast<void**>(&F.arm), 2 * n1 * sizeof(double))) ||
+      (rc = h->alloc(reinterpret_cast<void**>(&F.gstart), (ngroups + 1) * sizeof(int))) ||
+      (rc = h->alloc(reinterpret_cast<void**>(&F.out), 3 * (size_t)ngroups * sizeof(double))))
+    return rc;
+  if (nlinks > 0) {
+    LBM_CUDA(cudaMemcpyAsync(F.node, node.data(), nlinks * sizeof(long long), cudaMemcpyHostToDevice, h->stream));
+    LBM_CUDA(cudaMemcpyAsync(F.rec, rec.data(), nlinks * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    LBM_CUDA(cudaMemcpyAsync(F.kk, kk.data(), 2 * nlinks, cudaMemcpyHostToDevice, h->stream));
+    LBM_CUDA(cudaMemcpyAsync(F.arm, arm.data(), 2 * nlinks * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  }
+  LBM_CUDA(cudaMemcpyAsync(F.gstart, gstart.data(), (ngroups + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                           h->stream));
+  F.ngroups = ngroups;
+  F.n = nlinks;
+  return h->wait();   // the host vectors go out of scope
+}
+
+int lbm_forces(LbmHandle* h, double* out) {
+  if (!h || !out) return fail(LBM_ERR_ARG, "lbm_forces: null argument");
+  if (!h->initialized) return fail(LBM_ERR_STATE, "lbm_forces: not initialised");
+  const auto& F = h->force;
+  if (F.ngroups == 0) return LBM_OK;
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  lbm::ForceArgs a;
+  a.g = h->g;
+  a.p = h->p;
+  a.pop = h->pop[h->cur];
+  a.side = h->side[h->cur];
+  a.node = F.node;
+  a.rec = F.rec;
+  a.kk = F.kk;
+  a.arm = F.arm;
+  a.gstart = F.gstart;
+  a.nopull = h->nopull ? 1 : 0;
+  a.out = F.out;
+  LBM_CUDA(h->ks->forces(a, F.ngroups, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(out, F.out, 3 * (size_t)F.ngroups * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return h->wait();
 }
 
 int lbm_time(LbmHandle* h, int64_t* t) {

@@ -88,6 +88,22 @@ struct AdjArgs {
   int nopull;             // t = 1: f^1 are the stored populations themselves
 };
 
+// Momentum-exchange force sums over link groups (obstacles, wall elements).
+// Links are sorted by group; group i owns [gstart[i], gstart[i+1]).
+struct ForceArgs {
+  Geom g;
+  Params p;
+  const void* pop;        // post-collision populations p_t (storage type)
+  const void* side;       // rho, u of step t at boundary nodes (compute type)
+  const long long* node;  // [n] device node index
+  const int* rec;         // [n] link record of the node
+  const int8_t* kk;       // [2n] k_out, k_in
+  const double* arm;      // [2n] lever arm rx, ry
+  const int* gstart;      // [ngroups+1]
+  int nopull;             // state holds incoming populations (t = 0): f_new = p
+  double* out;            // [ngroups][3] fx, fy, torque
+};
+
 // Launch shape of the fused step.
 //   kind 0: scalar kernel, one node per thread
 //   kind 1: vector kernel, `vec` consecutive nodes per thread
@@ -131,6 +147,8 @@ struct KernelSet {
                               double* partials, cudaStream_t s);
   // one reverse step (null where the storage has no adjoint)
   cudaError_t (*adjoint)(int forcing, const AdjArgs& a, cudaStream_t s);
+  // momentum-exchange sums, one block per group
+  cudaError_t (*forces)(const ForceArgs& a, int ngroups, cudaStream_t s);
 };
 
 const KernelSet& kernels_fp64();

@@ -123,6 +123,35 @@ class FluidLBM:
         check(self.lib.lbm_conservation(self.h, out))
         return np.array(out[:])
 
+    # -- momentum exchange (force_torque_kernels.py:11-141)
+    def forces(self):
+        """Force and torque from the momentum exchange on the current state:
+        {"obstacles": [nobs, 3] (fx, fy, torque), "walls": [nwalls, 2]
+        (fx, fy)}, in obstacle / wall-element order (``force_names``).  After
+        ``initialize`` these are the t = 0 values."""
+        if getattr(self, "_force_names", None) is None:
+            from .obstacles import force_links
+            links, obs, walls = force_links(self.case)
+            ng = len(obs) + len(walls)
+            links = np.ascontiguousarray(links)
+            check(self.lib.lbm_set_force_links(self.h, ptr(links) if len(links) else None,
+                                               len(links), ng))
+            self._force_names = (obs, walls)
+        obs, walls = self._force_names
+        out = np.zeros((len(obs) + len(walls), 3))
+        if len(out):
+            check(self.lib.lbm_forces(self.h, ptr(out)))
+        return {"obstacles": out[:len(obs)], "walls": out[len(obs):, :2]}
+
+    @property
+    def force_names(self):
+        """(obstacle names, wall element names) of ``forces``."""
+        if getattr(self, "_force_names", None) is None:
+            from .obstacles import force_links
+            _, obs, walls = force_links(self.case)
+            return obs, walls
+        return self._force_names
+
     def populations(self):
         """Post-collision populations of the last step, padded AoS FP64."""
         nx, ny = self.case.nx, self.case.ny

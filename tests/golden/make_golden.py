@@ -17,7 +17,17 @@ With it the reference's own modules run as plain FP64 Python:
   density, gravity force, velocity, BGK collision, the GPU periodic wrap
   kernels of pylabolt/parallel/gpu/MPI_kernels.py:51-99 (looped over thread
   indices), ``scalar_based_kernel`` and the boundary kernels in element order;
-* residues come from ``compute_residue_scalar/vector``.
+* residues come from ``compute_residue_scalar/vector``;
+* the obstacle geometry fields (solid_id, solid_boundary, fluid_boundary,
+  surface_normals) come from the reference's own ``ObstacleOperator``
+  (pylabolt/base/obstacle_operator.py:19-45, with its single-rank
+  ``halo_exchange_cpu``), built on a second State so that the stepping above
+  keeps ghost nodes non-solid;
+* momentum-exchange forces at t = 0 and at every checkpoint come from
+  ``compute_force_torque_single_phase`` (every obstacle) and
+  ``compute_boundary_force_single_phase`` (every wall element),
+  pylabolt/parallel/cpu/force_torque_kernels.py:11-141, applied to the
+  checkpointed pop / pop_new.
 
 Deviations, each forced by a defect of the reference snapshot:
 * ``move_obstacles`` is skipped (it calls the undefined
@@ -67,8 +77,21 @@ def install_numba_stub():
     cuda.device_array = np.zeros
     cuda.device_array_like = np.zeros_like
     numba.cuda = cuda
+    # type names imported by the GPU kernel modules (``from numba import int64``)
+    numba.__getattr__ = lambda name: getattr(np, name) if hasattr(np, name) else object()
+    cuda.__getattr__ = lambda name: object()
     sys.modules["numba"] = numba
     sys.modules["numba.cuda"] = cuda
+
+
+def install_mpi4py_stub():
+    """``mpi4py`` is not installed; the reference's MPIOperator imports it."""
+    mpi4py = types.ModuleType("mpi4py")
+    mpi = types.ModuleType("mpi4py.MPI")
+    mpi.SUM = "sum"
+    mpi4py.MPI = mpi
+    sys.modules["mpi4py"] = mpi4py
+    sys.modules["mpi4py.MPI"] = mpi
 
 
 class DummyComm:
@@ -77,6 +100,12 @@ class DummyComm:
 
     def Get_size(self):
         return 1
+
+    def Sendrecv(self, sendbuf, dest, sendtag, recvbuf, source, recvtag):
+        recvbuf[...] = sendbuf          # one rank: it exchanges with itself
+
+    def Allreduce(self, a, b, op=None):
+        b[...] = a
 
     def Barrier(self):
         pass
@@ -275,6 +304,8 @@ def run_case(name, case, nsteps, ref):
         size, lat.cx, lat.cy, lat.weights, lat.no_of_directions, lat.inv_cs_2,
         lat.inv_cs_4, fld.solid, fld.ghost_node, fld.density, fld.velocity,
         fld.pop_fluid, fld.pop_fluid_new)
+    pop_init = fld.pop_fluid.copy()
+    pop_new_init = fld.pop_fluid_new.copy()
 
     dens_old = np.zeros_like(fld.density)
     vel_old = np.zeros_like(fld.velocity)
@@ -338,6 +369,9 @@ def run_case(name, case, nsteps, ref):
             out[f"pop_t{t}"] = fld.pop_fluid.copy()
             out[f"pop_new_t{t}"] = fld.pop_fluid_new.copy()
 
+    geo = geometry_and_forces(case, {0: (pop_init, pop_new_init),
+                                     **{t: (out[f"pop_t{t}"], out[f"pop_new_t{t}"])
+                                        for t in checkpoints}})
     arrays = {}
     for region, rd in case["initial_fields_dict"].items():
         for fname, spec in rd["fluid"].items():
@@ -348,8 +382,41 @@ def run_case(name, case, nsteps, ref):
         case_json=np.array(jsonable(case)), nsteps=np.array(nsteps),
         checkpoints=np.array(checkpoints), rho0=rho0, u0=u0, solid=solid0,
         residuals=np.array(resid), inv_cs_2=np.array(lat.inv_cs_2),
-        inv_cs_4=np.array(lat.inv_cs_4), omega=np.array(omega), **arrays, **out)
+        inv_cs_4=np.array(lat.inv_cs_4), omega=np.array(omega), **arrays, **out, **geo)
     return len(resid)
+
+
+def geometry_and_forces(case, states):
+    """Obstacle geometry fields from the reference's ObstacleOperator and
+    momentum-exchange forces of `states` {t: (pop, pop_new)}."""
+    from pylabolt.base.state import State
+    from pylabolt.parallel.MPI_operator import MPIOperator
+    from pylabolt.base.obstacle_operator import ObstacleOperator
+    import pylabolt.parallel.cpu.force_torque_kernels as ftk
+
+    with contextlib.redirect_stdout(io.StringIO()):
+        st = State(to_module(case), DummyComm(), 0, fluid=True)
+        ObstacleOperator(None, st, None, MPIOperator(DummyComm(), st), None)
+    lat, fld, dom = st.lattice, st.fields, st.domain
+    out = {"geo_solid": fld.solid.copy(), "geo_solid_id": fld.solid_id.copy(),
+           "geo_solid_boundary": fld.solid_boundary.copy(),
+           "geo_fluid_boundary": fld.fluid_boundary.copy(),
+           "geo_surface_normals": fld.surface_normals.copy()}
+    walls = [el for el in st.boundary.boundary_elements if el.wall]
+    out["wall_names"] = np.array([el.name for el in walls])
+    out["obstacle_names"] = np.array([o.name for o in st.obstacle.obstacles])
+    for t, (pop, pop_new) in states.items():
+        obs = [ftk.compute_force_torque_single_phase(
+            dom.size, dom.shape, dom.offset, st.mesh.grid_global_shape, lat.cx, lat.cy,
+            lat.inv_list, lat.no_of_directions, st.boundary.x_periodic, st.boundary.y_periodic,
+            fld.solid, fld.solid_id, fld.fluid_boundary, fld.ghost_node, pop, pop_new,
+            o.ref_point, o.id) for o in st.obstacle.obstacles]
+        wall = [ftk.compute_boundary_force_single_phase(
+            lat.cx, lat.cy, fld.solid, pop, pop_new, el.boundary_nodes, el.out_list,
+            el.inv_list) for el in walls]
+        out[f"force_obstacles_t{t}"] = np.array(obs).reshape(-1, 3)
+        out[f"force_walls_t{t}"] = np.array(wall).reshape(-1, 2)
+    return out
 
 
 def main():
@@ -358,6 +425,7 @@ def main():
     ap.add_argument("--only", default=None)
     args = ap.parse_args()
     install_numba_stub()
+    install_mpi4py_stub()
     sys.path.insert(0, args.ref)
     for name, (case, nsteps, _) in make_cases().items():
         if args.only and name != args.only:

@@ -7,4 +7,6 @@ include/lbm_gb300.h); :class:`FluidLBM` is the Python host object over it and
 from .config import Case
 from .lbm import FluidLBM
 
+__version__ = "0.1.0+gb300"
+
 __all__ = ["Case", "FluidLBM"]

@@ -45,6 +45,23 @@ def _has(sim, name):
     return name in sim if isinstance(sim, dict) else hasattr(sim, name)
 
 
+def _write_interval(opts, where):
+    """``write_*_data: {"interval": int | None}`` (boundary.py:254-272,
+    obstacle.py:169-184); 1 when the option is absent."""
+    key = "write_boundary_data" if where == "boundary_dict" else "write_obstacle_data"
+    if key not in opts:
+        return 1
+    d = opts[key]
+    if "interval" not in d:
+        raise ValueError(f"interval missing {where} options!")
+    iv = d["interval"]
+    if not isinstance(iv, (int, type(None))):
+        raise ValueError(f"interval must be int or None in {where} options")
+    if isinstance(iv, int) and iv <= 0:
+        raise ValueError(f"if interval is int then it must be > 0 in {where} options")
+    return iv
+
+
 class BoundaryElement:
     """One segment of one ``boundary_dict`` entry (boundary.py:7-127)."""
 
@@ -228,6 +245,7 @@ class Case:
         if not isinstance(self.compute_boundary_force, (bool, np.bool_)):
             raise ValueError("compute_force must be a bool: True/False (default: False)")
         self.write_boundary_data = "write_boundary_data" in opts
+        self.boundary_write_interval = _write_interval(opts, "boundary_dict")
         for name, ud in bd.items():
             if name == "options":
                 continue
@@ -337,6 +355,13 @@ class Case:
         self.compute_force_torque = opts.get("compute_force_torque", False)
         if not isinstance(self.compute_force_torque, (bool, np.bool_)):
             raise ValueError("compute_force_torque must be bool: True/False (default: False)")
+        if "ref_point_torque" in opts and self.compute_force_torque:
+            # parsed and validated as obstacle.py:147-163 does; like the
+            # reference, the torque is taken about each obstacle's centre
+            if not isinstance(opts["ref_point_torque"], list):
+                raise ValueError("ref_point_torque must be list: (x, y)")
+        self.write_obstacle_data = "write_obstacle_data" in opts
+        self.obstacle_write_interval = _write_interval(opts, "obstacle_dict")
         names = [k for k in od if k != "options"]
         for oid, name in enumerate(names):
             d = od[name]

@@ -1,0 +1,157 @@
+"""Drop-in fluidLB solver for ``pylabolt --solver fluidLB -b gpu``.
+
+``Solver.run`` follows the reference's run loop (pylabolt/solvers/fluidLB.py:
+306-384): initial populations, t = 0 forces and output, then per time step
+the step itself, boundary forces, residues and the status line, field output
+and histories, and the final run-time line.  The GPU library advances the
+steps between two output events in one call (replayed CUDA graphs); steps
+with an event record what the event reads (moments for field output, the
+residual pass for the status line).  Outputs are the reference's files
+(pylabolt_gb300.output).
+"""
+import os
+import sys
+import time
+
+import numpy as np
+
+from .config import Case
+from .lbm import FluidLBM
+from .obstacles import Geometry
+from .output import Output, log_line
+
+
+def load_simulation(path=None):
+    """``import simulation`` from the working directory (helpers.py:10-24)."""
+    d = path or os.getcwd()
+    if d not in sys.path:
+        sys.path.append(d)
+    try:
+        import simulation
+    except ImportError:
+        raise ImportError("Missing simulation.py file in current working directory")
+    return simulation
+
+
+def _next_multiple(t, interval):
+    return (t // interval + 1) * interval
+
+
+class Solver:
+    """One fluidLB run on one GPU.  `simulation`: the ``simulation`` module
+    (or a dict with its dictionaries); `root`: directory that receives
+    ``metadata.json`` and ``output/``."""
+
+    def __init__(self, simulation, root=".", storage=None, device=0, verbose=True):
+        self.verbose = verbose
+        self.case = Case(simulation)
+        self.geometry = Geometry(self.case)
+        self.out = Output(self.case, self.geometry, root)
+        self.lbm = FluidLBM(self.case, storage=storage, device=device)
+        nobs = len(self.case.obstacles)
+        self.nobs = nobs
+        self.residues = None
+
+    def log(self, msg):
+        if self.verbose:
+            print(msg, flush=True)
+
+    # -- events of step t
+    def _events(self, t):
+        c = self.case
+        std = c.std_out_interval is not None and t % c.std_out_interval == 0
+        return std, self.out.save_due(t), self.out.boundary_due(t), self.out.obstacle_due(t)
+
+    def _next_event(self, t):
+        c = self.case
+        cands = [c.end_time]
+        for iv in (c.std_out_interval, c.save_interval):
+            if iv is not None:
+                cands.append(_next_multiple(t, iv))
+        if c.write_boundary_data and c.boundary_write_interval is not None:
+            cands.append(_next_multiple(t, c.boundary_write_interval))
+        if c.write_obstacle_data and c.obstacle_write_interval is not None:
+            cands.append(_next_multiple(t, c.obstacle_write_interval))
+        return min(cands)
+
+    def _update_forces(self, obstacles, walls):
+        """The reference computes obstacle forces every step when
+        compute_force_torque is set (fluidLB.py:249-253) and wall forces on
+        write steps when compute_force is set; here both are evaluated on the
+        steps whose histories read them."""
+        c = self.case
+        want_obs = obstacles and c.compute_force_torque
+        want_walls = walls and c.compute_boundary_force
+        if not (want_obs or want_walls):
+            return
+        f = self.lbm.forces()
+        if want_obs:
+            self.obstacle_forces = f["obstacles"]
+        if want_walls:
+            self.wall_forces = f["walls"]
+
+    def run(self):
+        c = self.case
+        self.log("\n" + "-" * 80)
+        self.log("Running simulation...\n")
+        self.out.write_metadata()
+        self.out.setup_histories()
+        self.obstacle_forces = np.zeros((self.nobs, 3))
+        self.wall_forces = np.zeros((len(self.out.walls), 2))
+        self.lbm.initialize()
+        # t = 0 forces and initial output (fluidLB.py:323-344)
+        self._update_forces(self.out.obstacle_due(0), self.out.boundary_due(0))
+        if self.out.save_due(c.start_time):
+            rho, u = self.lbm.moments()
+            self.out.write_fields(c.start_time, rho, u)
+        if self.out.obstacle_due(0):
+            self.out.write_obstacles(0, self.obstacle_forces)
+        if self.out.boundary_due(0):
+            self.out.write_walls(0, self.wall_forces)
+        t0 = time.perf_counter()
+        t = c.start_time
+        while t < c.end_time:
+            te = self._next_event(t)
+            std, save, bnd, obs = self._events(te)
+            self.lbm.step(te - t, moments=save, residual=std)
+            t = te
+            self._update_forces(obs, bnd)
+            if std:
+                r = self.lbm.residual().astype(self.out.dtype)
+                self.residues = r
+                self.log(log_line(t, res_density=r[:1], res_velocity=r[1:]))
+            if save:
+                rho, u = self.lbm.moments()
+                self.out.write_fields(t, rho, u)
+            if obs:
+                self.out.write_obstacles(t, self.obstacle_forces)
+            if bnd:
+                self.out.write_walls(t, self.wall_forces)
+        self.lbm.synchronize()
+        run_time = time.perf_counter() - t0
+        self.log("\n" + "-" * 80)
+        self.log(f"{'Simulation complete, run time':<30}: {str(run_time) + ' s':<30}")
+        self.log("-" * 80)
+        return run_time
+
+    def close(self):
+        self.lbm.close()
+
+
+def main(backend="gpu", n_threads=1, debug_mode=False, root=None):
+    """Entry point of ``pylabolt --solver fluidLB -b gpu`` (fluidLB.py:387-395)."""
+    if backend != "gpu":
+        raise SystemExit("pylabolt_gb300 provides the gpu backend only; "
+                         "run the reference package for -b cpu")
+    try:
+        sim = load_simulation(root)
+        solver = Solver(sim, root=root or ".")
+    except (ValueError, ImportError) as e:
+        print("-" * 80, flush=True)
+        print("FATAL ERROR!", flush=True)
+        print(str(e), flush=True)
+        raise SystemExit(1)
+    try:
+        solver.run()
+    finally:
+        solver.close()

@@ -87,4 +87,3 @@ def test_cylinder_channel_forces_against_oracle():
         got = sim.forces()
     np.testing.assert_allclose(got["obstacles"][0], ref_cyl, rtol=FORCE_RTOL, atol=1e-14)
     np.testing.assert_allclose(got["walls"], np.array(ref_w), rtol=FORCE_RTOL, atol=1e-14)
-    assert ref_cyl[0] > 0          # drag along the flow

@@ -1,0 +1,93 @@
+"""The drop-in Solver and command line on the GPU.
+
+The full run (FP64 storage) of the output-enabled channel_cylinder_abb case
+against what the reference's own writers produced for the reference's fields:
+field files bit-exact, metadata identical, history files and status lines
+with the same layout and values within the reduction tolerance (forces and
+residues are sums whose order differs, 1e-12 relative)."""
+import json
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from _golden import GOLDEN_DIR
+from pylabolt_gb300 import output, solver
+
+pytestmark = pytest.mark.gpu
+
+SUM_RTOL = 1e-12
+SUM_ATOL = 1e-13   # forces are sums of O(0.1-1) link terms: small results (lift) carry
+                   # an absolute, not relative, reduction-order error
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _io_case():
+    import test_output_cpu
+    return test_output_cpu._io()
+
+
+def _numbers(text):
+    return np.array([float(v) for v in re.findall(r"-?\d\.\d+e[+-]\d+", text)])
+
+
+def test_solver_run_matches_reference_output(tmp_path, monkeypatch, capsys):
+    case, d, _ = _io_case()
+    monkeypatch.setattr(output, "package_version", lambda: str(d["version"]))
+    s = solver.Solver(case, root=str(tmp_path), storage="fp64")
+    try:
+        s.run()
+    finally:
+        s.close()
+    out = capsys.readouterr().out
+    with open(tmp_path / "metadata.json") as f:
+        assert f.read() == str(d["metadata_json"])
+    for t in (0, 30, 60):
+        z = np.load(tmp_path / "output" / "fields" / f"t_{t}.npz")
+        assert list(z.files) == d[f"fields_t{t}_keys"].tolist()
+        for k in z.files:
+            ref = d[f"fields_t{t}:{k}"]
+            assert z[k].dtype == ref.dtype and np.array_equal(z[k], ref), (t, k)
+    for h in d["history_names"].tolist():
+        with open(tmp_path / "output" / "histories" / h) as f:
+            mine = f.read()
+        ref = str(d[f"history:{h}"])
+        assert re.sub(r"-?\d\.\d+e[+-]\d+", "X", mine) == re.sub(r"-?\d\.\d+e[+-]\d+", "X", ref)
+        np.testing.assert_allclose(_numbers(mine), _numbers(ref), rtol=SUM_RTOL, atol=SUM_ATOL)
+    lines = [l for l in out.splitlines() if l.startswith("time:")]
+    ref_lines = d["status_lines"].tolist()
+    assert len(lines) == len(ref_lines)
+    for a, b in zip(lines, ref_lines):
+        assert re.sub(r"-?\d\.\d+e[+-]\d+", "X", a) == re.sub(r"-?\d\.\d+e[+-]\d+", "X", b)
+        np.testing.assert_allclose(_numbers(a), _numbers(b), rtol=1e-4)
+
+
+def test_command_line_cavity(tmp_path):
+    """``python -m pylabolt_gb300 -s fluidLB -b gpu`` in a directory holding a
+    simulation.py, as the reference's ``pylabolt`` is run."""
+    from pylabolt_gb300 import workloads
+    from pylabolt_gb300.config import Case
+    from pylabolt_gb300.lbm import FluidLBM
+    c = workloads.cavity(64, re=100.0)
+    c["control_dict"].update({"end_time": 200, "std_out_interval": 100, "save_interval": 100})
+    with open(tmp_path / "simulation.py", "w") as f:
+        for k, v in c.items():
+            f.write(f"{k} = {json.dumps(v)}\n".replace("null", "None").replace("true", "True")
+                    .replace("false", "False"))
+    env = dict(os.environ, PYTHONPATH=ROOT + os.pathsep + os.environ.get("PYTHONPATH", ""))
+    r = subprocess.run([sys.executable, "-m", "pylabolt_gb300", "-s", "fluidLB", "-b", "gpu"],
+                       cwd=tmp_path, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = [l for l in r.stdout.splitlines() if l.startswith("time:")]
+    assert [l.split()[1] for l in lines] == ["100", "200"]
+    assert sorted(os.listdir(tmp_path / "output" / "fields")) == ["t_0.npz", "t_100.npz", "t_200.npz"]
+    z = np.load(tmp_path / "output" / "fields" / "t_200.npz")
+    with FluidLBM(Case(c), storage="fp64") as sim:
+        sim.initialize()
+        sim.step(200, moments=True)
+        rho, u = sim.moments()
+    assert np.array_equal(z["density"], rho.reshape(-1))
+    assert np.array_equal(z["velocity"], u.reshape(-1, 2))

@@ -49,7 +49,7 @@ struct Params {
 enum StepFlags {
   F_NOPULL = 1,      // populations in `fin` already are the incoming ones
   F_MOMENTS = 2,     // write rho/ux/uy
-  F_RESIDUAL = 4,    // residual sums against *_old, then *_old <- new
+  F_RESIDUAL = 4,    // residual sums against *_old, then *_new <- this step's fields
 };
 
 // Arguments of one fused step launch.  `void*` arrays are typed by the
@@ -62,7 +62,12 @@ struct StepArgs {
   const void* side_in;   // [nrec*3] rho, ux, uy of the previous step
   void* side_out;
   void* rho; void* ux; void* uy;            // [plane] moments
-  void* rho_old; void* ux_old; void* uy_old;
+  // residual: fields of the previous residual step are read from *_old and
+  // this step's written to *_new (two array sets swapped per residual step: a
+  // load and a store of one address in the same pass stall on the in-flight
+  // miss in L2)
+  const void* rho_old; const void* ux_old; const void* uy_old;
+  void* rho_new; void* ux_new; void* uy_new;
   double* partials;      // [nblocks*8] residual partial sums
   const void* body;      // [2*plane] body force or null
   int* err;              // device-visible error word (bounded waits)

@@ -465,9 +465,9 @@ __device__ __forceinline__ void node_outputs(const StepArgs& a, long long n, int
   }
   if (a.flags & F_RESIDUAL) {
     // compute_residues_kernels.py:6-73: sums over fluid nodes
-    T* ro = static_cast<T*>(a.rho_old);
-    T* xo = static_cast<T*>(a.ux_old);
-    T* yo = static_cast<T*>(a.uy_old);
+    const T* ro = static_cast<const T*>(a.rho_old);
+    const T* xo = static_cast<const T*>(a.ux_old);
+    const T* yo = static_cast<const T*>(a.uy_old);
     const T v[3] = {rho, ux, uy};
     const T o[3] = {ro[n], xo[n], yo[n]};
 #pragma unroll
@@ -477,9 +477,9 @@ __device__ __forceinline__ void node_outputs(const StepArgs& a, long long n, int
       red[2 * c + 1] += o[c] * o[c];
     }
     red[6] += (isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2])) ? T(0) : T(1);
-    ro[n] = rho;
-    xo[n] = ux;
-    yo[n] = uy;
+    static_cast<T*>(a.rho_new)[n] = rho;
+    static_cast<T*>(a.ux_new)[n] = ux;
+    static_cast<T*>(a.uy_new)[n] = uy;
   }
 }
 

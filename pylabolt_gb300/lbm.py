@@ -100,14 +100,22 @@ class FluidLBM:
         check(self.lib.lbm_synchronize(self.h, float(timeout_s)))
 
     # -- results
-    def moments(self, layout=capi.LAYOUT_INNER):
+    def moments(self, layout=capi.LAYOUT_INNER, out=None):
         """(rho, u) recorded at the last moments step: inner layout gives
         ``[Nx, Ny]`` / ``[Nx, Ny, 2]``; padded gives the reference's
-        ``[(Nx+2)*(Ny+2)]`` / ``[..., 2]`` arrays (ghosts 0)."""
+        ``[(Nx+2)*(Ny+2)]`` / ``[..., 2]`` arrays (ghosts 0).  `out` = (rho,
+        u): C-contiguous FP64 arrays of that size to fill instead (e.g. pinned
+        host memory for a faster copy)."""
         nx, ny = self.case.nx, self.case.ny
         n = nx * ny if layout == capi.LAYOUT_INNER else (nx + 2) * (ny + 2)
-        rho = np.empty(n)
-        u = np.empty((n, 2))
+        if out is None:
+            rho = np.empty(n)
+            u = np.empty((n, 2))
+        else:
+            rho, u = out
+            if (rho.dtype != np.float64 or u.dtype != np.float64 or rho.size != n
+                    or u.size != 2 * n or not rho.flags.c_contiguous or not u.flags.c_contiguous):
+                raise ValueError("moments(out=...): C-contiguous float64 arrays of the grid size")
         check(self.lib.lbm_get_moments(self.h, ptr(rho), ptr(u), layout))
         if layout == capi.LAYOUT_INNER:
             return rho.reshape(nx, ny), u.reshape(nx, ny, 2)

@@ -10,8 +10,11 @@ compute_force and compute_force_torque), runs the reference's
 ObstacleOperator set-up and InputOutputOperator (pylabolt/utils/io_operator.py)
 in a scratch directory, and feeds it the golden density / velocity and the
 reference-kernel forces of t = 0, 30 and 60 from ``channel_cylinder_abb.npz``.
-It also formats the golden residues of t = 30 and 60 with the reference's
-SimulationStatusLogger (pylabolt/utils/helpers.py:37-56).
+The residues of t = 30 and 60 are what the reference's ResidueOperator
+computes with a std_out interval of 30 (compute_residue_scalar/vector against
+the fields of the previous residue step, zeros at first;
+pylabolt/utils/residues.py:171-222), formatted by SimulationStatusLogger
+(pylabolt/utils/helpers.py:37-56).
 
 The stand-ins of make_golden.py are used (numba, mpi4py); the package
 version that ``dump_metadata`` reads with importlib.metadata is fixed to
@@ -67,6 +70,7 @@ def main():
     from pylabolt.utils.helpers import SimulationStatusLogger
     from pylabolt.solvers.fluidLB import FluidLB
     import pylabolt.parallel.cpu.io_operator_kernels as iok
+    import pylabolt.parallel.cpu.compute_residues_kernels as crk
 
     gold = np.load(os.path.join(HERE, "channel_cylinder_abb.npz"))
     case = io_case()
@@ -84,7 +88,11 @@ def main():
             iop.copy_inner_data_kernel_vector = iok.copy_inner_data_vector
             walls = [el for el in st.boundary.boundary_elements if el.wall]
             lines = []
+            residues = []
             logger = SimulationStatusLogger(0)
+            dens_old = np.zeros_like(st.fields.density)
+            vel_old = np.zeros_like(st.fields.velocity)
+            eps = st.control.float_min
             for t in TIMES:
                 if t == 0:
                     st.fields.density[:] = gold["rho0"]
@@ -100,13 +108,21 @@ def main():
                 iop.write_fields_cpu(st, None, t)
                 iop.write_histories_cpu(st, t)
                 if t > 0:
-                    r = gold["residuals"][t - 1]
+                    fl = st.fields
+                    a = crk.compute_residue_scalar(st.domain.size, fl.solid, fl.ghost_node,
+                                                   fl.density, dens_old)
+                    b = crk.compute_residue_vector(st.domain.size, fl.solid, fl.ghost_node,
+                                                   fl.velocity, vel_old)
+                    r = [np.sqrt(a[0] / (a[1] + eps)), np.sqrt(b[0] / (b[1] + eps)),
+                         np.sqrt(b[2] / (b[3] + eps))]
+                    residues.append([t] + r)
                     buf = io.StringIO()
                     with contextlib.redirect_stdout(buf):
-                        logger.log_data(st, t, res_density=np.array([r[1]]),
-                                        res_velocity=np.array([r[2], r[3]]))
+                        logger.log_data(st, t, res_density=np.array(r[:1]),
+                                        res_velocity=np.array(r[1:]))
                     lines.append(buf.getvalue().rstrip("\n"))
             out["status_lines"] = np.array(lines)
+            out["residues"] = np.array(residues)
             with open("metadata.json") as f:
                 out["metadata_json"] = np.array(f.read())
             hist = sorted(os.listdir("output/histories"))

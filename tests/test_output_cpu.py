@@ -32,7 +32,7 @@ class GoldenLBM:
 
     def __init__(self, case, storage=None, device=0):
         self.case = case
-        _, _, self.g = _io()
+        _, self.d, self.g = _io()
         self.t = 0
         self.calls = []
 
@@ -57,7 +57,8 @@ class GoldenLBM:
                 "walls": self.g[f"force_walls_t{self.t}"]}
 
     def residual(self):
-        return np.array(self.g["residuals"][self.t - 1][1:])
+        res = {int(r[0]): r[1:] for r in self.d["residues"]}
+        return np.array(res[self.t])
 
     def synchronize(self):
         pass

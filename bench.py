@@ -42,7 +42,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the FP64 / FP16 / error side measurements")
-    ap.add_argument("--only", choices=["adjoint", "batch"],
+    ap.add_argument("--only", choices=["adjoint", "batch", "error-study"],
                     help="run one side measurement alone and print it (profiling runs)")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
     return ap.parse_args()
@@ -333,6 +333,18 @@ def side_measurements(args, case_d, sim32, nodes, peak):
             mlups = nodes * steps / (ms / 1e3) / 1e6
             res[storage] = {"mlups": mlups,
                             "roofline_frac": B_LU[storage] * nodes / (ms / steps / 1e3) / 1e9 / peak}
+    # MRT (rates 1.4, 1.4, 1.2) on the same grid, FP32 shifted
+    mrt_args = argparse.Namespace(**{**vars(args), "collision": "MRT"})
+    with FluidLBM(Case(workload_case(mrt_args, "fp32_shifted")), storage="fp32_shifted") as s:
+        s.initialize()
+        s.step(3)
+        s.synchronize()
+        ms = s.time_steps(args.steps)
+        res["mrt_fp32_shifted"] = {
+            "mlups": nodes * args.steps / (ms / 1e3) / 1e6,
+            "roofline_frac": B_LU["fp32_shifted"] * nodes / (ms / args.steps / 1e3) / 1e9 / peak,
+            "kernel": list(s.kernel_variant)}
+    out["mrt_fp32_shifted"] = res["mrt_fp32_shifted"]
     out["adjoint"] = adjoint_measurement()
     out["batch"] = batch_measurement()
     out["fp64"] = res["fp64"]
@@ -352,6 +364,39 @@ def side_measurements(args, case_d, sim32, nodes, peak):
             "steps": err_steps,
             "u_rel_l2": float(np.linalg.norm(d) / np.linalg.norm(ref[fluid])),
             "u_max_abs_over_max": float(np.abs(d).max() / np.abs(ref[fluid]).max())}
+    return out
+
+
+def error_study(args, nsteps=10000):
+    """The cylinder case, BGK and MRT, 10,000 steps from the same seeded
+    start in FP64, FP32-shifted and FP16-shifted storage: throughput of each
+    and the velocity error of the reduced storages against FP64 (relative L2
+    and max |du| / max |u| over fluid nodes)."""
+    from pylabolt_gb300.config import Case
+    from pylabolt_gb300.lbm import FluidLBM
+    out = {"workload": workload_name(args), "steps": nsteps}
+    for coll in ("BGK", "MRT"):
+        cargs = argparse.Namespace(**{**vars(args), "collision": coll})
+        case = Case(workload_case(cargs, "fp64"))
+        fluid = ~case.solid
+        nodes = case.nx * case.ny
+        us, rates = {}, {}
+        for storage in ("fp64", "fp32_shifted", "fp16_shifted"):
+            with FluidLBM(case, storage=storage) as s:
+                s.initialize()
+                s.step(1)
+                s.synchronize()
+                ms = s.time_steps(nsteps - 2)
+                s.step(1, moments=True)
+                us[storage] = s.moments()[1]
+                rates[storage] = nodes * (nsteps - 2) / (ms / 1e3) / 1e6
+        ref = us["fp64"][fluid]
+        res = {"mlups": rates}
+        for storage in ("fp32_shifted", "fp16_shifted"):
+            d = us[storage][fluid] - ref
+            res[storage] = {"u_rel_l2": float(np.linalg.norm(d) / np.linalg.norm(ref)),
+                            "u_max_abs_over_max": float(np.abs(d).max() / np.abs(ref).max())}
+        out[coll.lower()] = res
     return out
 
 
@@ -465,7 +510,12 @@ def batch_measurement(nsteps=5000, n_check=16, seq_steps=50):
 def main():
     args = parse()
     if args.only:
-        out = adjoint_measurement(args.adjoint_steps) if args.only == "adjoint" else batch_measurement()
+        if args.only == "adjoint":
+            out = adjoint_measurement(args.adjoint_steps)
+        elif args.only == "batch":
+            out = batch_measurement()
+        else:
+            out = error_study(args)
         print(json.dumps({"only": args.only, **out}), flush=True)
         return
     world, rank, local = dist_setup()

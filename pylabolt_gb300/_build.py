@@ -1,6 +1,7 @@
 """Build recipe for liblbm_gb300.so (in-tree, sm_103a only).
 
-Each translation unit is compiled by nvcc in parallel; the FP64 unit gets
+Each translation unit is compiled by nvcc in parallel (one per storage type,
+the shared helpers, the C-ABI and the allocation-free entry); the FP64 unit gets
 ``--fmad=false`` so that it keeps the reference's rounding.  The result is
 ``pylabolt_gb300/_build/liblbm_gb300.so`` (git-ignored).
 """
@@ -21,6 +22,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
           "-I", INCLUDE, "-I", CSRC]
 UNITS = {
     "lbm_fp64.cu": ["--fmad=false"],
+    "lbm_fp32.cu": [],
+    "lbm_fp16.cu": [],
     "lbm_lowp.cu": [],
     "lbm_capi.cu": [],
     "lbm_noalloc.cu": [],

@@ -116,9 +116,12 @@ struct Kernels {
       }
     }
     if (v.kind != 0) return cudaErrorInvalidValue;
-    if (v.stages == 1) {
+    if (v.stages == 1 || v.stages == 2) {
       if (v.block > 256) return cudaErrorInvalidValue;
-      step_kernel<S, COLL, FORC, 1><<<grid, v.block, 0, s>>>(a);
+      if (v.stages == 1)
+        step_kernel<S, COLL, FORC, 1><<<grid, v.block, 0, s>>>(a);
+      else
+        step_kernel<S, COLL, FORC, 2><<<grid, v.block, 0, s>>>(a);
     } else {
       step_kernel<S, COLL, FORC, 0><<<grid, v.block, 0, s>>>(a);
     }
@@ -191,10 +194,10 @@ struct Kernels {
       constexpr int V1 = sizeof(S) == 4 ? 4 : 8;
       constexpr int V2 = sizeof(S) == 4 ? 2 : 4;
       // kind 2: {threads, stages}; kind 1: {nodes per thread, threads};
-      // kind 0: {threads, register cap}
-      const Variant vs[] = {{2, 0, 256, 4}, {2, 0, 512, 3}, {2, 0, 512, 2}, {2, 0, 1024, 2},
-                            {2, 0, 256, 2}, {1, V1, 256, 0}, {1, V2, 256, 0}, {0, 1, 128, 0},
-                            {0, 1, 256, 0}, {0, 1, 128, 1}, {0, 1, 256, 1}};
+      // kind 0: {threads, register cap: 0 none, 1 32, 2 40}
+      const Variant vs[] = {{2, 0, 256, 4}, {2, 0, 512, 3}, {2, 0, 256, 2}, {1, V1, 256, 0},
+                            {1, V2, 256, 0}, {0, 1, 128, 0}, {0, 1, 256, 0}, {0, 1, 128, 1},
+                            {0, 1, 256, 1}, {0, 1, 128, 2}, {0, 1, 256, 2}};
       k.nvariants = 11;
       for (int i = 0; i < 11; ++i) k.variants[i] = vs[i];
     } else {

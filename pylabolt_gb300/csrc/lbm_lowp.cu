@@ -1,19 +1,8 @@
-// FP32 / FP16 shifted-storage instantiations of the fused step, plus the
-// precision-independent helpers (deterministic final reduction, host-order
+// Precision-independent helpers (deterministic final reduction, host-order
 // <-> device-order node copies).
 #include "lbm_aux.cuh"
 
 namespace lbm {
-
-const KernelSet& kernels_fp32() {
-  static const KernelSet k = Kernels<float>::make();
-  return k;
-}
-
-const KernelSet& kernels_fp16() {
-  static const KernelSet k = Kernels<__half>::make();
-  return k;
-}
 
 // Sums rows of 8 doubles in two fixed-shape stages (same result every run):
 // kFinishBlocks blocks each sum a contiguous range of rows (thread t takes

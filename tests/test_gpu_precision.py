@@ -181,3 +181,48 @@ def test_poiseuille_mrt_guo_full_size_vs_analytic():
     err = np.abs(ux64[0] - prof).max() / prof.max()
     assert err < 5e-3, err
     assert _rel(u32, u64, np.ones(u64.shape, bool)) <= FP32_STARTUP_TOL
+
+
+# FP32 conserves what its populations hold: long runs stay at the 1e-7 level
+FP32_LONG_TOL = 1e-6
+FP32_MASS_DRIFT = 1e-10
+
+
+def test_fp32_closed_cavity_conserves_mass():
+    """Closed 256^2 cavity, 10,000 steps: relative change of the total mass
+    (the lid moves tangentially, so the exact mass is constant)."""
+    from pylabolt_gb300 import workloads
+    case = Case(workloads.cavity(256, re=100.0, lid=0.01))
+    with FluidLBM(case, storage="fp32_shifted") as s:
+        s.initialize()
+        s.step(1)
+        m0 = s.conservation()[0]
+        s.step(9999)
+        m1 = s.conservation()[0]
+    assert abs(m1 - m0) / m0 <= FP32_MASS_DRIFT
+
+
+@pytest.mark.parametrize("coll", ["BGK", "MRT"])
+def test_fp32_long_run_against_fp64(coll):
+    """1024x256 channel with a cylinder, pressure inlet / outlet, 5000 steps:
+    FP32-shifted velocity against FP64 (relative L2 over fluid nodes).  A
+    collision whose FP32 rounding does not conserve mass and momentum drifts
+    linearly in time and fails this (it measured 1e-5-scale errors)."""
+    from pylabolt_gb300 import workloads
+    case = Case(workloads.cylinder(nx=1024, ny=256, radius=16.0, center=(256, 131), model=coll,
+                                   seed=5))
+    fluid = ~case.solid
+    _, u64, _, _ = _run(case, "fp64", 5000)
+    _, u32, _, _ = _run(case, "fp32_shifted", 5000)
+    assert np.linalg.norm(u32[fluid] - u64[fluid]) / np.linalg.norm(u64[fluid]) <= FP32_LONG_TOL
+
+
+def test_fp32_mrt_poiseuille_long_run():
+    """Gravity-driven Poiseuille, MRT + Guo 2nd order, 20,000 steps."""
+    from pylabolt_gb300 import workloads
+    case_d, _ = workloads.poiseuille(nx=64, ny=128)
+    case = Case(case_d)
+    fluid = ~case.solid
+    _, u64, _, _ = _run(case, "fp64", 20000)
+    _, u32, _, _ = _run(case, "fp32_shifted", 20000)
+    assert np.linalg.norm(u32[fluid] - u64[fluid]) / np.linalg.norm(u64[fluid]) <= FP32_LONG_TOL

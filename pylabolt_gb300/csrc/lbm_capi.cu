@@ -678,6 +678,12 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
     p.f_i2 = (float)p.inv_cs_2;
     p.f_i4 = (float)p.inv_cs_4;
     p.f_homh = (float)p.one_m_half_omega;
+    const double rates[4] = {c.mrt_s[0], c.mrt_s[1], c.mrt_s[2], c.mrt_s[3]};
+    const double norm2[4] = {36.0, 36.0, 12.0, 4.0};   // |row|^2 of e, eps, q, nu
+    for (int i = 0; i < 4; ++i) {
+      p.f_mrt_s[i] = (float)(-rates[i] / norm2[i]);
+      p.f_mrt_h[i] = (float)((1.0 - 0.5 * rates[i]) / norm2[i]);
+    }
   }
   if (c.body_force_field) {
     if ((rc = h->alloc(&h->body, 2 * plane * cb))) return bail(rc);

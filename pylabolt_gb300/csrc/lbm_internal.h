@@ -44,6 +44,9 @@ struct Params {
   float f_omh[3];            // (1 - omega/2) * w * scale for |c|^2 = 0, 1, 2
   float f_gx, f_gy, f_scale, f_inv_scale;
   float f_i2, f_i4, f_homh;  // inv_cs_2, inv_cs_4, 1 - omega/2 of the FP32 paths
+  // MRT of the shifted paths, per relaxed moment (e, eps, q, nu):
+  // -s / |row|^2 and (1 - s/2) / |row|^2
+  float f_mrt_s[4], f_mrt_h[4];
 };
 
 enum StepFlags {

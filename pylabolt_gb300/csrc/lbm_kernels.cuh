@@ -338,33 +338,6 @@ __device__ __forceinline__ void mrt_collide(T f[9], T rho, T drho, T ux, T uy,
 #pragma unroll
   for (int i = 0; i < 9; ++i)
     a[i] = (m[i] - S[i] * (m[i] - meq[i]) + (T(1) - T(0.5) * S[i]) * mf[i]) * inv_norm[i];
-  if (SHIFTED && p.inv_cs_2 == 3.0 && p.inv_cs_4 == 9.0) {
-    // Delta form (shifted storage, D2Q9 constants): f* = f + M^-1 dm with
-    // dm = -S (m - meq) + (1 - S/2) mf on the non-conserved moments and the
-    // exact changes of the conserved ones (0 for rho; F for j, since
-    // meq_j + mf_j / 2 = rho u + F / 2 = j + F).  Reconstructing f* whole
-    // rounds at the scale of f and, as the flow changes slowly, the same
-    // mass / momentum defect repeats every step (1e-4 relative velocity drift
-    // in 10^4 steps); the correction M^-1 dm is small and its rounding is too.
-    a[0] = T(0);
-    a[3] = mf[3] * inv_norm[3];
-    a[5] = mf[5] * inv_norm[5];
-#pragma unroll
-    for (int i = 0; i < 9; ++i)
-      if (i != 0 && i != 3 && i != 5) a[i] = (-S[i] * (m[i] - meq[i]) + (T(1) - T(0.5) * S[i]) * mf[i]) * inv_norm[i];
-    const T b = a[0] - a[1] - T(2) * a[2];
-    const T c = a[0] + T(2) * a[1] + a[2];
-    f[0] += a[0] - T(4) * a[1] + T(4) * a[2];
-    f[1] += b + a[3] - T(2) * a[4] + a[7];
-    f[2] += b + a[5] - T(2) * a[6] - a[7];
-    f[3] += b - a[3] + T(2) * a[4] + a[7];
-    f[4] += b - a[5] + T(2) * a[6] - a[7];
-    f[5] += c + a[3] + a[4] + a[5] + a[6] + a[8];
-    f[6] += c - a[3] - a[4] + a[5] + a[6] - a[8];
-    f[7] += c - a[3] - a[4] - a[5] - a[6] + a[8];
-    f[8] += c + a[3] + a[4] - a[5] - a[6] - a[8];
-    return;
-  }
   // f = M^T diag(1/|row|^2) m*
   const T b = a[0] - a[1] - T(2) * a[2];
   const T c = a[0] + T(2) * a[1] + a[2];
@@ -429,6 +402,75 @@ __device__ __forceinline__ R warp_sum(R v) {
 }
 
 // ---------------------------------------------------------------------------
+// MRT on shifted storage in delta form: G* = G + M^-1 dm, in stored units
+// G = scale * g, with the D2Q9 constants (inv_cs_2 = 3, inv_cs_4 = 9; the
+// shifted paths always use them).  dm = -S (m - meq) + (1 - S/2) mf on the
+// non-conserved moments e, eps, qx, qy, pxx, pxy, and the exact changes of
+// the conserved ones: 0 for rho and F for j (meq_j + mf_j / 2 = rho u + F/2 =
+// j + F).  Reconstructing G* whole rounds at the scale of G and, as the flow
+// changes slowly, the same mass / momentum defect repeats every step (1e-4
+// relative velocity drift in 10^4 steps); the correction M^-1 dm is small and
+// so is its rounding.  Same moments as mrt_collide, specialised: no
+// divisions, no conserved-moment work.
+template <int FORC>
+__device__ __forceinline__ void mrt_shifted(float G[9], float rho, float drho, float ux,
+                                            float uy, float Fx, float Fy, const Params& p) {
+  const float sc = p.f_scale;
+  const float a13 = G[1] + G[3], a24 = G[2] + G[4];
+  const float a14 = a13 + a24;
+  const float a57 = G[5] + G[7], a68 = G[6] + G[8];
+  const float a58 = a57 + a68;
+  const float d57 = G[5] - G[7], d68 = G[6] - G[8];
+  const float m_e = fmaf(-4.f, G[0], fmaf(2.f, a58, -a14));
+  const float m_eps = fmaf(4.f, G[0], fmaf(-2.f, a14, a58));
+  const float m_qx = fmaf(-2.f, G[1] - G[3], d57 - d68);
+  const float m_qy = fmaf(-2.f, G[2] - G[4], d57 + d68);
+  const float m_xx = a13 - a24;
+  const float m_xy = a57 - a68;
+  const float rs = rho * sc;
+  const float r3u2 = 3.f * rs * (ux * ux + uy * uy);
+  const float dr = drho * sc;
+  const float eq_e = fmaf(-2.f, dr, r3u2);
+  const float eq_eps = dr - r3u2;
+  const float eq_qx = -rs * ux, eq_qy = -rs * uy;
+  const float eq_xx = rs * (ux * ux - uy * uy), eq_xy = rs * ux * uy;
+  float da_e = p.f_mrt_s[0] * (m_e - eq_e);
+  float da_eps = p.f_mrt_s[1] * (m_eps - eq_eps);
+  float da_qx = p.f_mrt_s[2] * (m_qx - eq_qx);
+  float da_qy = p.f_mrt_s[2] * (m_qy - eq_qy);
+  float da_xx = p.f_mrt_s[3] * (m_xx - eq_xx);
+  float da_xy = p.f_mrt_s[3] * (m_xy - eq_xy);
+  float da_jx = 0.f, da_jy = 0.f;
+  if (FORC != 0) {
+    const float fx = sc * Fx, fy = sc * Fy;
+    da_jx = fx * (1.f / 6.f);
+    da_jy = fy * (1.f / 6.f);
+    da_qx = fmaf(p.f_mrt_h[2], -fx, da_qx);
+    da_qy = fmaf(p.f_mrt_h[2], -fy, da_qy);
+    if (FORC == 2) {
+      const float uF = ux * fx + uy * fy;
+      da_e = fmaf(p.f_mrt_h[0], 6.f * uF, da_e);
+      da_eps = fmaf(p.f_mrt_h[1], -6.f * uF, da_eps);
+      da_xx = fmaf(p.f_mrt_h[3], 2.f * (fx * ux - fy * uy), da_xx);
+      da_xy = fmaf(p.f_mrt_h[3], fx * uy + fy * ux, da_xy);
+    }
+  }
+  // G* - G = M^T diag(1/|row|^2) dm
+  const float b = fmaf(-2.f, da_eps, -da_e);
+  const float c = fmaf(2.f, da_e, da_eps);
+  G[0] += 4.f * (da_eps - da_e);
+  const float x1 = fmaf(-2.f, da_qx, da_jx), y1 = fmaf(-2.f, da_qy, da_jy);
+  G[1] += (b + x1) + da_xx;
+  G[3] += (b - x1) + da_xx;
+  G[2] += (b + y1) - da_xx;
+  G[4] += (b - y1) - da_xx;
+  const float x2 = da_jx + da_qx, y2 = da_jy + da_qy;
+  G[5] += c + (x2 + y2) + da_xy;
+  G[6] += c + (y2 - x2) - da_xy;
+  G[7] += c - (x2 + y2) + da_xy;
+  G[8] += c + (x2 - y2) - da_xy;
+}
+
 // Moments, force, velocity and collision of one node: f holds the incoming
 // populations (f, or g = f - w when shifted) and receives the post-collision
 // ones.
@@ -475,16 +517,10 @@ __device__ __forceinline__ void node_update(typename Store<S>::T f[9], const Ste
     ux = (jx + T(0.5) * Fx) * inv_density;
     uy = (jy + T(0.5) * Fy) * inv_density;
   }
-  if constexpr (COLL == 1) {
-    if constexpr (Store<S>::scaled) {
-#pragma unroll
-      for (int k = 0; k < 9; ++k) f[k] *= p.f_inv_scale;
-    }
-    mrt_collide<FORC, SH>(f, rho, drho, ux, uy, Fx, Fy, p);
-    if constexpr (Store<S>::scaled) {
-#pragma unroll
-      for (int k = 0; k < 9; ++k) f[k] *= p.f_scale;
-    }
+  if constexpr (COLL == 1 && SH) {
+    mrt_shifted<FORC>(f, rho, drho, ux, uy, Fx, Fy, p);
+  } else if constexpr (COLL == 1) {
+    mrt_collide<FORC, false>(f, rho, drho, ux, uy, Fx, Fy, p);
   } else if constexpr (!SH) {
     const T hu2 = T(p.half_inv_cs_2) * (ux * ux + uy * uy);
     f[0] = bgk_ref_k<0, FORC>(f[0], rho, ux, uy, hu2, Fx, Fy, p);

@@ -215,6 +215,53 @@ int lbm_set_force_links(LbmHandle* h, const LbmForceLink* links, int64_t nlinks,
  * gives the t = 0 values (pop = pop_new = f_eq, fluidLB.py:323-335). */
 int lbm_forces(LbmHandle* h, double* out);
 
+/* A circular obstacle that moves (extension: the reference's moving-obstacle
+ * path cannot run, pylabolt/base/obstacle_operator.py:47-73 calls an undefined
+ * reconstruct_obstacles).  Each step, before the fused step:
+ *   1. motion (update_position_velocity, pylabolt/parallel/cpu/
+ *      obstacle_kernels.py:386-460, from the last step's force / torque):
+ *      calculated: omega += T/I (rotation), v += F/m + g (translation);
+ *      angle += omega_old + T/(2I); center += v_old + (F/m + g)/2;
+ *   2. re-rasterisation: (x-cx)^2 + (y-cy)^2 <= r^2 is solid, with velocity
+ *      v + omega x r and the obstacle's density; nodes it leaves become fluid
+ *      and are refilled with f_eq(mean rho of their fluid neighbours, the
+ *      wall velocity they had);
+ *   3. fluid nodes next to it pull moving-solid bounce-back
+ *      pop[x,kbar] - 2 w rho(x) inv_cs_2 (c_kbar . u_solid) at run time
+ *      (streaming_kernels.py:41-47);
+ * and after it the momentum exchange on the obstacle (force_torque_kernels.py:
+ * 11-90) feeds the next motion.  An obstacle must stay two nodes away from
+ * the domain edges and from static solids / boundary nodes, and move less
+ * than one node per step; a step that would break this fails with
+ * LBM_ERR_STATE and leaves the obstacle where it was. */
+typedef struct {
+  double center[2];        /* position, lattice units                        */
+  double radius;
+  double velocity[2];      /* linear velocity                                */
+  double omega;            /* angular velocity                               */
+  double angle;            /* inclination                                    */
+  double mass, inertia;    /* pi r^2 rho_s and m r^2 / 2 (obstacle.py)       */
+  double density;          /* rho_s: the density reported on its nodes       */
+  double force[2], torque; /* momentum exchange of the last step (output)    */
+  int32_t id;              /* obstacle id: reference order in obstacle_dict  */
+  int32_t calculated;      /* 1: velocities follow the force and torque      */
+  int32_t rotation, translation;  /* degrees of freedom                      */
+} LbmMovingObstacle;
+
+/* Registers the moving obstacles (at most 32) and the gravity of their
+ * motion; call after lbm_create and before lbm_init_fields.  Only the scalar
+ * step kernel serves a case with moving obstacles. */
+int lbm_set_moving_obstacles(LbmHandle* h, const LbmMovingObstacle* obs, int n,
+                             const double gravity[2]);
+
+/* Current state of the moving obstacles (position, velocities, force and
+ * torque of the last step), in registration order. */
+int lbm_get_moving_obstacles(LbmHandle* h, LbmMovingObstacle* out);
+
+/* Node flags of the current geometry, inner layout [nx*ny]: 0 fluid, 1 static
+ * solid, 2 + i solid of moving obstacle i (registration order). */
+int lbm_get_node_flags(LbmHandle* h, uint8_t* flags);
+
 /* Number of completed steps since the last init. */
 int lbm_time(LbmHandle* h, int64_t* t);
 

@@ -46,6 +46,16 @@ class LbmConfig(ctypes.Structure):
                 ("fp16_scale", ctypes.c_double)]
 
 
+class LbmMovingObstacle(ctypes.Structure):
+    _fields_ = [("center", ctypes.c_double * 2), ("radius", ctypes.c_double),
+                ("velocity", ctypes.c_double * 2), ("omega", ctypes.c_double),
+                ("angle", ctypes.c_double), ("mass", ctypes.c_double),
+                ("inertia", ctypes.c_double), ("density", ctypes.c_double),
+                ("force", ctypes.c_double * 2), ("torque", ctypes.c_double),
+                ("id", ctypes.c_int32), ("calculated", ctypes.c_int32),
+                ("rotation", ctypes.c_int32), ("translation", ctypes.c_int32)]
+
+
 class LbmPopView(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("nx", ctypes.c_int32), ("ny", ctypes.c_int32),
                 ("reserved", ctypes.c_int32), ("pitch", ctypes.c_int64), ("plane", ctypes.c_int64),
@@ -75,7 +85,8 @@ EXPORTS = ["lbm_create", "lbm_init_fields", "lbm_set_body_force", "lbm_step",
            "lbm_kernel_launches", "lbm_kernel_variant", "lbm_tuning", "lbm_device_bytes", "lbm_time_steps",
            "lbm_synchronize", "lbm_last_error", "lbm_destroy", "lbm_conservation_noalloc",
            "lbm_adjoint_forward", "lbm_adjoint_backward", "lbm_set_omega_map",
-           "lbm_set_force_links", "lbm_forces"]
+           "lbm_set_force_links", "lbm_forces", "lbm_set_moving_obstacles",
+           "lbm_get_moving_obstacles", "lbm_get_node_flags"]
 
 
 def lib_path():
@@ -119,6 +130,9 @@ def load(build=True):
         "lbm_adjoint_backward": [P, P, P, dbl, P],
         "lbm_set_force_links": [P, P, i64, ctypes.c_int],
         "lbm_forces": [P, P],
+        "lbm_set_moving_obstacles": [P, P, ctypes.c_int, P],
+        "lbm_get_moving_obstacles": [P, P],
+        "lbm_get_node_flags": [P, P],
     }
     for name, argtypes in sig.items():
         fn = getattr(lib, name)

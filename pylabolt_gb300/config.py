@@ -101,6 +101,15 @@ class Obstacle:
         self.static = static
         self.linear_velocity = np.asarray(linear_velocity, dtype=np.float64)
         self.angular_velocity = float(angular_velocity)
+        # solid_motion_dict (obstacle.py:478-538); mass and moment of inertia
+        # of a disc of the obstacle's density (obstacle.py:475-476)
+        self.motion_type = None
+        self.calculated = False
+        self.rotation_allowed = False
+        self.translation_allowed = False
+        r = float(radius) if radius is not None else 0.0
+        self.mass = np.pi * r * r * density
+        self.moment_of_inertia = self.mass * r * r / 2
 
 
 class Case:
@@ -389,17 +398,42 @@ class Case:
                     if key not in sm:
                         raise ValueError(key + " missing in solid_motion_dict: " + name)
                 lin, ang = sm["linear_velocity"], sm["angular_velocity"]
+                if sm["type"] not in ("fixed_velocity", "calculated"):
+                    raise ValueError("Unsupported motion type: " + str(sm["type"]) +
+                                     " in obstacle: " + name)
+                if sm["degree_of_freedom"] not in ("rotation", "translation", "both"):
+                    raise ValueError("Unsupported degree of freedom: " +
+                                     str(sm["degree_of_freedom"]) + " in obstacle: " + name)
+                if not isinstance(lin, list):
+                    raise ValueError("linear_velocity must be list [ux, uy]: " + name)
+                if not isinstance(ang, (int, float)):
+                    raise ValueError("angular_velocity must be int/float: " + name)
             obs = Obstacle(oid, name, "circle", d["center"], float(d["radius"]),
                            float(d["density"]), bool(d["static"]), lin, ang)
+            if not d["static"]:
+                sm = d["solid_motion_dict"]
+                obs.motion_type = sm["type"]
+                obs.calculated = sm["type"] == "calculated"
+                obs.rotation_allowed = sm["degree_of_freedom"] in ("rotation", "both")
+                obs.translation_allowed = sm["degree_of_freedom"] in ("translation", "both")
             self.obstacles.append(obs)
-            self._rasterise_circle(obs)
+            moving = (not obs.static) and bool(opts.get("move_obstacles", False))
+            self._rasterise_circle(obs, solid=not moving)
         if any(not o.static for o in self.obstacles) and not self.compute_force_torque:
             raise ValueError("If any obstacle is not static, "
                              "then compute_force_torque must be True")
+        # extension: move the non-static obstacles (the reference's moving path
+        # cannot run; without this key they keep their place and act as moving
+        # walls, which is what the reference's kernels do for one step)
+        self.move_obstacles = bool(opts.get("move_obstacles", False))
+        if not isinstance(opts.get("move_obstacles", False), (bool, np.bool_)):
+            raise ValueError("move_obstacles must be bool: True/False (default: False)")
+        self.moving = [o for o in self.obstacles if not o.static] if self.move_obstacles else []
 
-    def _rasterise_circle(self, obs):
+    def _rasterise_circle(self, obs, solid=True):
         """dist^2 <= r^2 with the periodic minimum image (obstacle_kernels.py:11-93);
-        solid nodes take the body velocity and density."""
+        solid nodes take the body velocity and density.  solid=False (a moving
+        obstacle) sets only the fields: the device places it."""
         X, Y = np.meshgrid(np.arange(self.nx, dtype=np.float64),
                            np.arange(self.ny, dtype=np.float64), indexing="ij")
         rx = X - obs.center[0]
@@ -417,8 +451,9 @@ class Case:
             rym = np.where(np.abs(b) < np.abs(rym), b, rym)
         r = np.float64(obs.radius)
         inside = rxm * rxm + rym * rym <= r * r
-        self.solid |= inside
-        self.solid_id[inside] = obs.id
+        if solid:
+            self.solid |= inside
+            self.solid_id[inside] = obs.id
         lin = obs.linear_velocity
         ang = np.float64(obs.angular_velocity)
         self.velocity[inside, 0] = lin[0] - ang * rym[inside]

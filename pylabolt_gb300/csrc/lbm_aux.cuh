@@ -3,6 +3,7 @@
 #pragma once
 #include "lbm_adjoint.cuh"
 #include "lbm_force.cuh"
+#include "lbm_moving.cuh"
 
 namespace lbm {
 
@@ -185,6 +186,24 @@ struct Kernels {
     force_kernel<S><<<ngroups, kForceBlock, 0, s>>>(a);
     return cudaGetLastError();
   }
+  static cudaError_t mov_motion(const MovArgs& a, cudaStream_t s) {
+    mov_motion_kernel<S><<<1, kMovMaxObstacles, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  static cudaError_t mov_raster(const MovArgs& a, int side, cudaStream_t s) {
+    const dim3 blk(16, 16), grid((side + 15) / 16, (side + 15) / 16);
+    mov_raster_kernel<S><<<grid, blk, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  static cudaError_t mov_classify(const MovArgs& a, int side, cudaStream_t s) {
+    const dim3 blk(16, 16), grid((side + 2 + 15) / 16, (side + 2 + 15) / 16);
+    mov_classify_kernel<S><<<grid, blk, 0, s>>>(a);
+    return cudaGetLastError();
+  }
+  static cudaError_t mov_force(const MovArgs& a, cudaStream_t s) {
+    mov_force_kernel<S><<<1, 32, 0, s>>>(a);
+    return cudaGetLastError();
+  }
   static KernelSet make() {
     KernelSet k;
     k.elem_bytes = sizeof(S);
@@ -211,6 +230,10 @@ struct Kernels {
     k.body_from_f64 = &body_from_f64;
     k.conservation = &conservation;
     k.forces = &forces;
+    k.mov_motion = &mov_motion;
+    k.mov_raster = &mov_raster;
+    k.mov_classify = &mov_classify;
+    k.mov_force = &mov_force;
     if constexpr (sizeof(S) >= 4)
       k.adjoint = &adjoint<S>;
     else

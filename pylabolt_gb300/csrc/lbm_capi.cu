@@ -110,6 +110,20 @@ struct LbmHandle {
     int64_t graph_T = -1;
     int graph_interval = -1;
   } adj;
+  // moving obstacles (lbm_set_moving_obstacles)
+  struct Mov {
+    int n = 0;
+    int side = 0;                    // raster launch covers side x side nodes
+    lbm::MovObs* obs = nullptr;      // device state
+    std::vector<lbm::MovObs> init;   // registered state (restored by lbm_init_fields)
+    uint8_t* dsolid = nullptr;
+    uint8_t* fresh = nullptr;
+    void* us = nullptr;
+    void* rho_dyn[2] = {nullptr, nullptr};   // swapped with the population buffers
+    uint8_t* cls_static = nullptr;   // classes / segment flags without moving obstacles
+    uint8_t* seg_static = nullptr;
+    double gx = 0.0, gy = 0.0;
+  } mov;
   // momentum-exchange links (lbm_set_force_links)
   struct Force {
     long long* node = nullptr;
@@ -166,7 +180,16 @@ struct LbmHandle {
       cudaError_t e = cudaStreamQuery(stream);
       if (e == cudaSuccess) {
         if (err_host && *reinterpret_cast<volatile int*>(err_host) != 0) {
+          const int code = *reinterpret_cast<volatile int*>(err_host);
           *err_host = 0;
+          if (code == lbm::kErrMovBounds)
+            return fail(LBM_ERR_STATE, "a moving obstacle would come within two nodes of the domain edge; "
+                                       "it was left where it was");
+          if (code == lbm::kErrMovSpeed)
+            return fail(LBM_ERR_STATE, "a moving obstacle would move a node or more in one step; "
+                                       "it was left where it was");
+          if (code == lbm::kErrMovNeighbour)
+            return fail(LBM_ERR_STATE, "a moving obstacle reached a boundary node or a static solid");
           return fail(LBM_ERR_TIMEOUT, "a bounded mbarrier wait in the step kernel expired");
         }
         return LBM_OK;
@@ -216,14 +239,16 @@ struct LbmHandle {
   int launch(int flags, bool advance = true) { return launch_v(flags, variant, advance); }
 
   int launch_v(int flags, lbm::Variant v, bool advance) {
-    const int rc = launch_bufs(flags, v, pop[cur], pop[cur ^ 1], side[cur], side[cur ^ 1]);
+    const int rc = launch_bufs(flags, v, pop[cur], pop[cur ^ 1], side[cur], side[cur ^ 1], nullptr,
+                               mov.rho_dyn[cur], mov.rho_dyn[cur ^ 1]);
     if (rc == LBM_OK && advance) cur ^= 1;
     return rc;
   }
 
   // One fused step from `fin` / `side_in` into `fout` / `side_out`.
   int launch_bufs(int flags, lbm::Variant v, const void* fin, void* fout, const void* sin,
-                  void* sout, cudaStream_t on = nullptr) {
+                  void* sout, cudaStream_t on = nullptr, const void* rdin = nullptr,
+                  void* rdout = nullptr) {
     lbm::StepArgs a;
     a.g = g;
     a.p = p;
@@ -244,6 +269,10 @@ struct LbmHandle {
     a.body = body;
     a.err = err_dev;
     a.omega_seg = omega_seg;
+    a.dsolid = mov.dsolid;
+    a.us = mov.us;
+    a.rho_dyn_in = rdin;
+    a.rho_dyn_out = rdout;
     a.flags = flags;
     LBM_CUDA(ks->step(cfg.collision, cfg.forcing, a, v, sms, on ? on : stream));
     return LBM_OK;
@@ -255,6 +284,7 @@ struct LbmHandle {
     if (adj.tables) return adj.unsupported.empty() ? LBM_OK : fail(LBM_ERR_ARG, adj.unsupported);
     adj.tables = true;
     if (cfg.collision != LBM_BGK) adj.unsupported = "adjoint: only BGK collision is supported";
+    if (mov.n) adj.unsupported = "adjoint: moving obstacles are not supported";
     if (!ks->adjoint) adj.unsupported = "adjoint: FP64 or FP32-shifted storage is required";
     const int nx = g.nx, ny = g.ny, pitch = g.pitch;
     auto dev = [&](int64_t node) { return (long long)(node % ny + 1) * pitch + node / ny; };
@@ -363,6 +393,8 @@ struct LbmHandle {
         for (int i = 0; i < ks->nvariants; ++i)
           if (ks->variants[i].kind == kind && ks->variants[i].vec == vec &&
               ks->variants[i].block == blk && ks->variants[i].stages == st) {
+            if (mov.n && kind != 0)
+              return fail(LBM_ERR_ARG, "LBM_VARIANT: moving obstacles need the scalar kernel (kind 0)");
             variant = ks->variants[i];
             return LBM_OK;
           }
@@ -370,6 +402,12 @@ struct LbmHandle {
       }
     }
     variant = ks->variants[0];
+    if (mov.n)
+      for (int i = 0; i < ks->nvariants; ++i)
+        if (ks->variants[i].kind == 0) {
+          variant = ks->variants[i];
+          break;
+        }
     const char* t = std::getenv("LBM_TUNE");
     if (t && t[0] == '0') return LBM_OK;
     const int flags = 0;
@@ -380,6 +418,10 @@ struct LbmHandle {
     int rc = LBM_OK;
     for (int i = 0; i < ks->nvariants && rc == LBM_OK; ++i) {
       const lbm::Variant v = ks->variants[i];
+      if (mov.n && v.kind != 0) {   // class-4 links are served by the scalar kernel only
+        tune_ms[i] = 1e30;
+        continue;
+      }
       if ((rc = launch_v(flags, v, false))) break;
       cudaEventRecord(e0, stream);
       for (int r = 0; r < 3 && rc == LBM_OK; ++r) rc = launch_v(flags, v, false);
@@ -428,12 +470,58 @@ struct LbmHandle {
     return rc;
   }
 
+  lbm::MovArgs mov_args(int j, int nopull_state) {
+    lbm::MovArgs a;
+    a.g = g;
+    a.p = p;
+    a.obs = mov.obs;
+    a.n = mov.n;
+    a.j = j;
+    a.gx = mov.gx;
+    a.gy = mov.gy;
+    a.dsolid = mov.dsolid;
+    a.fresh = mov.fresh;
+    a.cls = const_cast<uint8_t*>(g.cls);
+    a.segflag = const_cast<uint8_t*>(g.segflag);
+    a.us = mov.us;
+    a.rho_dyn = mov.rho_dyn[cur];
+    a.pop = pop[cur];
+    a.mr = mom[0];
+    a.mx = mom[1];
+    a.my = mom[2];
+    a.nopull = nopull_state;
+    a.err = err_dev;
+    return a;
+  }
+
+  // Geometry of the moving obstacles for the coming step (motion = false:
+  // only place them at their current position, as at initialisation).
+  int mov_geometry(bool motion) {
+    LBM_CUDA(ks->mov_motion(mov_args(motion ? 0 : -1, 0), stream));
+    for (int j = 0; j < mov.n; ++j) LBM_CUDA(ks->mov_raster(mov_args(j, 0), mov.side, stream));
+    for (int j = 0; j < mov.n; ++j) LBM_CUDA(ks->mov_classify(mov_args(j, 0), mov.side, stream));
+    return LBM_OK;
+  }
+  int mov_forces(int nopull_state) {
+    for (int j = 0; j < mov.n; ++j) LBM_CUDA(ks->mov_force(mov_args(j, nopull_state), stream));
+    return LBM_OK;
+  }
+
+  // One time step with the moving-obstacle work around the fused step.
+  int step_full(int flags) {
+    int rc;
+    if (mov.n && (rc = mov_geometry(true))) return rc;
+    if ((rc = launch(flags))) return rc;
+    if (mov.n && (rc = mov_forces(0))) return rc;
+    return LBM_OK;
+  }
+
   int capture_graph() {
     cudaGraph_t graph = nullptr;
     LBM_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     const int c0 = cur;
     int rc = LBM_OK;
-    for (int i = 0; i < kGraphChunk && rc == LBM_OK; ++i) rc = launch(0);
+    for (int i = 0; i < kGraphChunk && rc == LBM_OK; ++i) rc = step_full(0);
     cudaError_t e = cudaStreamEndCapture(stream, &graph);
     cur = c0;
     if (rc) {
@@ -719,11 +807,30 @@ int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout
   LBM_CUDA(cudaMemsetAsync(ds, 0, 3 * plane * sizeof(double), h->stream));
   LBM_CUDA(lbm::reorder(h->g, hs, ds, 1, layout, 1, h->stream));
   LBM_CUDA(lbm::reorder(h->g, hs + nh, ds + plane, 2, layout, 1, h->stream));
+  if (h->mov.n) {   // static classes back before f_eq is written (a run may have moved obstacles)
+    LBM_CUDA(cudaMemcpyAsync(const_cast<uint8_t*>(h->g.cls), h->mov.cls_static, plane,
+                             cudaMemcpyDeviceToDevice, h->stream));
+    LBM_CUDA(cudaMemcpyAsync(const_cast<uint8_t*>(h->g.segflag), h->mov.seg_static,
+                             (size_t)h->g.ny * h->g.nseg, cudaMemcpyDeviceToDevice, h->stream));
+  }
   LBM_CUDA(h->ks->init(h->g, h->p, ds, ds + plane, h->pop[h->cur], h->mom[0], h->mom[1],
                        h->mom[2], h->stream));
   for (int i = 0; i < 6; ++i)
     LBM_CUDA(cudaMemsetAsync(h->old[i], 0, plane * h->ks->compute_bytes, h->stream));
   h->old_cur = 0;
+  if (h->mov.n) {
+    // registered obstacle state, static classes, then the obstacles placed,
+    // their nodes classified and the t = 0 momentum exchange (the reference
+    // computes forces before the first step, fluidLB.py:323-335)
+    auto& M = h->mov;
+    const size_t cb = h->ks->compute_bytes;
+    LBM_CUDA(cudaMemcpyAsync(M.obs, M.init.data(), M.n * sizeof(lbm::MovObs), cudaMemcpyHostToDevice,
+                             h->stream));
+    LBM_CUDA(cudaMemsetAsync(M.dsolid, 0, plane, h->stream));
+    LBM_CUDA(cudaMemsetAsync(M.fresh, 0, plane, h->stream));
+    LBM_CUDA(cudaMemcpyAsync(M.rho_dyn[h->cur], h->mom[0], plane * cb, cudaMemcpyDeviceToDevice, h->stream));
+    if ((rc = h->mov_geometry(false)) || (rc = h->mov_forces(1))) return rc;
+  }
   if ((rc = h->wait())) return rc;
   h->initialized = true;
   h->nopull = true;
@@ -795,7 +902,7 @@ int lbm_step_ex(LbmHandle* h, int64_t nsteps, int flags) {
   int64_t s = 0;
   int rc;
   auto one = [&](int fl) {
-    int r = h->launch(fl);
+    int r = h->step_full(fl);
     if (r) return r;
     if (fl & lbm::F_RESIDUAL) h->old_cur ^= 1;
     h->nopull = false;
@@ -1107,6 +1214,7 @@ int lbm_get_populations(LbmHandle* h, double* pop) {
 
 int lbm_set_populations(LbmHandle* h, const double* pop_new) {
   if (!h || !pop_new) return fail(LBM_ERR_ARG, "lbm_set_populations: null argument");
+  if (h->mov.n) return fail(LBM_ERR_STATE, "lbm_set_populations: not supported with moving obstacles");
   LBM_CUDA(cudaSetDevice(h->cfg.device));
   const long long nh = h->host_nodes(LBM_LAYOUT_PADDED), plane = h->g.plane;
   int rc = h->ensure_stage(9 * nh + 9 * plane);
@@ -1209,6 +1317,145 @@ int lbm_forces(LbmHandle* h, double* out) {
   LBM_CUDA(h->ks->forces(a, F.ngroups, h->stream));
   LBM_CUDA(cudaMemcpyAsync(out, F.out, 3 * (size_t)F.ngroups * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   return h->wait();
+}
+
+int lbm_set_moving_obstacles(LbmHandle* h, const LbmMovingObstacle* obs, int n,
+                             const double gravity[2]) {
+  if (!h || (n > 0 && !obs)) return fail(LBM_ERR_ARG, "lbm_set_moving_obstacles: null argument");
+  if (n < 0 || n > lbm::kMovMaxObstacles)
+    return fail(LBM_ERR_ARG, "lbm_set_moving_obstacles: 0 to " + std::to_string(lbm::kMovMaxObstacles) +
+                                 " obstacles");
+  if (h->mov.n) return fail(LBM_ERR_STATE, "lbm_set_moving_obstacles: already set");
+  if (n == 0) return LBM_OK;
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  const lbm::Geom& g = h->g;
+  auto& M = h->mov;
+  M.init.assign(n, lbm::MovObs{});
+  double rmax = 0.0;
+  for (int j = 0; j < n; ++j) {
+    const LbmMovingObstacle& o = obs[j];
+    lbm::MovObs& m = M.init[j];
+    if (!(o.radius > 0.0) || !std::isfinite(o.center[0]) || !std::isfinite(o.center[1]))
+      return fail(LBM_ERR_ARG, "lbm_set_moving_obstacles: obstacle " + std::to_string(j) + ": bad radius or centre");
+    if (o.calculated && ((o.translation && !(o.mass > 0.0)) || (o.rotation && !(o.inertia > 0.0))))
+      return fail(LBM_ERR_ARG, "lbm_set_moving_obstacles: obstacle " + std::to_string(j) + ": mass and inertia must be > 0");
+    m.cx = o.center[0];
+    m.cy = o.center[1];
+    m.r = o.radius;
+    m.vx = o.velocity[0];
+    m.vy = o.velocity[1];
+    m.om = o.omega;
+    m.angle = o.angle;
+    m.mass = o.mass;
+    m.inertia = o.inertia;
+    m.density = o.density;
+    m.fx = m.fy = m.tq = 0.0;
+    m.id = o.id;
+    m.calculated = o.calculated;
+    m.rotation = o.rotation;
+    m.translation = o.translation;
+    // the initial box with its border must lie in [1, nx-2] x [1, ny-2] and
+    // in static bulk fluid
+    const int bx0 = (int)std::floor(m.cx - m.r) - 1, bx1 = (int)std::ceil(m.cx + m.r) + 1;
+    const int by0 = (int)std::floor(m.cy - m.r) - 1, by1 = (int)std::ceil(m.cy + m.r) + 1;
+    if (bx0 < 2 || by0 < 2 || bx1 > g.nx - 3 || by1 > g.ny - 3)
+      return fail(LBM_ERR_ARG, "lbm_set_moving_obstacles: obstacle " + std::to_string(j) +
+                                   " must stay two nodes away from the domain edges");
+    for (int y = by0 - 1; y <= by1 + 1; ++y)
+      for (int x = bx0 - 1; x <= bx1 + 1; ++x)
+        if (h->h_cls[g.node(x, y)] != 0)
+          return fail(LBM_ERR_ARG, "lbm_set_moving_obstacles: obstacle " + std::to_string(j) +
+                                       " starts next to a boundary node or a static solid");
+    rmax = std::max(rmax, m.r);
+  }
+  M.side = 2 * (int)std::ceil(rmax) + 8;
+  M.gx = gravity ? gravity[0] : 0.0;
+  M.gy = gravity ? gravity[1] : 0.0;
+  const size_t plane = g.plane, cb = h->ks->compute_bytes;
+  const size_t nseg = (size_t)g.ny * g.nseg;
+  int rc;
+  if ((rc = h->alloc(reinterpret_cast<void**>(&M.obs), n * sizeof(lbm::MovObs))) ||
+      (rc = h->alloc(reinterpret_cast<void**>(&M.dsolid), plane)) ||
+      (rc = h->alloc(reinterpret_cast<void**>(&M.fresh), plane)) ||
+      (rc = h->alloc(&M.us, 2 * plane * cb)) || (rc = h->alloc(&M.rho_dyn[0], plane * cb)) ||
+      (rc = h->alloc(&M.rho_dyn[1], plane * cb)) ||
+      (rc = h->alloc(reinterpret_cast<void**>(&M.cls_static), plane)) ||
+      (rc = h->alloc(reinterpret_cast<void**>(&M.seg_static), nseg)))
+    return rc;
+  LBM_CUDA(cudaMemsetAsync(M.us, 0, 2 * plane * cb, h->stream));
+  LBM_CUDA(cudaMemsetAsync(M.dsolid, 0, plane, h->stream));
+  LBM_CUDA(cudaMemsetAsync(M.fresh, 0, plane, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(M.cls_static, h->g.cls, plane, cudaMemcpyDeviceToDevice, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(M.seg_static, h->g.segflag, nseg, cudaMemcpyDeviceToDevice, h->stream));
+  M.n = n;
+  // only the scalar kernel serves class-4 nodes: every launch from now on,
+  // the no-pull first step included, uses a scalar shape (re-picked among
+  // the scalar candidates by the autotuner)
+  for (int i = 0; i < h->ks->nvariants; ++i)
+    if (h->ks->variants[i].kind == 0) {
+      h->variant = h->ks->variants[i];
+      break;
+    }
+  h->tuned = false;
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  return h->wait();
+}
+
+int lbm_get_moving_obstacles(LbmHandle* h, LbmMovingObstacle* out) {
+  if (!h || !out) return fail(LBM_ERR_ARG, "lbm_get_moving_obstacles: null argument");
+  auto& M = h->mov;
+  if (!M.n) return LBM_OK;
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  std::vector<lbm::MovObs> st(M.n);
+  LBM_CUDA(cudaMemcpyAsync(st.data(), M.obs, M.n * sizeof(lbm::MovObs), cudaMemcpyDeviceToHost, h->stream));
+  int rc = h->wait();
+  if (rc) return rc;
+  for (int j = 0; j < M.n; ++j) {
+    const lbm::MovObs& m = st[j];
+    LbmMovingObstacle& o = out[j];
+    o.center[0] = m.cx;
+    o.center[1] = m.cy;
+    o.radius = m.r;
+    o.velocity[0] = m.vx;
+    o.velocity[1] = m.vy;
+    o.omega = m.om;
+    o.angle = m.angle;
+    o.mass = m.mass;
+    o.inertia = m.inertia;
+    o.density = m.density;
+    o.force[0] = m.fx;
+    o.force[1] = m.fy;
+    o.torque = m.tq;
+    o.id = m.id;
+    o.calculated = m.calculated;
+    o.rotation = m.rotation;
+    o.translation = m.translation;
+  }
+  return LBM_OK;
+}
+
+int lbm_get_node_flags(LbmHandle* h, uint8_t* flags) {
+  if (!h || !flags) return fail(LBM_ERR_ARG, "lbm_get_node_flags: null argument");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  const lbm::Geom& g = h->g;
+  std::vector<uint8_t> ds;
+  if (h->mov.n) {
+    ds.resize(g.plane);
+    LBM_CUDA(cudaMemcpyAsync(ds.data(), h->mov.dsolid, g.plane, cudaMemcpyDeviceToHost, h->stream));
+    int rc = h->wait();
+    if (rc) return rc;
+  }
+  for (long long x = 0; x < g.nx; ++x)
+    for (long long y = 0; y < g.ny; ++y) {
+      const long long n = g.node((int)x, (int)y);
+      uint8_t v = h->h_cls[n] == 2 ? 1 : 0;
+      if (!ds.empty() && ds[n]) v = (uint8_t)(1 + ds[n]);
+      flags[x * g.ny + y] = v;
+    }
+  return LBM_OK;
 }
 
 int lbm_time(LbmHandle* h, int64_t* t) {

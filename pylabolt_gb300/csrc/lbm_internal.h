@@ -75,6 +75,14 @@ struct StepArgs {
   const void* body;      // [2*plane] body force or null
   int* err;              // device-visible error word (bounded waits)
   const float* omega_seg;  // [ny*nseg] relaxation rate per 32-node segment, or null
+  // moving obstacles (class-4 nodes pull their links at run time)
+  const uint8_t* dsolid;   // [plane] 0, or 1 + index of the moving obstacle covering it
+  const void* us;          // [2*plane] velocity of moving-solid nodes (compute type)
+  // [plane] density of class-4 nodes: of the last step (read) and of this one
+  // (written); two buffers swapped with the populations, so that a launch
+  // that does not advance the state (autotuner) leaves it untouched
+  const void* rho_dyn_in;
+  void* rho_dyn_out;
   int flags;
 };
 
@@ -112,6 +120,33 @@ struct ForceArgs {
   double* out;            // [ngroups][3] fx, fy, torque
 };
 
+// A moving obstacle on the device (FP64 state, see lbm_set_moving_obstacles).
+struct MovObs {
+  double cx, cy, r, vx, vy, om, angle, mass, inertia, density, fx, fy, tq;
+  int id, calculated, rotation, translation;
+  int bx0, by0, bx1, by1;   // nodes the last move may have changed (inclusive)
+};
+
+// Arguments of the moving-obstacle kernels.
+struct MovArgs {
+  Geom g;
+  Params p;
+  MovObs* obs;
+  int n;                    // obstacles
+  int j;                    // obstacle of this launch (raster, classify, force)
+  double gx, gy;            // gravity of the motion
+  uint8_t* dsolid;
+  uint8_t* fresh;           // [plane] 1: left by an obstacle this step
+  uint8_t* cls;             // writable views of Geom::cls / segflag
+  uint8_t* segflag;
+  void* us;                 // [2*plane]
+  void* rho_dyn;            // [plane] buffer of the current state
+  void* pop;                // current state (storage type)
+  void* mr; void* mx; void* my;   // moments (solid nodes get rho_s, u_s)
+  int nopull;               // force: the state holds incoming populations
+  int* err;                 // device-visible error word
+};
+
 // Launch shape of the fused step.
 //   kind 0: scalar kernel, one node per thread
 //   kind 1: vector kernel, `vec` consecutive nodes per thread
@@ -127,6 +162,10 @@ struct Variant {
 constexpr int kTmaRowBytes = 4096;   // tile width in bytes of one plane row
 constexpr int kTmaHaloBytes = 16;    // TMA granule: halo on each side
 constexpr int kErrWaitTimeout = 1;   // err code: an mbarrier wait timed out
+constexpr int kErrMovBounds = 2;     // a moving obstacle would leave the allowed region
+constexpr int kErrMovSpeed = 3;      // a moving obstacle would move a node or more in a step
+constexpr int kErrMovNeighbour = 4;  // a moving obstacle reached a static solid or boundary node
+constexpr int kMovMaxObstacles = 32;
 
 // Kernels of one storage precision.
 struct KernelSet {
@@ -157,6 +196,12 @@ struct KernelSet {
   cudaError_t (*adjoint)(int forcing, const AdjArgs& a, cudaStream_t s);
   // momentum-exchange sums, one block per group
   cudaError_t (*forces)(const ForceArgs& a, int ngroups, cudaStream_t s);
+  // moving obstacles: motion (one thread each), raster and classify (one
+  // launch per obstacle over its box, side x side threads), momentum exchange
+  cudaError_t (*mov_motion)(const MovArgs& a, cudaStream_t s);
+  cudaError_t (*mov_raster)(const MovArgs& a, int side, cudaStream_t s);
+  cudaError_t (*mov_classify)(const MovArgs& a, int side, cudaStream_t s);
+  cudaError_t (*mov_force)(const MovArgs& a, cudaStream_t s);
 };
 
 const KernelSet& kernels_fp64();

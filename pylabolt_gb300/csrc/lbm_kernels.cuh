@@ -558,6 +558,45 @@ __device__ __forceinline__ void special_links(typename Store<S>::T f[9], const S
   }
 }
 
+// lin2 with run-time coefficients in {-1, 0, 1} (same IEEE result).
+template <class T>
+__device__ __forceinline__ T lin2r(int A, int B, T x, T y) {
+  if (A == 0 && B == 0) return T(0);
+  if (A == 0) return B > 0 ? y : -y;
+  if (B == 0) return A > 0 ? x : -x;
+  const T ax = A > 0 ? x : -x;
+  return B > 0 ? ax + y : ax - y;
+}
+
+// Incoming populations of a node next to a moving obstacle (class 4): pull,
+// or moving-solid bounce-back from a source the obstacle covers
+// (streaming_kernels.py:41-47; rho of this node from the previous step).
+template <class S>
+__device__ __forceinline__ void dynamic_links(typename Store<S>::T f[9], const StepArgs& a,
+                                              const S* __restrict__ fin, int ni) {
+  using T = typename Store<S>::T;
+  constexpr bool SH = Store<S>::shifted;
+  const Geom& g = a.g;
+  const Params& p = a.p;
+  const T* us = static_cast<const T*>(a.us);
+  const T rho = static_cast<const T*>(a.rho_dyn_in)[ni];
+#pragma unroll
+  for (int k = 1; k < 9; ++k) {
+    const int src = ni - CYk(k) * g.pitch - CXk(k);
+    const int kb = INVk(k);
+    T v;
+    if (a.dsolid[src]) {
+      const T raw = Store<S>::ld(fin + kb * g.plane, ni, p);
+      const T cu = lin2r<T>(CXk(kb), CYk(kb), us[src], us[g.plane + src]);
+      v = SH ? raw - (T(2.0 * Wk(kb)) * rho * T(3)) * cu
+             : raw - ((T(2.0 * Wk(kb)) * rho) * T(p.inv_cs_2)) * cu;
+    } else {
+      v = Store<S>::ld(fin + k * g.plane, src, p);
+    }
+    f[k] = Store<S>::scaled ? v * p.f_scale : v;
+  }
+}
+
 // Side data, moment output and residual terms of one updated node.  The
 // residual terms are formed in the compute type T (FP32 for shifted storage:
 // GB300's FP64 rate is a small fraction of its FP32 rate) and summed in FP64
@@ -640,7 +679,8 @@ __global__ void __launch_bounds__(CAP ? 256 : 512, CAP == 1 ? 8 : (CAP == 2 ? 6 
     const S* __restrict__ fin = static_cast<const S*>(a.fin);
     S* __restrict__ fout = static_cast<S*>(a.fout);
     int cls = 0;
-    if (g.segflag[y * g.nseg + (x >> 5)]) cls = g.cls[ni];
+    const bool seg = g.segflag[y * g.nseg + (x >> 5)] != 0;
+    if (seg) cls = g.cls[ni];
     if (cls != 2) {
       T f[9];
       int r = -1;
@@ -652,6 +692,9 @@ __global__ void __launch_bounds__(CAP ? 256 : 512, CAP == 1 ? 8 : (CAP == 2 ? 6 
 #pragma unroll
         for (int k = 0; k < 9; ++k)
           f[k] = Store<S>::ldr(fin + k * g.plane, ni - CYk(k) * g.pitch - CXk(k));
+      } else if (cls == 4) {
+        f[0] = Store<S>::ldr(fin, ni);
+        dynamic_links<S>(f, a, fin, ni);
       } else {
         f[0] = Store<S>::ldr(fin, n);
         special_links<S>(f, a, fin, n, r);
@@ -660,6 +703,10 @@ __global__ void __launch_bounds__(CAP ? 256 : 512, CAP == 1 ? 8 : (CAP == 2 ? 6 
       node_update<S, COLL, FORC>(f, a, n, rho, ux, uy, y * g.nseg + (x >> 5));
 #pragma unroll
       for (int k = 0; k < 9; ++k) Store<S>::str(fout + k * g.plane, ni, f[k]);
+      // density of every node of a flagged segment: the segments around a
+      // moving obstacle are flagged a step before their nodes can enter
+      // class 4, whose bounce-back then reads it
+      if (seg && a.rho_dyn_out) static_cast<T*>(a.rho_dyn_out)[ni] = rho;
       node_outputs<T>(a, n, r, rho, ux, uy, red);
     }
   }

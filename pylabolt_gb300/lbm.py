@@ -54,6 +54,23 @@ class FluidLBM:
         self.h = h
         if case.body_force_field is not None:
             self.set_body_force(case.body_force_field)
+        if case.moving:
+            arr = (capi.LbmMovingObstacle * len(case.moving))()
+            for a, o in zip(arr, case.moving):
+                a.center[:] = [float(o.center[0]), float(o.center[1])]
+                a.radius = float(o.radius)
+                a.velocity[:] = [float(o.linear_velocity[0]), float(o.linear_velocity[1])]
+                a.omega = float(o.angular_velocity)
+                a.angle = 0.0
+                a.mass = float(o.mass)
+                a.inertia = float(o.moment_of_inertia)
+                a.density = float(o.density)
+                a.id = o.id
+                a.calculated = int(o.calculated)
+                a.rotation = int(o.rotation_allowed)
+                a.translation = int(o.translation_allowed)
+            g = (ctypes.c_double * 2)(*[float(v) for v in case.gravity])
+            check(self.lib.lbm_set_moving_obstacles(self.h, arr, len(case.moving), g))
 
     # -- life cycle
     def close(self):
@@ -149,7 +166,34 @@ class FluidLBM:
         out = np.zeros((len(obs) + len(walls), 3))
         if len(out):
             check(self.lib.lbm_forces(self.h, ptr(out)))
-        return {"obstacles": out[:len(obs)], "walls": out[len(obs):, :2]}
+        res = {"obstacles": out[:len(obs)], "walls": out[len(obs):, :2]}
+        if self.case.moving:   # moving obstacles: the device's own momentum exchange
+            full = np.zeros((len(self.case.obstacles), 3))
+            static = [o for o in self.case.obstacles if o not in self.case.moving]
+            for o, v in zip(static, res["obstacles"]):
+                full[o.id] = v
+            for st in self.moving_obstacles():
+                full[st["id"]] = [st["force"][0], st["force"][1], st["torque"]]
+            res["obstacles"] = full
+        return res
+
+    def moving_obstacles(self):
+        """State of the moving obstacles: list of dicts (id, center, velocity,
+        omega, angle, force, torque) in the case's moving-obstacle order."""
+        n = len(self.case.moving)
+        if n == 0:
+            return []
+        arr = (capi.LbmMovingObstacle * n)()
+        check(self.lib.lbm_get_moving_obstacles(self.h, arr))
+        return [{"id": a.id, "center": np.array(a.center[:]), "velocity": np.array(a.velocity[:]),
+                 "omega": a.omega, "angle": a.angle, "force": np.array(a.force[:]),
+                 "torque": a.torque} for a in arr]
+
+    def node_flags(self):
+        """[Nx, Ny] uint8: 0 fluid, 1 static solid, 2 + i solid of moving obstacle i."""
+        out = np.empty(self.case.nx * self.case.ny, dtype=np.uint8)
+        check(self.lib.lbm_get_node_flags(self.h, ptr(out)))
+        return out.reshape(self.case.nx, self.case.ny)
 
     @property
     def force_names(self):

@@ -128,10 +128,11 @@ class Geometry:
 
 
 def force_links(case, geometry=None):
-    """Momentum-exchange links of every obstacle (groups 0..nobs-1, in
-    obstacle order) and every wall boundary element (the following groups, in
-    element order).  Returns (links [FORCE_LINK_DTYPE], obstacle names, wall
-    element names)."""
+    """Momentum-exchange links of every static obstacle (groups 0..nobs-1, in
+    obstacle order; moving obstacles are summed on the device by the step
+    itself) and every wall boundary element (the following groups, in element
+    order).  Returns (links [FORCE_LINK_DTYPE], obstacle names, wall element
+    names)."""
     geo = geometry or Geometry(case)
     nx, ny = case.nx, case.ny
     recs = []
@@ -139,7 +140,8 @@ def force_links(case, geometry=None):
     X, Y = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
     fb = geo.fluid_boundary[1:-1, 1:-1]
     sid = geo.solid_id[1:-1, 1:-1]
-    for g, obs in enumerate(case.obstacles):
+    static = [o for o in case.obstacles if o not in case.moving]
+    for g, obs in enumerate(static):
         ref = obs.center              # the reference's ref_point (obstacle.py:450)
         rx = _min_image(X - ref[0], nx, geo.x_periodic)
         ry = _min_image(Y - ref[1], ny, geo.y_periodic)
@@ -164,10 +166,10 @@ def force_links(case, geometry=None):
         for ko, ki in zip(el.out_list, el.inv_list):
             r = np.zeros(nodes.size, dtype=FORCE_LINK_DTYPE)
             r["node"] = nodes
-            r["group"] = len(case.obstacles) + j
+            r["group"] = len(static) + j
             r["k_out"] = ko
             r["k_in"] = ki
             recs.append(r)
     links = np.concatenate(recs) if recs else np.zeros(0, dtype=FORCE_LINK_DTYPE)
-    return links, [o.name for o in case.obstacles], [el.name for el in walls]
+    return links, [o.name for o in static], [el.name for el in walls]
 

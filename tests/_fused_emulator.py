@@ -87,10 +87,14 @@ class FusedEmulator:
             fin[s, k] = val
         return fin
 
+    def _active(self):
+        """Nodes updated this step (fluid nodes)."""
+        return self.fluid
+
     def step(self):
         c = self.case
         fin = self._incoming()
-        idx = self.fluid
+        idx = self._active()
         f = fin[idx]
         rho = np.zeros(idx.size)
         for k in range(9):
@@ -126,10 +130,14 @@ class FusedEmulator:
         self.rho[idx] = rho
         self.u[idx, 0] = ux
         self.u[idx, 1] = uy
+        self._after_collision(idx, rho)
         self.side[:, 0] = self.rho[self.spec]
         self.side[:, 1] = self.u[self.spec, 0]
         self.side[:, 2] = self.u[self.spec, 1]
         self.nopull = False
+
+    def _after_collision(self, idx, rho):
+        pass
 
     def padded(self, arr):
         """Inner x-major node array -> reference padded layout."""

@@ -1,0 +1,99 @@
+"""Moving obstacles on the GPU against the CPU restatement of the same step
+(tests/_moving_emulator.py), FP64 bit for bit: prescribed translation and
+rotation, force-driven motion; plus the resting-obstacle identity with the
+static path, FP32 against FP64, and the bounded failure when an obstacle
+would leave its allowed region."""
+import numpy as np
+import pytest
+
+from pylabolt_gb300 import capi
+from pylabolt_gb300.config import Case
+from pylabolt_gb300.lbm import FluidLBM
+from _moving_emulator import MovingEmulator
+from test_moving_cpu import disk_case
+
+pytestmark = pytest.mark.gpu
+
+FORCE_RTOL = 1e-12
+
+
+def _gpu(case, steps, storage="fp64"):
+    with FluidLBM(case, storage=storage) as s:
+        s.initialize()
+        s.step(steps, moments=True)
+        rho, u = s.moments()
+        return rho, u, s.moving_obstacles(), s.node_flags()
+
+
+def _emu(case, steps):
+    e = MovingEmulator(case)
+    e.initialize()
+    for _ in range(steps):
+        e.step()
+    return e
+
+
+@pytest.mark.parametrize("kw", [
+    {"v": (0.05, 0.02), "om": 0.01},                       # prescribed translation + rotation
+    {"v": (0.0, 0.0), "om": 0.0, "kind": "calculated", "density": 1.5},   # force-driven
+])
+def test_moving_disk_fp64_matches_restatement(kw):
+    case = Case(disk_case(True, **kw))
+    steps = 120
+    rho, u, obs, flags = _gpu(case, steps)
+    e = _emu(case, steps)
+    nx, ny = case.nx, case.ny
+    o, eo = obs[0], e.obs[0]
+    assert o["center"][0] == eo["cx"] and o["center"][1] == eo["cy"]
+    assert o["velocity"][0] == eo["vx"] and o["velocity"][1] == eo["vy"]
+    assert o["omega"] == eo["om"] and o["angle"] == eo["angle"]
+    assert o["force"][0] == eo["fx"] and o["force"][1] == eo["fy"] and o["torque"] == eo["tq"]
+    assert np.array_equal(flags.ravel() >= 2, e.dsolid > 0)
+    assert np.array_equal(rho.ravel(), e.rho)
+    assert np.array_equal(u.reshape(-1, 2), e.u)
+
+
+def test_resting_moving_disk_equals_static_path():
+    st_case = Case(disk_case(False))
+    mv_case = Case(disk_case(True))
+    with FluidLBM(st_case, storage="fp64") as s:
+        s.initialize()
+        f0 = s.forces()["obstacles"][0]
+        s.step(200, moments=True)
+        rho_s, u_s = s.moments()
+        f_s = s.forces()["obstacles"][0]
+    with FluidLBM(mv_case, storage="fp64") as m:
+        m.initialize()
+        g0 = m.forces()["obstacles"][0]
+        m.step(200, moments=True)
+        rho_m, u_m = m.moments()
+        f_m = m.forces()["obstacles"][0]
+    fl = ~st_case.solid
+    fl &= ~mv_case.solid
+    X, Y = np.meshgrid(np.arange(st_case.nx), np.arange(st_case.ny), indexing="ij")
+    disk = (X - 14.0) ** 2 + (Y - 16.0) ** 2 <= 16.0
+    fl &= ~disk
+    assert np.array_equal(rho_s[fl], rho_m[fl]) and np.array_equal(u_s[fl], u_m[fl])
+    np.testing.assert_allclose(g0, f0, rtol=FORCE_RTOL, atol=1e-15)
+    np.testing.assert_allclose(f_m, f_s, rtol=FORCE_RTOL, atol=1e-15)
+
+
+def test_moving_disk_fp32_close_to_fp64():
+    case = Case(disk_case(True, v=(0.05, 0.02), om=0.01))
+    _, u64, o64, _ = _gpu(case, 300)
+    _, u32, o32, _ = _gpu(case, 300, storage="fp32_shifted")
+    assert np.linalg.norm(u32 - u64) / np.linalg.norm(u64) <= 1e-5
+    assert np.allclose(o32[0]["center"], o64[0]["center"], rtol=0, atol=1e-12)
+
+
+def test_obstacle_leaving_its_region_fails_cleanly():
+    case = Case(disk_case(True, v=(-0.5, 0.0), center=(9, 16)))
+    with FluidLBM(case, storage="fp32_shifted") as s:
+        s.initialize()
+        with pytest.raises(capi.LbmError, match="within two nodes of the domain edge"):
+            s.step(40)
+            s.synchronize()
+        # it stays where it last was allowed, and the handle keeps working
+        c = s.moving_obstacles()[0]["center"][0]
+        assert 7.0 <= c < 9.0
+        s.step(1)

@@ -55,16 +55,21 @@ def _min_image(r, n, periodic):
 
 
 class Geometry:
-    """Padded geometry fields of a Case ([nx+2, ny+2] arrays, x-major)."""
+    """Padded geometry fields of a Case ([nx+2, ny+2] arrays, x-major).
+    `solid`, `solid_id` [nx, ny] and `centers` {obstacle id: (x, y)} replace
+    the case's set-up geometry (moving obstacles: the device's node flags and
+    positions at the time of output)."""
 
-    def __init__(self, case):
+    def __init__(self, case, solid=None, solid_id=None, centers=None):
         nx, ny = case.nx, case.ny
         self.nx, self.ny = nx, ny
         self.x_periodic, self.y_periodic = case.x_periodic, case.y_periodic
-        solid = np.zeros((nx + 2, ny + 2), dtype=bool)
-        solid_id = np.full((nx + 2, ny + 2), -1, dtype=np.int64)
-        solid[1:-1, 1:-1] = case.solid
-        solid_id[1:-1, 1:-1] = case.solid_id
+        centers = centers or {}
+        solid_a = np.zeros((nx + 2, ny + 2), dtype=bool)
+        solid_id_a = np.full((nx + 2, ny + 2), -1, dtype=np.int64)
+        solid_a[1:-1, 1:-1] = case.solid if solid is None else solid
+        solid_id_a[1:-1, 1:-1] = case.solid_id if solid_id is None else solid_id
+        solid, solid_id = solid_a, solid_id_a
         _fill_ghosts(solid, self.x_periodic, self.y_periodic)
         _fill_ghosts(solid_id, self.x_periodic, self.y_periodic)
         inner = np.zeros_like(solid)
@@ -90,8 +95,9 @@ class Geometry:
                            np.arange(-1, ny + 1, dtype=np.float64), indexing="ij")
         for obs in case.obstacles:
             sel = inner & (solid_id == obs.id) & (solid_boundary | fluid_boundary)
-            rx = _min_image(X - obs.center[0], nx, self.x_periodic)
-            ry = _min_image(Y - obs.center[1], ny, self.y_periodic)
+            cx, cy = centers.get(obs.id, obs.center)
+            rx = _min_image(X - cx, nx, self.x_periodic)
+            ry = _min_image(Y - cy, ny, self.y_periodic)
             mag = np.sqrt(rx * rx + ry * ry)
             with np.errstate(invalid="ignore", divide="ignore"):
                 normals[..., 0] = np.where(sel, rx / mag, normals[..., 0])

@@ -143,12 +143,24 @@ class Output:
         return (c.write_boundary_data and c.boundary_write_interval is not None
                 and t % c.boundary_write_interval == 0)
 
-    def write_obstacles(self, t, force_torque):
-        """force_torque [nobs, 3] (zeros when compute_force_torque is off)."""
+    def set_geometry(self, geometry):
+        """New geometry fields for the following field files (moving obstacles)."""
+        for name in ("solid", "solid_id", "solid_boundary", "fluid_boundary", "surface_normals"):
+            self.static[name] = geometry.inner(name).astype(self.static[name].dtype)
+
+    def write_obstacles(self, t, force_torque, states=None):
+        """force_torque [nobs, 3] (zeros when compute_force_torque is off);
+        states {obstacle id: dict(center, angle, velocity, omega)} of moving
+        obstacles (the others report their set-up values)."""
         d = self.dtype
+        states = states or {}
         for o, ft in zip(self.case.obstacles, force_torque):
-            vals = [o.center[0], o.center[1], 0.0, o.linear_velocity[0],
-                    o.linear_velocity[1], o.angular_velocity, ft[0], ft[1], ft[2]]
+            st = states.get(o.id)
+            if st is None:
+                pos, alpha, vel, om = o.center, 0.0, o.linear_velocity, o.angular_velocity
+            else:
+                pos, alpha, vel, om = st["center"], st["angle"], st["velocity"], st["omega"]
+            vals = [pos[0], pos[1], alpha, vel[0], vel[1], om, ft[0], ft[1], ft[2]]
             line = f"{t:<24}" + "".join(f"{float(d(v)):<30.16e}" for v in vals) + "\n"
             with open(os.path.join(self.history_dir, o.name + ".dat"), "a") as f:
                 f.write(line)

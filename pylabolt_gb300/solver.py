@@ -90,6 +90,24 @@ class Solver:
         if want_walls:
             self.wall_forces = f["walls"]
 
+    def _moving_states(self):
+        if not self.case.moving:
+            return {}
+        return {st["id"]: st for st in self.lbm.moving_obstacles()}
+
+    def _moving_geometry(self):
+        """Geometry fields of the current step: static solids from the case,
+        moving ones from the device's node flags, normals about their current
+        centres."""
+        c = self.case
+        flags = self.lbm.node_flags()
+        solid = flags > 0
+        solid_id = np.where(flags == 1, c.solid_id, -1)
+        for j, o in enumerate(c.moving):
+            solid_id[flags == 2 + j] = o.id
+        centers = {st["id"]: st["center"] for st in self.lbm.moving_obstacles()}
+        return Geometry(c, solid=solid, solid_id=solid_id, centers=centers)
+
     def run(self):
         c = self.case
         self.log("\n" + "-" * 80)
@@ -103,9 +121,11 @@ class Solver:
         self._update_forces(self.out.obstacle_due(0), self.out.boundary_due(0))
         if self.out.save_due(c.start_time):
             rho, u = self.lbm.moments()
+            if c.moving:
+                self.out.set_geometry(self._moving_geometry())
             self.out.write_fields(c.start_time, rho, u)
         if self.out.obstacle_due(0):
-            self.out.write_obstacles(0, self.obstacle_forces)
+            self.out.write_obstacles(0, self.obstacle_forces, self._moving_states())
         if self.out.boundary_due(0):
             self.out.write_walls(0, self.wall_forces)
         t0 = time.perf_counter()
@@ -122,9 +142,11 @@ class Solver:
                 self.log(log_line(t, res_density=r[:1], res_velocity=r[1:]))
             if save:
                 rho, u = self.lbm.moments()
+                if c.moving:
+                    self.out.set_geometry(self._moving_geometry())
                 self.out.write_fields(t, rho, u)
             if obs:
-                self.out.write_obstacles(t, self.obstacle_forces)
+                self.out.write_obstacles(t, self.obstacle_forces, self._moving_states())
             if bnd:
                 self.out.write_walls(t, self.wall_forces)
         self.lbm.synchronize()

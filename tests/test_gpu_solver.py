@@ -91,3 +91,30 @@ def test_command_line_cavity(tmp_path):
         rho, u = sim.moments()
     assert np.array_equal(z["density"], rho.reshape(-1))
     assert np.array_equal(z["velocity"], u.reshape(-1, 2))
+
+
+def test_solver_moving_obstacle_outputs(tmp_path, capsys):
+    """A translating disk: its history rows follow the device state and each
+    field file carries the geometry of its own step."""
+    from test_moving_cpu import disk_case
+    c = disk_case(True, v=(0.05, 0.0))
+    c["control_dict"].update({"end_time": 40, "std_out_interval": 20, "save_interval": 20})
+    c["obstacle_dict"]["options"]["write_obstacle_data"] = {"interval": 20}
+    s = solver.Solver(c, root=str(tmp_path), storage="fp64")
+    try:
+        s.run()
+    finally:
+        s.close()
+    rows = [l.split() for l in open(tmp_path / "output" / "histories" / "disk.dat")
+            if not l.startswith("#")]
+    assert [int(r[0]) for r in rows] == [0, 20, 40]
+    xs = [float(r[1]) for r in rows]
+    np.testing.assert_allclose(xs, [14.0, 15.0, 16.0], atol=1e-12)
+    z0 = np.load(tmp_path / "output" / "fields" / "t_0.npz")
+    z40 = np.load(tmp_path / "output" / "fields" / "t_40.npz")
+    ny = 32
+    X, Y = np.divmod(np.arange(40 * ny), ny)
+    for z, cx in ((z0, 14.0), (z40, 16.0)):
+        assert np.array_equal(z["solid"], (X - cx) ** 2 + (Y - 16.0) ** 2 <= 16.0)
+        assert np.all(z["solid_id"][z["solid"]] == 0)
+        assert np.all(z["fluid_boundary"] <= ~z["solid"])

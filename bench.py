@@ -345,6 +345,23 @@ def side_measurements(args, case_d, sim32, nodes, peak):
             "roofline_frac": B_LU["fp32_shifted"] * nodes / (ms / args.steps / 1e3) / 1e9 / peak,
             "kernel": list(s.kernel_variant)}
     out["mrt_fp32_shifted"] = res["mrt_fp32_shifted"]
+    # the same cylinder translating at 0.02 nodes per step (moving-obstacle
+    # kernels around the fused step)
+    mv = dict(case_d)
+    mv["obstacle_dict"] = {k: dict(v) for k, v in case_d["obstacle_dict"].items()}
+    mv["obstacle_dict"]["options"] = {"compute_force_torque": True, "move_obstacles": True}
+    mv["obstacle_dict"]["cylinder"].update({"static": False, "solid_motion_dict": {
+        "type": "fixed_velocity", "degree_of_freedom": "translation",
+        "linear_velocity": [0.02, 0.0], "angular_velocity": 0.0}})
+    with FluidLBM(Case(mv), storage="fp32_shifted") as s:
+        s.initialize()
+        s.step(3)
+        s.synchronize()
+        ms = s.time_steps(args.steps)
+        out["moving_cylinder_fp32_shifted"] = {
+            "mlups": nodes * args.steps / (ms / 1e3) / 1e6,
+            "launches_per_step": 5, "kernel": list(s.kernel_variant),
+            "center_after": float(s.moving_obstacles()[0]["center"][0])}
     out["adjoint"] = adjoint_measurement()
     out["batch"] = batch_measurement()
     out["fp64"] = res["fp64"]

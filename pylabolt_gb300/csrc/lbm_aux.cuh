@@ -201,7 +201,8 @@ struct Kernels {
     return cudaGetLastError();
   }
   static cudaError_t mov_force(const MovArgs& a, cudaStream_t s) {
-    mov_force_kernel<S><<<1, 32, 0, s>>>(a);
+    mov_force_kernel<S><<<kMovForceBlocks, kMovForceThreads, 0, s>>>(a);
+    mov_force_finish_kernel<S><<<1, kMovForceBlocks, 0, s>>>(a);
     return cudaGetLastError();
   }
   static KernelSet make() {

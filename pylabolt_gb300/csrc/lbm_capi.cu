@@ -120,6 +120,7 @@ struct LbmHandle {
     uint8_t* fresh = nullptr;
     void* us = nullptr;
     void* rho_dyn[2] = {nullptr, nullptr};   // swapped with the population buffers
+    double* part = nullptr;          // momentum-exchange partial sums
     uint8_t* cls_static = nullptr;   // classes / segment flags without moving obstacles
     uint8_t* seg_static = nullptr;
     double gx = 0.0, gy = 0.0;
@@ -490,6 +491,7 @@ struct LbmHandle {
     a.mx = mom[1];
     a.my = mom[2];
     a.nopull = nopull_state;
+    a.part = mov.part;
     a.err = err_dev;
     return a;
   }
@@ -1379,6 +1381,7 @@ int lbm_set_moving_obstacles(LbmHandle* h, const LbmMovingObstacle* obs, int n,
       (rc = h->alloc(reinterpret_cast<void**>(&M.fresh), plane)) ||
       (rc = h->alloc(&M.us, 2 * plane * cb)) || (rc = h->alloc(&M.rho_dyn[0], plane * cb)) ||
       (rc = h->alloc(&M.rho_dyn[1], plane * cb)) ||
+      (rc = h->alloc(reinterpret_cast<void**>(&M.part), (size_t)n * lbm::kMovForceBlocks * 3 * sizeof(double))) ||
       (rc = h->alloc(reinterpret_cast<void**>(&M.cls_static), plane)) ||
       (rc = h->alloc(reinterpret_cast<void**>(&M.seg_static), nseg)))
     return rc;

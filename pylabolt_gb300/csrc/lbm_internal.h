@@ -144,6 +144,7 @@ struct MovArgs {
   void* pop;                // current state (storage type)
   void* mr; void* mx; void* my;   // moments (solid nodes get rho_s, u_s)
   int nopull;               // force: the state holds incoming populations
+  double* part;             // force: per-block partial sums [n][blocks][3]
   int* err;                 // device-visible error word
 };
 
@@ -166,6 +167,8 @@ constexpr int kErrMovBounds = 2;     // a moving obstacle would leave the allowe
 constexpr int kErrMovSpeed = 3;      // a moving obstacle would move a node or more in a step
 constexpr int kErrMovNeighbour = 4;  // a moving obstacle reached a static solid or boundary node
 constexpr int kMovMaxObstacles = 32;
+constexpr int kMovForceThreads = 256;   // momentum-exchange launch of a moving obstacle
+constexpr int kMovForceBlocks = 64;
 
 // Kernels of one storage precision.
 struct KernelSet {

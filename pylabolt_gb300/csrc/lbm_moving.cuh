@@ -19,9 +19,11 @@
 //   mov_force_kernel     momentum exchange on the obstacle
 //                        (compute_force_torque_single_phase,
 //                        force_torque_kernels.py:11-90) with the bounce-back
-//                        the next step applies, summed in a fixed order (one
-//                        warp: lane l takes box nodes l, l+32, ..., then a
-//                        shuffle tree), and the fresh flags cleared.
+//                        the next step applies, summed in a fixed order
+//                        (thread g of kMovForceBlocks x kMovForceThreads
+//                        takes box nodes g, g + 16384, ..., a shared-memory
+//                        tree per block, then mov_force_finish's tree over
+//                        the blocks), and the fresh flags cleared.
 // Class-4 nodes pull their links at run time in the step kernel
 // (dynamic_links): a moving-solid source gives
 // pop[x,kbar] - 2 w_kbar rho(x) inv_cs_2 (c_kbar . u_solid)
@@ -197,14 +199,15 @@ __global__ void mov_classify_kernel(const MovArgs a) {
   }
 }
 
+
 template <class S>
-__global__ void mov_force_kernel(const MovArgs a) {
+__global__ void __launch_bounds__(kMovForceThreads) mov_force_kernel(const MovArgs a) {
   using T = typename Store<S>::T;
   constexpr bool SH = Store<S>::shifted;
-  MovObs* ob = a.obs + a.j;
-  if (ob->bx1 < ob->bx0) return;
+  const MovObs* ob = a.obs + a.j;
   const int x0 = ob->bx0 - 1, y0 = ob->by0 - 1;
-  const int W = ob->bx1 - ob->bx0 + 3, H = ob->by1 - ob->by0 + 3;
+  // an empty box (bx1 < bx0) contributes nothing
+  const int W = ob->bx1 < ob->bx0 ? 0 : ob->bx1 - ob->bx0 + 3, H = ob->by1 - ob->by0 + 3;
   const double cx = ob->cx, cy = ob->cy;
   const Geom& g = a.g;
   const Params& p = a.p;
@@ -213,8 +216,9 @@ __global__ void mov_force_kernel(const MovArgs a) {
   const T* rd = static_cast<const T*>(a.rho_dyn);
   const uint8_t me = (uint8_t)(a.j + 1);
   double sx = 0.0, sy = 0.0, st = 0.0;
-  const int lane = threadIdx.x;
-  for (int i = lane; i < W * H; i += 32) {
+  const int tid = threadIdx.x;
+  for (int i = blockIdx.x * kMovForceThreads + tid; i < W * H;
+       i += kMovForceThreads * kMovForceBlocks) {
     const int x = x0 + i / H, y = y0 + i % H;
     const long long n = g.node(x, y);
     if (a.fresh[n]) a.fresh[n] = 0;
@@ -255,16 +259,39 @@ __global__ void mov_force_kernel(const MovArgs a) {
       st += rx * vy - ry * vx;
     }
   }
+  __shared__ double red[3][kMovForceThreads];
+  red[0][tid] = sx;
+  red[1][tid] = sy;
+  red[2][tid] = st;
+  __syncthreads();
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    sx += __shfl_down_sync(0xffffffffu, sx, o);
-    sy += __shfl_down_sync(0xffffffffu, sy, o);
-    st += __shfl_down_sync(0xffffffffu, st, o);
+  for (int h = kMovForceThreads / 2; h > 0; h >>= 1) {
+    if (tid < h)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) red[c][tid] += red[c][tid + h];
+    __syncthreads();
   }
-  if (lane == 0) {
-    ob->fx = sx;
-    ob->fy = sy;
-    ob->tq = st;
+  if (tid < 3) a.part[(a.j * kMovForceBlocks + blockIdx.x) * 3 + tid] = red[tid][0];
+}
+
+template <class S>
+__global__ void mov_force_finish_kernel(const MovArgs a) {
+  __shared__ double red[3][kMovForceBlocks];
+  const int t = threadIdx.x;
+  for (int c = 0; c < 3; ++c) red[c][t] = a.part[(a.j * kMovForceBlocks + t) * 3 + c];
+  __syncthreads();
+#pragma unroll
+  for (int h = kMovForceBlocks / 2; h > 0; h >>= 1) {
+    if (t < h)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) red[c][t] += red[c][t + h];
+    __syncthreads();
+  }
+  if (t == 0) {
+    MovObs* ob = a.obs + a.j;
+    ob->fx = red[0][0];
+    ob->fy = red[1][0];
+    ob->tq = red[2][0];
   }
 }
 

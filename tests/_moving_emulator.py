@@ -16,6 +16,9 @@ from pylabolt_gb300.lattice import CX, CY, W, INV
 from _fused_emulator import FusedEmulator
 
 
+THREADS, BLOCKS = 256, 64   # the device's force launch (kMovForceThreads, kMovForceBlocks)
+
+
 class MovingEmulator(FusedEmulator):
     def __init__(self, case):
         super().__init__(case)
@@ -161,7 +164,9 @@ class MovingEmulator(FusedEmulator):
         super().step()
         self._forces(nopull=False)
 
-    # -- momentum exchange on each obstacle, the device's summation order
+    # -- momentum exchange on each obstacle, the device's summation order:
+    # thread g sums box nodes g, g + BLOCKS*THREADS, ..., a halving tree in
+    # each block, then a halving tree over the blocks
     def _forces(self, nopull):
         c = self.case
         ny, i2 = c.ny, c.inv_cs_2
@@ -169,7 +174,7 @@ class MovingEmulator(FusedEmulator):
             x0, x1, y0, y1 = o["box"]
             x0, y0 = x0 - 1, y0 - 1
             Wd, H = x1 - x0 + 2, y1 - y0 + 2
-            lanes = np.zeros((32, 3))
+            lanes = np.zeros((BLOCKS * THREADS, 3))
             for i in range(Wd * H):
                 x, y = x0 + i // H, y0 + i % H
                 n = self._node(x, y)
@@ -183,7 +188,7 @@ class MovingEmulator(FusedEmulator):
                 if first != j + 1:
                     continue
                 rx, ry = float(x) - o["cx"], float(y) - o["cy"]
-                acc = lanes[i % 32]
+                acc = lanes[i % (BLOCKS * THREADS)]
                 for k in range(1, 9):
                     q = self._node(x + CX[k], y + CY[k])
                     if self.dsolid[q] == 0:
@@ -200,6 +205,14 @@ class MovingEmulator(FusedEmulator):
                     acc[0] += vx
                     acc[1] += vy
                     acc[2] += rx * vy - ry * vx
-            for off in (16, 8, 4, 2, 1):
+            blk = lanes.reshape(BLOCKS, THREADS, 3)
+            off = THREADS // 2
+            while off:
+                blk[:, :off] = blk[:, :off] + blk[:, off:2 * off]
+                off //= 2
+            lanes = blk[:, 0].copy()
+            off = BLOCKS // 2
+            while off:
                 lanes[:off] = lanes[:off] + lanes[off:2 * off]
+                off //= 2
             o["fx"], o["fy"], o["tq"] = lanes[0]

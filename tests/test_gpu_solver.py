@@ -114,7 +114,10 @@ def test_solver_moving_obstacle_outputs(tmp_path, capsys):
     z40 = np.load(tmp_path / "output" / "fields" / "t_40.npz")
     ny = 32
     X, Y = np.divmod(np.arange(40 * ny), ny)
-    for z, cx in ((z0, 14.0), (z40, 16.0)):
+    cx40 = 14.0
+    for _ in range(40):     # the device's motion update, in the same FP64 order
+        cx40 = cx40 + (0.05 + 0.5 * (0.0 / 1.0 + 0.0))
+    for z, cx in ((z0, 14.0), (z40, cx40)):
         assert np.array_equal(z["solid"], (X - cx) ** 2 + (Y - 16.0) ** 2 <= 16.0)
         assert np.all(z["solid_id"][z["solid"]] == 0)
         assert np.all(z["fluid_boundary"] <= ~z["solid"])

@@ -59,3 +59,35 @@ def test_translating_disk_geometry():
     # classes: solid 2, its fluid neighbours 4
     assert np.all(mv.cls[inside] == 2)
     assert np.all(np.isfinite(mv.fstar[~inside]))
+
+
+def test_motion_dict_validation_messages():
+    """solid_motion_dict errors as obstacle.py:478-538 words them."""
+    c = disk_case(True)
+    c["obstacle_dict"]["disk"]["solid_motion_dict"]["type"] = "spinning"
+    with pytest.raises(ValueError, match="Unsupported motion type: spinning in obstacle: disk"):
+        Case(c)
+    c = disk_case(True)
+    c["obstacle_dict"]["disk"]["solid_motion_dict"]["degree_of_freedom"] = "all"
+    with pytest.raises(ValueError, match="Unsupported degree of freedom: all in obstacle: disk"):
+        Case(c)
+    c = disk_case(True)
+    del c["obstacle_dict"]["disk"]["solid_motion_dict"]["linear_velocity"]
+    with pytest.raises(ValueError, match="linear_velocity missing in solid_motion_dict: disk"):
+        Case(c)
+    c = disk_case(True)
+    c["obstacle_dict"]["options"]["move_obstacles"] = "yes"
+    with pytest.raises(ValueError, match="move_obstacles must be bool"):
+        Case(c)
+
+
+def test_moving_obstacle_parameters():
+    case = Case(disk_case(True, kind="calculated", dof="rotation", density=2.0))
+    o = case.moving[0]
+    assert o.calculated and o.rotation_allowed and not o.translation_allowed
+    assert o.mass == pytest.approx(np.pi * 16.0 * 2.0)
+    assert o.moment_of_inertia == pytest.approx(o.mass * 16.0 / 2)
+    # a moving obstacle is not part of the static solid: the device places it
+    assert not case.solid.any()
+    static = Case(disk_case(False))
+    assert static.solid.sum() > 0 and not static.moving

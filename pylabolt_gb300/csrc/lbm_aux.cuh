@@ -117,6 +117,11 @@ struct Kernels {
       }
     }
     if (v.kind != 0) return cudaErrorInvalidValue;
+    if (a.rho_dyn_out) {   // moving obstacles: the uncapped scalar kernel only
+      if (v.stages != 0) return cudaErrorInvalidValue;
+      step_kernel<S, COLL, FORC, 0, true><<<grid, v.block, 0, s>>>(a);
+      return cudaGetLastError();
+    }
     if (v.stages == 1 || v.stages == 2) {
       if (v.block > 256) return cudaErrorInvalidValue;
       if (v.stages == 1)

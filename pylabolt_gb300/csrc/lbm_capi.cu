@@ -394,8 +394,8 @@ struct LbmHandle {
         for (int i = 0; i < ks->nvariants; ++i)
           if (ks->variants[i].kind == kind && ks->variants[i].vec == vec &&
               ks->variants[i].block == blk && ks->variants[i].stages == st) {
-            if (mov.n && kind != 0)
-              return fail(LBM_ERR_ARG, "LBM_VARIANT: moving obstacles need the scalar kernel (kind 0)");
+            if (mov.n && (kind != 0 || st != 0))
+              return fail(LBM_ERR_ARG, "LBM_VARIANT: moving obstacles need the uncapped scalar kernel (kind 0, stages 0)");
             variant = ks->variants[i];
             return LBM_OK;
           }
@@ -405,7 +405,7 @@ struct LbmHandle {
     variant = ks->variants[0];
     if (mov.n)
       for (int i = 0; i < ks->nvariants; ++i)
-        if (ks->variants[i].kind == 0) {
+        if (ks->variants[i].kind == 0 && ks->variants[i].stages == 0) {
           variant = ks->variants[i];
           break;
         }
@@ -419,7 +419,7 @@ struct LbmHandle {
     int rc = LBM_OK;
     for (int i = 0; i < ks->nvariants && rc == LBM_OK; ++i) {
       const lbm::Variant v = ks->variants[i];
-      if (mov.n && v.kind != 0) {   // class-4 links are served by the scalar kernel only
+      if (mov.n && (v.kind != 0 || v.stages != 0)) {   // class-4 links: the uncapped scalar kernel only
         tune_ms[i] = 1e30;
         continue;
       }
@@ -1395,7 +1395,7 @@ int lbm_set_moving_obstacles(LbmHandle* h, const LbmMovingObstacle* obs, int n,
   // the no-pull first step included, uses a scalar shape (re-picked among
   // the scalar candidates by the autotuner)
   for (int i = 0; i < h->ks->nvariants; ++i)
-    if (h->ks->variants[i].kind == 0) {
+    if (h->ks->variants[i].kind == 0 && h->ks->variants[i].stages == 0) {
       h->variant = h->ks->variants[i];
       break;
     }

@@ -656,60 +656,65 @@ __device__ __forceinline__ void block_residual(const StepArgs& a, T red[7]) {
 }
 
 // ---------------------------------------------------------------------------
+// One node of the scalar kernel.  MOV: the case has moving obstacles
+// (class-4 nodes, the density kept for their bounce-back).
+template <class S, int COLL, int FORC, bool MOV>
+__device__ __forceinline__ void step_node(const StepArgs& a, int x, int y,
+                                          typename Store<S>::T red[7]) {
+  using T = typename Store<S>::T;
+  const Geom& g = a.g;
+  // 32-bit node index (plane < 2^31 is checked at create) with per-plane
+  // base pointers (uniform): one wide multiply-add per access instead of
+  // 64-bit index arithmetic
+  const int ni = (y + 1) * g.pitch + x;
+  const long long n = ni;
+  const S* __restrict__ fin = static_cast<const S*>(a.fin);
+  S* __restrict__ fout = static_cast<S*>(a.fout);
+  int cls = 0;
+  const bool seg = g.segflag[y * g.nseg + (x >> 5)] != 0;
+  if (seg) cls = g.cls[ni];
+  if (cls == 2) return;
+  T f[9];
+  int r = -1;
+  if (cls == 1) r = g.recmap[ni];
+  if (a.flags & F_NOPULL) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) f[k] = Store<S>::ldr(fin + k * g.plane, ni);
+  } else if (cls == 0) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+      f[k] = Store<S>::ldr(fin + k * g.plane, ni - CYk(k) * g.pitch - CXk(k));
+  } else if (MOV && cls == 4) {
+    f[0] = Store<S>::ldr(fin, ni);
+    dynamic_links<S>(f, a, fin, ni);
+  } else {
+    f[0] = Store<S>::ldr(fin, n);
+    special_links<S>(f, a, fin, n, r);
+  }
+  T rho, ux, uy;
+  node_update<S, COLL, FORC>(f, a, n, rho, ux, uy, y * g.nseg + (x >> 5));
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Store<S>::str(fout + k * g.plane, ni, f[k]);
+  // density of every node of a flagged segment: the segments around a
+  // moving obstacle are flagged a step before their nodes can enter class 4,
+  // whose bounce-back then reads it
+  if (MOV && seg) static_cast<T*>(a.rho_dyn_out)[ni] = rho;
+  node_outputs<T>(a, n, r, rho, ux, uy, red);
+}
+
 // Scalar kernel: one node per thread.  Used for FP64 (whose cost is its FP64
 // arithmetic, not memory) and as an autotuner candidate.
 // CAP = 1 asks for 8 resident blocks of 256 threads (at most 32 registers),
-// CAP = 2 for 6 (at most 40 registers; for the MRT collision).
-template <class S, int COLL, int FORC, int CAP>
+// CAP = 2 for 6 (at most 40 registers; for the MRT collision).  MOV = true
+// (moving obstacles) is instantiated uncapped only.
+template <class S, int COLL, int FORC, int CAP, bool MOV = false>
 __global__ void __launch_bounds__(CAP ? 256 : 512, CAP == 1 ? 8 : (CAP == 2 ? 6 : 1))
     step_kernel(const StepArgs a) {
   using T = typename Store<S>::T;
-  const Geom& g = a.g;
-  const Params& p = a.p;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   T red[7] = {0, 0, 0, 0, 0, 0, 0};
-
-  if (x < g.nx) {
-    // 32-bit node index (plane < 2^31 is checked at create) with per-plane
-    // base pointers (uniform): one wide multiply-add per access instead of
-    // 64-bit index arithmetic
-    const int ni = (y + 1) * g.pitch + x;
-    const long long n = ni;
-    const S* __restrict__ fin = static_cast<const S*>(a.fin);
-    S* __restrict__ fout = static_cast<S*>(a.fout);
-    int cls = 0;
-    const bool seg = g.segflag[y * g.nseg + (x >> 5)] != 0;
-    if (seg) cls = g.cls[ni];
-    if (cls != 2) {
-      T f[9];
-      int r = -1;
-      if (cls == 1) r = g.recmap[ni];
-      if (a.flags & F_NOPULL) {
-#pragma unroll
-        for (int k = 0; k < 9; ++k) f[k] = Store<S>::ldr(fin + k * g.plane, ni);
-      } else if (cls == 0) {
-#pragma unroll
-        for (int k = 0; k < 9; ++k)
-          f[k] = Store<S>::ldr(fin + k * g.plane, ni - CYk(k) * g.pitch - CXk(k));
-      } else if (cls == 4) {
-        f[0] = Store<S>::ldr(fin, ni);
-        dynamic_links<S>(f, a, fin, ni);
-      } else {
-        f[0] = Store<S>::ldr(fin, n);
-        special_links<S>(f, a, fin, n, r);
-      }
-      T rho, ux, uy;
-      node_update<S, COLL, FORC>(f, a, n, rho, ux, uy, y * g.nseg + (x >> 5));
-#pragma unroll
-      for (int k = 0; k < 9; ++k) Store<S>::str(fout + k * g.plane, ni, f[k]);
-      // density of every node of a flagged segment: the segments around a
-      // moving obstacle are flagged a step before their nodes can enter
-      // class 4, whose bounce-back then reads it
-      if (seg && a.rho_dyn_out) static_cast<T*>(a.rho_dyn_out)[ni] = rho;
-      node_outputs<T>(a, n, r, rho, ux, uy, red);
-    }
-  }
+  if (x < a.g.nx) step_node<S, COLL, FORC, MOV>(a, x, y, red);
   if (a.flags & F_RESIDUAL) block_residual<decltype(red[0] + 0)>(a, red);
 }
 

@@ -1404,6 +1404,8 @@ int lbm_set_moving_obstacles(LbmHandle* h, const LbmMovingObstacle* obs, int n,
     cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
   }
+  // the obstacles are placed by lbm_init_fields, which must come next
+  h->initialized = false;
   return h->wait();
 }
 

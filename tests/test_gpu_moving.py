@@ -97,3 +97,29 @@ def test_obstacle_leaving_its_region_fails_cleanly():
         c = s.moving_obstacles()[0]["center"][0]
         assert 7.0 <= c < 9.0
         s.step(1)
+
+
+def test_registration_errors():
+    """Host-side checks of lbm_set_moving_obstacles (no device work is done
+    for a rejected set)."""
+    with pytest.raises(capi.LbmError, match="two nodes away from the domain edges"):
+        FluidLBM(Case(disk_case(True, center=(5, 16))))
+    c = disk_case(True, center=(14, 16))
+    c["obstacle_dict"]["wall_disk"] = {"type": "circle", "radius": 3.0, "center": [22, 16],
+                                      "density": 1.0, "static": True}
+    with pytest.raises(capi.LbmError, match="next to a boundary node or a static solid"):
+        FluidLBM(Case(c))
+
+
+def test_force_link_validation():
+    case = Case(disk_case(False))
+    with FluidLBM(case, storage="fp64") as s:
+        links = np.zeros(1, dtype=capi.FORCE_LINK_DTYPE)
+        links["node"] = 5 * case.ny + 5          # an interior bulk node: no link record
+        links["k_out"], links["k_in"] = 1, 3
+        with pytest.raises(capi.LbmError, match="not on a boundary node"):
+            capi.check(s.lib.lbm_set_force_links(s.h, capi.ptr(links), 1, 1))
+        links["node"] = 0
+        links["group"] = 3
+        with pytest.raises(capi.LbmError, match="group out of range"):
+            capi.check(s.lib.lbm_set_force_links(s.h, capi.ptr(links), 1, 1))

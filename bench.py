@@ -42,7 +42,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the FP64 / FP16 / error side measurements")
-    ap.add_argument("--only", choices=["adjoint", "batch", "error-study"],
+    ap.add_argument("--only", choices=["adjoint", "batch", "error-study", "aa"],
                     help="run one side measurement alone and print it (profiling runs)")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
     return ap.parse_args()
@@ -345,6 +345,7 @@ def side_measurements(args, case_d, sim32, nodes, peak):
             "roofline_frac": B_LU["fp32_shifted"] * nodes / (ms / args.steps / 1e3) / 1e9 / peak,
             "kernel": list(s.kernel_variant)}
     out["mrt_fp32_shifted"] = res["mrt_fp32_shifted"]
+    out.update(aa_measurement(args, case_d, peak))
     # the same cylinder translating at 0.02 nodes per step (moving-obstacle
     # kernels around the fused step)
     mv = dict(case_d)
@@ -381,6 +382,33 @@ def side_measurements(args, case_d, sim32, nodes, peak):
             "steps": err_steps,
             "u_rel_l2": float(np.linalg.norm(d) / np.linalg.norm(ref[fluid])),
             "u_max_abs_over_max": float(np.abs(d).max() / np.abs(ref[fluid]).max())}
+    return out
+
+
+def aa_measurement(args, case_d=None, peak=None):
+    """The same step on one population buffer updated in place (AA pattern):
+    throughput, roofline fraction (same bytes per node update as two
+    buffers) and device memory of both layouts."""
+    from pylabolt_gb300.config import Case
+    from pylabolt_gb300.lbm import FluidLBM
+    case = Case(case_d or workload_case(args, "fp32_shifted"))
+    peak = peak or measured_peak()[0]
+    nodes = case.nx * case.ny
+    out = {}
+    for storage in ("fp32_shifted", "fp16_shifted"):
+        rec = {}
+        for layout in ("aa", "ab"):
+            with FluidLBM(case, storage=storage, layout=layout) as s:
+                s.initialize()
+                s.step(3)
+                s.synchronize()
+                rec[f"device_gb_{layout}"] = s.device_bytes / 1e9
+                if layout == "aa":
+                    ms = s.time_steps(args.steps)
+                    rec["mlups"] = nodes * args.steps / (ms / 1e3) / 1e6
+                    rec["roofline_frac"] = B_LU[storage] * nodes / (ms / args.steps / 1e3) / 1e9 / peak
+                    rec["kernel"] = list(s.kernel_variant)
+        out[f"aa_{storage}"] = rec
     return out
 
 
@@ -531,6 +559,8 @@ def main():
             out = adjoint_measurement(args.adjoint_steps)
         elif args.only == "batch":
             out = batch_measurement()
+        elif args.only == "aa":
+            out = aa_measurement(args)
         else:
             out = error_study(args)
         print(json.dumps({"only": args.only, **out}), flush=True)

@@ -67,6 +67,16 @@ typedef struct LbmHandle LbmHandle;
 #define LBM_LAYOUT_INNER 0   /* [nx*ny], ind = x*ny + y                    */
 #define LBM_LAYOUT_PADDED 1  /* [(nx+2)*(ny+2)], ind = x*(ny+2) + y, ghosts 0 */
 
+/* population layouts (LbmConfig.layout) */
+#define LBM_POP_AB 0   /* two buffers: a step pulls from one, writes the other   */
+#define LBM_POP_AA 1   /* one buffer, in place (AA pattern): even steps read and
+                          write each node's own slots (swapped), odd steps pull
+                          from and push to the neighbours' slots.  Half the
+                          population memory.  Not with moving obstacles, the
+                          adjoint or zero_gradient links; the scalar kernel
+                          only, its launch shape fixed (no autotuner trials:
+                          they would advance the state). */
+
 /* flags of lbm_step_ex: what the last step of the call records */
 #define LBM_STEP_MOMENTS 1   /* keep rho/u of that step for lbm_get_moments */
 #define LBM_STEP_RESIDUAL 2  /* evaluate the residual for lbm_residual      */
@@ -78,7 +88,7 @@ typedef struct {
   int32_t forcing;         /* LBM_FORCING_NONE / LBM_GUO_*                     */
   int32_t body_force_field;/* 1: per-node force field replaces rho*g           */
   int32_t device;          /* CUDA device ordinal                              */
-  int32_t reserved;
+  int32_t layout;          /* LBM_POP_AB (default) / LBM_POP_AA                */
   double omega;            /* 1/tau, tau = kin_visc*inv_cs_2 + 0.5             */
   double inv_cs_2, inv_cs_4; /* pylabolt/base/lattice.py:41-44 values           */
   double eps;              /* control.float_min (FP64 eps)                     */

@@ -17,6 +17,7 @@ LBM_BGK, LBM_MRT = 0, 1
 LBM_FORCING_NONE, LBM_GUO_LINEAR, LBM_GUO_SECOND_ORDER = 0, 1, 2
 LINK_PULL, LINK_ZERO, LINK_BB, LINK_MBB, LINK_ABB = 0, 1, 2, 3, 4
 LAYOUT_INNER, LAYOUT_PADDED = 0, 1
+POP_AB, POP_AA = 0, 1
 STEP_MOMENTS, STEP_RESIDUAL = 1, 2
 
 STATUS_NAMES = {0: "LBM_OK", 1: "LBM_ERR_ARG", 2: "LBM_ERR_CUDA", 3: "LBM_ERR_NONFINITE",
@@ -39,7 +40,7 @@ class LbmConfig(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32),
                 ("precision", ctypes.c_int32), ("collision", ctypes.c_int32),
                 ("forcing", ctypes.c_int32), ("body_force_field", ctypes.c_int32),
-                ("device", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("device", ctypes.c_int32), ("layout", ctypes.c_int32),
                 ("omega", ctypes.c_double), ("inv_cs_2", ctypes.c_double),
                 ("inv_cs_4", ctypes.c_double), ("eps", ctypes.c_double),
                 ("gravity", ctypes.c_double * 2), ("mrt_s", ctypes.c_double * 4),

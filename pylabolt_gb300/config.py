@@ -13,6 +13,10 @@ Project extensions (no reference key exists for them):
   selects the population storage (default: ``fp64`` for precision
   ``double``, ``fp32_shifted`` for ``single``), ``control_dict["fp16_scale"]``
   the FP16 storage scale;
+* ``control_dict["population_layout"]`` in ``{"ab", "aa"}``: two population
+  buffers (default) or one buffer updated in place (AA pattern; half the
+  population memory, not with moving obstacles, the adjoint or
+  zero_gradient boundaries);
 * ``collision_dict["fluid"]["mrt_rates"] = {"s_e", "s_eps", "s_q", "s_nu"}``
   (defaults: the reference's S = [1,...,1, omega, omega]);
 * boundary type ``zero_gradient``;
@@ -29,6 +33,7 @@ COLLISION_MODELS = ["BGK", "MRT"]
 EQUILIBRIUM_MODELS = ["density_based_second_order"]
 FORCING_MODELS = [None, "guo_linear", "guo_second_order"]
 STORAGES = ["fp64", "fp32_shifted", "fp16_shifted"]
+POPULATION_LAYOUTS = ["ab", "aa"]
 
 
 def _get(sim, name):
@@ -147,6 +152,10 @@ class Case:
         if self.storage not in STORAGES:
             raise ValueError(f"unsupported storage {self.storage!r}; available {STORAGES}")
         self.fp16_scale = float(cd.get("fp16_scale", 4096.0))
+        self.population_layout = cd.get("population_layout", "ab")
+        if self.population_layout not in POPULATION_LAYOUTS:
+            raise ValueError(f"unsupported population_layout {self.population_layout!r}; "
+                             f"available {POPULATION_LAYOUTS}")
 
     # ---- mesh_dict -- mesh.py:20-42
     def _mesh(self, md):

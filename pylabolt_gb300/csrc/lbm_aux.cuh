@@ -11,7 +11,7 @@ constexpr int kStepBlock = 256;
 
 template <class S>
 __global__ void convert_kernel(const Geom g, const Params p, S* f, double* f64,
-                               int dir) {
+                               int dir, int aa_state) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   if (x >= g.nx) return;
@@ -22,7 +22,8 @@ __global__ void convert_kernel(const Geom g, const Params p, S* f, double* f64,
     const long long i = k * g.plane + n;
     const double w = Store<S>::shifted ? Wk(k) : 0.0;
     if (dir == 0) {
-      f64[i] = solid ? 0.0 : double(Store<S>::ld(f, i, p)) + w;
+      const long long src = aa_post_index(g.plane, g.pitch, aa_state, n, k);
+      f64[i] = solid ? 0.0 : double(Store<S>::ld(f, src, p)) + w;
     } else {
       Store<S>::st(f, i, typename Store<S>::T(solid ? 0.0 : f64[i] - w), p);
     }
@@ -54,7 +55,7 @@ __global__ void body_from_f64_kernel(const Geom g, const double* in, T* out) {
 // One block per row; fixed summation order -> deterministic.
 template <class S>
 __global__ void conservation_kernel(const Geom g, const Params p, const S* f,
-                                    double* partials) {
+                                    double* partials, int aa_state) {
   const int y = blockIdx.x;
   double s[3] = {0, 0, 0};
   for (int x = threadIdx.x; x < g.nx; x += blockDim.x) {
@@ -62,7 +63,7 @@ __global__ void conservation_kernel(const Geom g, const Params p, const S* f,
     if (g.cls[n] == 2) continue;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-      const double v = double(Store<S>::ld(f, k * g.plane + n, p)) +
+      const double v = double(Store<S>::ld(f, aa_post_index(g.plane, g.pitch, aa_state, n, k), p)) +
                        (Store<S>::shifted ? Wk(k) : 0.0);
       s[0] += v;
       s[1] += CXk(k) * v;
@@ -91,6 +92,15 @@ struct Kernels {
   template <int COLL, int FORC>
   static cudaError_t step_t(const StepArgs& a, Variant v, int sms, cudaStream_t s) {
     const dim3 grid = step_grid(a.g, v, sms, sizeof(S));
+    if (a.aa) {   // AA layout: the scalar kernel (capped for shifted storage), one phase
+      constexpr int AC = Store<S>::shifted ? (COLL == 0 ? 1 : 2) : 0;
+      if (v.kind != 0 || v.block > 256) return cudaErrorInvalidValue;
+      if (a.aa == 1)
+        step_aa_kernel<S, COLL, FORC, AC, false><<<grid, v.block, 0, s>>>(a);
+      else
+        step_aa_kernel<S, COLL, FORC, AC, true><<<grid, v.block, 0, s>>>(a);
+      return cudaGetLastError();
+    }
     if constexpr (Store<S>::shifted) {
       if (v.kind == 2) {
         if (v.stages < 1 || v.stages > 8) return cudaErrorInvalidValue;
@@ -153,9 +163,9 @@ struct Kernels {
     return cudaGetLastError();
   }
   static cudaError_t convert(const Geom& g, const Params& p, void* f,
-                             double* f64, int dir, cudaStream_t s) {
+                             double* f64, int dir, int aa_state, cudaStream_t s) {
     convert_kernel<S><<<node_grid(g), kStepBlock, 0, s>>>(g, p, static_cast<S*>(f),
-                                                           f64, dir);
+                                                           f64, dir, aa_state);
     return cudaGetLastError();
   }
   static cudaError_t moments_to_f64(const Geom& g, const void* mr, const void* mx,
@@ -172,8 +182,9 @@ struct Kernels {
     return cudaGetLastError();
   }
   static cudaError_t conservation(const Geom& g, const Params& p, const void* f,
-                                  double* partials, cudaStream_t s) {
-    conservation_kernel<S><<<g.ny, 256, 0, s>>>(g, p, static_cast<const S*>(f), partials);
+                                  double* partials, int aa_state, cudaStream_t s) {
+    conservation_kernel<S><<<g.ny, 256, 0, s>>>(g, p, static_cast<const S*>(f), partials,
+                                                aa_state);
     return cudaGetLastError();
   }
   template <class U = S>

@@ -69,7 +69,8 @@ struct LbmHandle {
   double* host_red = nullptr;  // pinned  [16]
   double* stage = nullptr;     // device FP64 staging
   size_t stage_elems = 0;
-  int cur = 0;
+  int cur = 0;                 // AA layout: both pop[] are one buffer; cur 0 = next step even
+  bool aa = false;             // LBM_POP_AA
   bool initialized = false, nopull = true, has_moments = false, has_residual = false;
   int64_t t = 0, launches = 0;
   cudaGraphExec_t gexec = nullptr;
@@ -241,7 +242,7 @@ struct LbmHandle {
 
   int launch_v(int flags, lbm::Variant v, bool advance) {
     const int rc = launch_bufs(flags, v, pop[cur], pop[cur ^ 1], side[cur], side[cur ^ 1], nullptr,
-                               mov.rho_dyn[cur], mov.rho_dyn[cur ^ 1]);
+                               mov.rho_dyn[cur], mov.rho_dyn[cur ^ 1], aa ? (cur == 0 ? 1 : 2) : 0);
     if (rc == LBM_OK && advance) cur ^= 1;
     return rc;
   }
@@ -249,7 +250,7 @@ struct LbmHandle {
   // One fused step from `fin` / `side_in` into `fout` / `side_out`.
   int launch_bufs(int flags, lbm::Variant v, const void* fin, void* fout, const void* sin,
                   void* sout, cudaStream_t on = nullptr, const void* rdin = nullptr,
-                  void* rdout = nullptr) {
+                  void* rdout = nullptr, int aa_phase = 0) {
     lbm::StepArgs a;
     a.g = g;
     a.p = p;
@@ -274,6 +275,7 @@ struct LbmHandle {
     a.us = mov.us;
     a.rho_dyn_in = rdin;
     a.rho_dyn_out = rdout;
+    a.aa = aa_phase;
     a.flags = flags;
     LBM_CUDA(ks->step(cfg.collision, cfg.forcing, a, v, sms, on ? on : stream));
     return LBM_OK;
@@ -352,6 +354,11 @@ struct LbmHandle {
     return wait();
   }
 
+  // Where the post-collision populations of the current state sit
+  // (lbm::aa_post_index): 0 two buffers or freshly set, 1 after an even AA
+  // phase, 2 after an odd one.
+  int aa_state() const { return !aa || nopull ? 0 : (cur == 1 ? 1 : 2); }
+
   size_t state_bytes() const { return (9 * g.plane + 2 * g.pitch) * (size_t)ks->elem_bytes; }
   size_t side_bytes() const { return 3 * (size_t)std::max(g.nrec, 1) * ks->compute_bytes; }
 
@@ -388,6 +395,7 @@ struct LbmHandle {
   // advancing it) and keeps the fastest.
   int autotune() {
     tuned = true;
+    if (aa) return LBM_OK;   // in place: a trial launch would advance the state
     if (const char* f = std::getenv("LBM_VARIANT")) {
       int kind = -1, vec = 0, blk = 0, st = 0;
       if (std::sscanf(f, "%d,%d,%d,%d", &kind, &vec, &blk, &st) == 4) {
@@ -564,14 +572,19 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
     return fail(LBM_ERR_ARG, "lbm_create: omega = 1/tau must lie in (0, 2)");
   if (c.precision == LBM_FP16_SHIFTED && !(c.fp16_scale > 0.0))
     return fail(LBM_ERR_ARG, "lbm_create: fp16_scale must be > 0");
+  if (c.layout != LBM_POP_AB && c.layout != LBM_POP_AA)
+    return fail(LBM_ERR_ARG, "lbm_create: unknown population layout");
+  const bool aa = c.layout == LBM_POP_AA;
 
   const lbm::KernelSet* ks = c.precision == LBM_FP64 ? &lbm::kernels_fp64()
                              : c.precision == LBM_FP32_SHIFTED ? &lbm::kernels_fp32()
                                                                 : &lbm::kernels_fp16();
   const int nx = c.nx, ny = c.ny;
-  // rows are whole TMA tiles (4096 B) for shifted storage, 512 B for FP64
-  const int align = (c.precision == LBM_FP64 ? 512 : lbm::kTmaRowBytes) / ks->elem_bytes;
-  const int pitch = (nx + align - 1) / align * align;
+  // rows are whole TMA tiles (4096 B) for shifted storage, 512 B for FP64.
+  // AA layout (scalar kernel only): 128-byte rows with at least one padding
+  // column, which receives the pushes across the x edges.
+  const int align = (aa ? 128 : c.precision == LBM_FP64 ? 512 : lbm::kTmaRowBytes) / ks->elem_bytes;
+  const int pitch = ((aa ? nx + 1 : nx) + align - 1) / align * align;
   const long long plane = (long long)(ny + 2) * pitch;
   if (plane >= (1LL << 31) / 1)
     return fail(LBM_ERR_ARG, "lbm_create: grid too large (ny*pitch must be < 2^31)");
@@ -640,6 +653,34 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
                                        std::to_string(y) + ") borders the grid edge or a solid but has no link record");
       }
     }
+  // AA layout: a thread's in-place reads and writes must not meet another
+  // node's.  A non-pull link of direction k reads a slot that the node's
+  // neighbour x - c_k would write, so that neighbour must be solid or outside
+  // the grid; a pull from s reads a slot that the node s + c_k would write,
+  // so that node must be the puller itself, solid or outside the grid.
+  if (aa)
+    for (int64_t r = 0; r < nlinks; ++r) {
+      const LbmNodeLinks& L = links[r];
+      const long long x = L.node / ny, y = L.node % ny;
+      for (int k = 1; k < 9; ++k) {
+        long long tx, ty;
+        if (L.type[k] == LBM_LINK_PULL) {
+          tx = L.src[k] / ny + kCX[k];
+          ty = L.src[k] % ny + kCY[k];
+          if (tx == x && ty == y) continue;
+        } else if (L.type[k] == LBM_LINK_ZERO) {
+          continue;
+        } else {
+          tx = x - kCX[k];
+          ty = y - kCY[k];
+        }
+        if (tx >= 0 && tx < nx && ty >= 0 && ty < ny && cls[dnode(tx, ty)] != 2)
+          return fail(LBM_ERR_ARG, "lbm_create: AA layout: link " + std::to_string(k) + " of node (" +
+                                       std::to_string(x) + "," + std::to_string(y) +
+                                       ") reads a population another fluid node overwrites in place "
+                                       "(zero_gradient or an inner boundary); use the two-buffer layout");
+      }
+    }
   const int nseg = (nx + 31) / 32;
   std::vector<uint8_t> segflag((size_t)ny * nseg, 0);
   for (int y = 0; y < ny; ++y)
@@ -683,10 +724,12 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
       (rc = h->alloc(&d_rparam, 9 * nrec1 * sizeof(double))) ||
       (rc = h->alloc(&d_raux, 9 * nrec1 * sizeof(int))) ||
       (rc = h->alloc(&h->pop_raw[0], (9 * plane + 2 * pitch) * eb)) ||
-      (rc = h->alloc(&h->pop_raw[1], (9 * plane + 2 * pitch) * eb)) ||
+      (!aa && (rc = h->alloc(&h->pop_raw[1], (9 * plane + 2 * pitch) * eb))) ||
       (rc = h->alloc(&h->side[0], 3 * nrec1 * cb)) || (rc = h->alloc(&h->side[1], 3 * nrec1 * cb)))
     return bail(rc);
   // one guard row before and after the nine planes
+  if (aa) h->pop_raw[1] = h->pop_raw[0];
+  h->aa = aa;
   for (int i = 0; i < 2; ++i) h->pop[i] = static_cast<char*>(h->pop_raw[i]) + pitch * eb;
   for (int i = 0; i < 3; ++i)
     if ((rc = h->alloc(&h->mom[i], plane * cb))) return bail(rc);
@@ -700,6 +743,10 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&h->err_dev), h->err_host, 0);
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaHostGetDevicePointer: ") + cudaGetErrorString(e)));
   h->variant = ks->variants[0];
+  if (aa) {   // the scalar kernel, 256 threads (its register cap is chosen per storage)
+    h->variant = lbm::Variant{0, 1, 256, c.precision == LBM_FP64 ? 0 : (c.collision == LBM_BGK ? 1 : 2)};
+    h->tuned = true;
+  }
   long long maxparts = ny;
   for (int i = 0; i < ks->nvariants; ++i) maxparts = std::max(maxparts, h->nparts_of(ks->variants[i]));
   if ((rc = h->alloc(reinterpret_cast<void**>(&h->partials), maxparts * 8 * sizeof(double))) ||
@@ -815,6 +862,7 @@ int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout
     LBM_CUDA(cudaMemcpyAsync(const_cast<uint8_t*>(h->g.segflag), h->mov.seg_static,
                              (size_t)h->g.ny * h->g.nseg, cudaMemcpyDeviceToDevice, h->stream));
   }
+  if (h->aa) h->cur = 0;   // AA: the first step is an even phase
   LBM_CUDA(h->ks->init(h->g, h->p, ds, ds + plane, h->pop[h->cur], h->mom[0], h->mom[1],
                        h->mom[2], h->stream));
   for (int i = 0; i < 6; ++i)
@@ -952,6 +1000,7 @@ int lbm_adjoint_forward(LbmHandle* h, int64_t nsteps, int interval) {
   if (nsteps < 1 || interval < 1) return fail(LBM_ERR_ARG, "lbm_adjoint_forward: need nsteps >= 1, interval >= 1");
   if (!h->initialized || !h->nopull || h->t != 0)
     return fail(LBM_ERR_STATE, "lbm_adjoint_forward: call lbm_init_fields first (the pass starts at t = 0)");
+  if (h->aa) return fail(LBM_ERR_ARG, "lbm_adjoint_forward: not available with the AA population layout");
   LBM_CUDA(cudaSetDevice(h->cfg.device));
   int rc = h->build_adjoint_tables();
   if (rc) return rc;
@@ -1189,7 +1238,7 @@ int lbm_conservation(LbmHandle* h, double out[3]) {
   if (!h || !out) return fail(LBM_ERR_ARG, "lbm_conservation: null argument");
   if (!h->initialized) return fail(LBM_ERR_STATE, "lbm_conservation: not initialised");
   LBM_CUDA(cudaSetDevice(h->cfg.device));
-  LBM_CUDA(h->ks->conservation(h->g, h->p, h->pop[h->cur], h->partials, h->stream));
+  LBM_CUDA(h->ks->conservation(h->g, h->p, h->pop[h->cur], h->partials, h->aa_state(), h->stream));
   LBM_CUDA(lbm::finish_reduce(h->partials, h->g.ny, h->scratch, h->red + 8, h->stream));
   LBM_CUDA(cudaMemcpyAsync(h->host_red + 8, h->red + 8, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   int rc = h->wait();
@@ -1207,7 +1256,7 @@ int lbm_get_populations(LbmHandle* h, double* pop) {
   if (rc) return rc;
   double* hs = h->stage;
   double* ds = h->stage + 9 * nh;
-  LBM_CUDA(h->ks->convert(h->g, h->p, h->pop[h->cur], ds, 0, h->stream));
+  LBM_CUDA(h->ks->convert(h->g, h->p, h->pop[h->cur], ds, 0, h->aa_state(), h->stream));
   LBM_CUDA(cudaMemsetAsync(hs, 0, 9 * nh * sizeof(double), h->stream));
   LBM_CUDA(lbm::reorder(h->g, ds, hs, 9, LBM_LAYOUT_PADDED, 0, h->stream));
   LBM_CUDA(cudaMemcpyAsync(pop, hs, 9 * nh * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -1226,7 +1275,8 @@ int lbm_set_populations(LbmHandle* h, const double* pop_new) {
   LBM_CUDA(cudaMemcpyAsync(hs, pop_new, 9 * nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   LBM_CUDA(cudaMemsetAsync(ds, 0, 9 * plane * sizeof(double), h->stream));
   LBM_CUDA(lbm::reorder(h->g, hs, ds, 9, LBM_LAYOUT_PADDED, 1, h->stream));
-  LBM_CUDA(h->ks->convert(h->g, h->p, h->pop[h->cur], ds, 1, h->stream));
+  if (h->aa) h->cur = 0;   // AA: the next step is an even phase that reads the set values
+  LBM_CUDA(h->ks->convert(h->g, h->p, h->pop[h->cur], ds, 1, 0, h->stream));
   if ((rc = h->wait())) return rc;
   h->initialized = true;
   h->nopull = true;
@@ -1315,6 +1365,7 @@ int lbm_forces(LbmHandle* h, double* out) {
   a.arm = F.arm;
   a.gstart = F.gstart;
   a.nopull = h->nopull ? 1 : 0;
+  a.aa_state = h->aa_state();
   a.out = F.out;
   LBM_CUDA(h->ks->forces(a, F.ngroups, h->stream));
   LBM_CUDA(cudaMemcpyAsync(out, F.out, 3 * (size_t)F.ngroups * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -1328,6 +1379,8 @@ int lbm_set_moving_obstacles(LbmHandle* h, const LbmMovingObstacle* obs, int n,
     return fail(LBM_ERR_ARG, "lbm_set_moving_obstacles: 0 to " + std::to_string(lbm::kMovMaxObstacles) +
                                  " obstacles");
   if (h->mov.n) return fail(LBM_ERR_STATE, "lbm_set_moving_obstacles: already set");
+  if (h->aa && n > 0)
+    return fail(LBM_ERR_ARG, "lbm_set_moving_obstacles: not available with the AA population layout");
   if (n == 0) return LBM_OK;
   LBM_CUDA(cudaSetDevice(h->cfg.device));
   const lbm::Geom& g = h->g;

@@ -11,7 +11,8 @@
 // pop_new at a boundary node is what the next step's pull computes from the
 // node's link record, so the same link evaluation is reused.  Right after
 // initialisation both are the stored populations (the reference initialises
-// pop = pop_new = f_eq).
+// pop = pop_new = f_eq).  In the AA layout p_t and the link values are read
+// where the phase left them (aa_post_index, special_link_aa).
 //
 // One block per group, a fixed-stride walk over the group's links and a fixed
 // shared-memory tree: the sums are deterministic; they are formed in FP64 for
@@ -39,6 +40,25 @@ __device__ __forceinline__ typename Store<S>::T incoming_k(const Geom& g, const 
   }
 }
 
+// The same for the AA layout: ODD = the coming step is an odd phase.
+template <class S, bool ODD>
+__device__ __forceinline__ typename Store<S>::T incoming_k_aa(const Geom& g, const Params& p,
+                                                             const S* __restrict__ f, long long n,
+                                                             int r, const typename Store<S>::T* side,
+                                                             int k) {
+  switch (k) {
+    case 1: return special_link_aa<1, S, ODD>(g, p, f, n, r, side);
+    case 2: return special_link_aa<2, S, ODD>(g, p, f, n, r, side);
+    case 3: return special_link_aa<3, S, ODD>(g, p, f, n, r, side);
+    case 4: return special_link_aa<4, S, ODD>(g, p, f, n, r, side);
+    case 5: return special_link_aa<5, S, ODD>(g, p, f, n, r, side);
+    case 6: return special_link_aa<6, S, ODD>(g, p, f, n, r, side);
+    case 7: return special_link_aa<7, S, ODD>(g, p, f, n, r, side);
+    case 8: return special_link_aa<8, S, ODD>(g, p, f, n, r, side);
+    default: return Store<S>::ld(f, n, p);
+  }
+}
+
 constexpr int kForceBlock = 256;
 
 template <class S>
@@ -53,9 +73,16 @@ __global__ void __launch_bounds__(kForceBlock) force_kernel(const ForceArgs a) {
   for (int i = a.gstart[grp] + threadIdx.x; i < a.gstart[grp + 1]; i += kForceBlock) {
     const long long n = a.node[i];
     const int ko = a.kk[2 * i], ki = a.kk[2 * i + 1];
-    double fo = double(Store<S>::ld(f, ko * a.g.plane + n, a.p));
-    double fi = double(a.nopull ? Store<S>::ld(f, ki * a.g.plane + n, a.p)
-                                : incoming_k<S>(a.g, a.p, f, n, a.rec[i], side, ki));
+    double fo = double(Store<S>::ld(f, aa_post_index(a.g.plane, a.g.pitch, a.aa_state, n, ko), a.p));
+    double fi;
+    if (a.nopull)
+      fi = double(Store<S>::ld(f, ki * a.g.plane + n, a.p));
+    else if (a.aa_state == 1)   // AA, after an even phase: the next step is odd
+      fi = double(incoming_k_aa<S, true>(a.g, a.p, f, n, a.rec[i], side, ki));
+    else if (a.aa_state == 2)
+      fi = double(incoming_k_aa<S, false>(a.g, a.p, f, n, a.rec[i], side, ki));
+    else
+      fi = double(incoming_k<S>(a.g, a.p, f, n, a.rec[i], side, ki));
     if (SH) {  // shifted storage holds f - w
       fo += Wk(ko);
       fi += Wk(ki);

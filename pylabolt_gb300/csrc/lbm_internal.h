@@ -83,6 +83,8 @@ struct StepArgs {
   // that does not advance the state (autotuner) leaves it untouched
   const void* rho_dyn_in;
   void* rho_dyn_out;
+  int aa;                  // 0: two buffers (fin -> fout); AA layout (fin == fout):
+                           // 1 even phase, 2 odd phase
   int flags;
 };
 
@@ -117,8 +119,23 @@ struct ForceArgs {
   const double* arm;      // [2n] lever arm rx, ry
   const int* gstart;      // [ngroups+1]
   int nopull;             // state holds incoming populations (t = 0): f_new = p
+  int aa_state;           // AA layout: 1 after an even phase, 2 after an odd one
   double* out;            // [ngroups][3] fx, fy, torque
 };
+
+// Where the post-collision population k of node n sits in the AA layout:
+// after an even phase in the node's own opposite slot, after an odd phase in
+// slot k of the neighbour it moves to; otherwise (two buffers, or the
+// incoming populations after initialisation) at the node's slot k.
+__host__ __device__ inline long long aa_post_index(long long plane, int pitch, int state,
+                                                   long long n, int k) {
+  const int cx = (k == 1 || k == 5 || k == 8) ? 1 : ((k == 3 || k == 6 || k == 7) ? -1 : 0);
+  const int cy = (k == 2 || k == 5 || k == 6) ? 1 : ((k == 4 || k == 7 || k == 8) ? -1 : 0);
+  const int kb = k == 0 ? 0 : (k <= 4 ? ((k + 1) % 4) + 1 : ((k - 3) % 4) + 5);
+  if (state == 1) return kb * plane + n;
+  if (state == 2) return k * plane + n + (long long)cy * pitch + cx;
+  return k * plane + n;
+}
 
 // A moving obstacle on the device (FP64 state, see lbm_set_moving_obstacles).
 struct MovObs {
@@ -184,8 +201,9 @@ struct KernelSet {
                       const double* u, void* f, void* mr, void* mx, void* my,
                       cudaStream_t s);
   // storage <-> FP64 [9][plane] (dir 0: to FP64, 1: from FP64); solids 0.
+  // aa_state (dir 0): where the post-collision values sit (aa_post_index).
   cudaError_t (*convert)(const Geom& g, const Params& p, void* f, double* f64,
-                         int dir, cudaStream_t s);
+                         int dir, int aa_state, cudaStream_t s);
   // moments (compute type) -> FP64 [3][plane]
   cudaError_t (*moments_to_f64)(const Geom& g, const void* mr, const void* mx,
                                 const void* my, double* out, cudaStream_t s);
@@ -194,7 +212,7 @@ struct KernelSet {
                                cudaStream_t s);
   // partial sums {sum f, sum cx f, sum cy f} per block row -> partials[ny][8]
   cudaError_t (*conservation)(const Geom& g, const Params& p, const void* f,
-                              double* partials, cudaStream_t s);
+                              double* partials, int aa_state, cudaStream_t s);
   // one reverse step (null where the storage has no adjoint)
   cudaError_t (*adjoint)(int forcing, const AdjArgs& a, cudaStream_t s);
   // momentum-exchange sums, one block per group

@@ -719,6 +719,125 @@ __global__ void __launch_bounds__(CAP ? 256 : 512, CAP == 1 ? 8 : (CAP == 2 ? 6 
 }
 
 // ---------------------------------------------------------------------------
+// AA layout: one population array updated in place (pylabolt_gb300 layout
+// LBM_POP_AA).  With off(k) = c_ky * pitch + c_kx:
+//   even phase  reads  f_k = A[n][k]                 (the incoming values)
+//               writes A[n][kbar] = p_k               (own node, swapped)
+//   odd phase   reads  f_k = A[n - off(k)][kbar]      (neighbour's swapped slot)
+//               writes A[n + off(k)][k] = p_k         (pushed to the neighbour)
+// Every location a thread writes is one only it reads, so the update is in
+// place without races.  Link records see the same values as the pull kernel:
+//   even  PULL from s: A[s + off(k)][k]   bounce-back raw p_kbar: A[n - off(k)][kbar]
+//   odd   PULL from s: A[s][kbar]         bounce-back raw p_kbar: A[n][k]
+// (the first step after initialisation reads A[n][k] for every node, like
+// the pull kernel's no-pull step).  Pushes beyond the domain edges land in
+// the padding rows / columns (pitch >= nx + 2) or the guard rows; the host
+// rejects PULL sources whose even-phase location another node would
+// overwrite (zero_gradient).
+template <int K, class S, bool ODD>
+__device__ __forceinline__ typename Store<S>::T special_link_aa(
+    const Geom& g, const Params& p, const S* __restrict__ A, long long n, int r,
+    const typename Store<S>::T* __restrict__ side) {
+  using T = typename Store<S>::T;
+  constexpr bool SH = Store<S>::shifted;
+  constexpr int KB = INVk(K);
+  const long long off = (long long)CYk(K) * g.pitch + CXk(K);
+  const int li = r * 9 + K;
+  const int type = g.rtype[li];
+  if (type == LINK_PULL) {
+    const long long s = g.rsrc[li];
+    return ODD ? Store<S>::ld(A, KB * g.plane + s, p) : Store<S>::ld(A, K * g.plane + s + off, p);
+  }
+  if (type == LINK_ZERO) return SH ? T(-Wk(K)) : T(0);
+  const T raw = ODD ? Store<S>::ld(A, K * g.plane + n, p) : Store<S>::ld(A, KB * g.plane + n - off, p);
+  if (type == LINK_BB) return raw;
+  if (type == LINK_MBB) {
+    const T rho = side[3 * r];
+    if (!SH)
+      return raw - ((T(2.0 * Wk(KB)) * rho) * T(p.inv_cs_2)) * T(g.rparam[li]);
+    return raw - (T(2.0 * Wk(KB)) * rho * T(3)) * T(g.rparam[li]);
+  }
+  const int ra = g.raux[li];
+  const T ux = side[3 * r + 1], uy = side[3 * r + 2];
+  const T uex = ux + T(0.5) * (ux - side[3 * ra + 1]);
+  const T uey = uy + T(0.5) * (uy - side[3 * ra + 2]);
+  const T u2 = uex * uex + uey * uey;
+  const T cu = lin2<CXk(KB), CYk(KB)>(uex, uey);
+  const T rho_w = T(g.rparam[li]);
+  if (!SH) {
+    const T temp = (T(2.0 * Wk(KB)) * rho_w) *
+                   ((T(1) + (T(p.half_inv_cs_4) * cu) * cu) - T(p.half_inv_cs_2) * u2);
+    return -raw + temp;
+  }
+  const T drho_w = T(g.rparam[li] - 1.0);
+  return -raw + T(2.0 * Wk(KB)) * (drho_w + rho_w * (T(4.5) * cu * cu - T(1.5) * u2));
+}
+
+template <class S, bool ODD>
+__device__ __forceinline__ void special_links_aa(typename Store<S>::T f[9], const StepArgs& a,
+                                                 const S* __restrict__ A, long long n, int r) {
+  using T = typename Store<S>::T;
+  const T* side = static_cast<const T*>(a.side_in);
+  f[1] = special_link_aa<1, S, ODD>(a.g, a.p, A, n, r, side);
+  f[2] = special_link_aa<2, S, ODD>(a.g, a.p, A, n, r, side);
+  f[3] = special_link_aa<3, S, ODD>(a.g, a.p, A, n, r, side);
+  f[4] = special_link_aa<4, S, ODD>(a.g, a.p, A, n, r, side);
+  f[5] = special_link_aa<5, S, ODD>(a.g, a.p, A, n, r, side);
+  f[6] = special_link_aa<6, S, ODD>(a.g, a.p, A, n, r, side);
+  f[7] = special_link_aa<7, S, ODD>(a.g, a.p, A, n, r, side);
+  f[8] = special_link_aa<8, S, ODD>(a.g, a.p, A, n, r, side);
+  if constexpr (Store<S>::scaled) {
+#pragma unroll
+    for (int k = 1; k < 9; ++k) f[k] *= a.p.f_scale;
+  }
+}
+
+template <class S, int COLL, int FORC, int CAP, bool ODD>
+__global__ void __launch_bounds__(CAP ? 256 : 512, CAP == 1 ? 8 : (CAP == 2 ? 6 : 1))
+    step_aa_kernel(const StepArgs a) {
+  using T = typename Store<S>::T;
+  const Geom& g = a.g;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  T red[7] = {0, 0, 0, 0, 0, 0, 0};
+  if (x < g.nx) {
+    const int ni = (y + 1) * g.pitch + x;
+    const long long n = ni;
+    S* A = static_cast<S*>(a.fout);   // == a.fin
+    int cls = 0;
+    if (g.segflag[y * g.nseg + (x >> 5)]) cls = g.cls[ni];
+    if (cls != 2) {
+      T f[9];
+      int r = -1;
+      if (cls == 1) r = g.recmap[ni];
+      if (!ODD && ((a.flags & F_NOPULL) || cls == 0)) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) f[k] = Store<S>::ldr(A + k * g.plane, ni);
+      } else if (ODD && cls == 0) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+          f[k] = Store<S>::ldr(A + INVk(k) * g.plane, ni - CYk(k) * g.pitch - CXk(k));
+      } else {
+        f[0] = Store<S>::ldr(A, ni);
+        special_links_aa<S, ODD>(f, a, A, n, r);
+      }
+      T rho, ux, uy;
+      node_update<S, COLL, FORC>(f, a, n, rho, ux, uy, y * g.nseg + (x >> 5));
+      if (!ODD) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Store<S>::str(A + INVk(k) * g.plane, ni, f[k]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 9; ++k)
+          Store<S>::str(A + k * g.plane, ni + CYk(k) * g.pitch + CXk(k), f[k]);
+      }
+      node_outputs<T>(a, n, r, rho, ux, uy, red);
+    }
+  }
+  if (a.flags & F_RESIDUAL) block_residual<decltype(red[0] + 0)>(a, red);
+}
+
+// ---------------------------------------------------------------------------
 // Vector I/O of V consecutive nodes (16- or 8-byte aligned accesses).
 template <class S, int V> struct VecIO;
 template <int V> struct VecIO<float, V> {

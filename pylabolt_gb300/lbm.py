@@ -20,8 +20,9 @@ _FORCING = {None: capi.LBM_FORCING_NONE, "guo_linear": capi.LBM_GUO_LINEAR,
             "guo_second_order": capi.LBM_GUO_SECOND_ORDER}
 
 
-def make_config(case, storage=None, device=0):
+def make_config(case, storage=None, device=0, layout=None):
     storage = storage or case.storage
+    layout = layout or case.population_layout
     cfg = capi.LbmConfig()
     cfg.nx, cfg.ny = case.nx, case.ny
     cfg.precision = _STORAGE[storage]
@@ -34,19 +35,23 @@ def make_config(case, storage=None, device=0):
     cfg.gravity[:] = [float(v) for v in case.gravity]
     cfg.mrt_s[:] = list(case.mrt_rates)
     cfg.fp16_scale = case.fp16_scale
+    cfg.layout = capi.POP_AA if layout == "aa" else capi.POP_AB
     return cfg
 
 
 class FluidLBM:
     """One fluidLB case resident on the GPU."""
 
-    def __init__(self, case, storage=None, device=0):
+    def __init__(self, case, storage=None, device=0, layout=None):
         if not isinstance(case, Case):
             case = Case(case)
         self.case = case
         self.storage = storage or case.storage
+        self.layout = layout or case.population_layout
+        if self.layout not in ("ab", "aa"):
+            raise ValueError(f"unknown population layout {self.layout!r}")
         self.lib = capi.load()
-        self.cfg = make_config(case, self.storage, device)
+        self.cfg = make_config(case, self.storage, device, self.layout)
         self.node_solid, self.links = build_links(case)
         h = ctypes.c_void_p()
         check(self.lib.lbm_create(ctypes.byref(self.cfg), ptr(self.node_solid),

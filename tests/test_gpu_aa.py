@@ -1,0 +1,122 @@
+"""AA (in-place) population layout on the GPU.
+
+FP64 storage must reproduce the reference-kernel fixtures bit for bit, like
+the two-buffer layout, after even and odd step counts (populations read back
+through both phases' addressing); residuals, forces and conservation sums
+agree with the two-buffer run; FP32 / FP16 shifted storage agrees with the
+two-buffer run within AB_TOL (the same node arithmetic in a different
+kernel)."""
+import numpy as np
+import pytest
+
+from _golden import golden_names, load_golden
+from pylabolt_gb300 import capi, workloads
+from pylabolt_gb300.config import Case
+from pylabolt_gb300.lbm import FluidLBM
+
+pytestmark = pytest.mark.gpu
+
+RES_RTOL = 1e-12
+FORCE_RTOL = 1e-12
+AB_TOL = {"fp32_shifted": 1e-6, "fp16_shifted": 1e-4}   # max |u_aa - u_ab| / max |u_ab|
+
+
+def _inner_mask(nx, ny, solid_padded):
+    m = np.zeros((nx + 2, ny + 2), dtype=bool)
+    m[1:-1, 1:-1] = True
+    return m.ravel() & ~solid_padded
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_aa_fp64_bit_exact_vs_reference_fixtures(name):
+    case_d, d = load_golden(name)
+    case = Case(case_d)
+    with FluidLBM(case, storage="fp64", layout="aa") as sim:
+        sim.initialize()
+        m = _inner_mask(case.nx, case.ny, d["solid"])
+        cps = set(d["checkpoints"].tolist())
+        res = []
+        for t in range(1, int(d["nsteps"]) + 1):
+            sim.step(1, moments=t in cps, residual=True)
+            res.append(sim.residual())
+            if t in cps:
+                rho, u = sim.moments(layout=capi.LAYOUT_PADDED)
+                pop = sim.populations()
+                assert np.array_equal(rho[m], d[f"density_t{t}"][m]), t
+                assert np.array_equal(u[m], d[f"velocity_t{t}"][m]), t
+                assert np.array_equal(pop[m], d[f"pop_t{t}"][m]), t
+        np.testing.assert_allclose(np.array(res), d["residuals"][:, 1:], rtol=RES_RTOL, atol=0)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_aa_forces_and_conservation_match_two_buffers(name):
+    case = Case(load_golden(name)[0])
+    with FluidLBM(case, storage="fp64") as ab, FluidLBM(case, storage="fp64", layout="aa") as aa:
+        ab.initialize()
+        aa.initialize()
+        for n in (0, 1, 1, 2, 5):   # forces read p_t and the next step's links in both phases
+            if n:
+                ab.step(n)
+                aa.step(n)
+            fa, fb = aa.forces(), ab.forces()
+            np.testing.assert_allclose(fa["obstacles"], fb["obstacles"], rtol=FORCE_RTOL, atol=1e-15)
+            np.testing.assert_allclose(fa["walls"], fb["walls"], rtol=FORCE_RTOL, atol=1e-15)
+            np.testing.assert_allclose(aa.conservation(), ab.conservation(), rtol=1e-13, atol=1e-13)
+            assert np.array_equal(aa.populations(), ab.populations())
+
+
+def test_aa_graph_replay_and_restart():
+    """Graph-replayed chunks (odd and even starting phase) equal single steps;
+    set_populations restarts from an even phase."""
+    case = Case(load_golden("periodic_moving_disk")[0])
+    with FluidLBM(case, storage="fp64", layout="aa") as a, \
+            FluidLBM(case, storage="fp64", layout="aa") as b, \
+            FluidLBM(case, storage="fp64") as c:
+        for s in (a, b, c):
+            s.initialize()
+        a.step(1)
+        a.step(100, moments=True)      # graphs start on an odd phase
+        for _ in range(101):
+            b.step(1)
+        c.step(101)
+        pa = a.populations()
+        assert np.array_equal(pa, b.populations())
+        assert np.array_equal(pa, c.populations())
+        a.step(64)
+        c.step(64)
+        assert np.array_equal(a.populations(), c.populations())
+        pop = c.populations()
+        b.set_populations(pop)
+        c.set_populations(pop)
+        b.step(33, moments=True)
+        c.step(33, moments=True)
+        assert np.array_equal(b.populations(), c.populations())
+        rb, ub = b.moments()
+        rc, uc = c.moments()
+        assert np.array_equal(rb, rc) and np.array_equal(ub, uc)
+
+
+@pytest.mark.parametrize("storage", ["fp32_shifted", "fp16_shifted"])
+@pytest.mark.parametrize("coll", ["BGK", "MRT"])
+def test_aa_shifted_storage_matches_two_buffers(storage, coll):
+    case = Case(workloads.cylinder(nx=512, ny=128, radius=16.0, center=(128, 67), model=coll))
+    out = {}
+    for layout in ("ab", "aa"):
+        with FluidLBM(case, storage=storage, layout=layout) as sim:
+            sim.initialize()
+            sim.step(501, moments=True)
+            out[layout] = sim.moments()[1]
+            if layout == "aa":
+                assert sim.device_bytes < out["bytes_ab"]
+            else:
+                out["bytes_ab"] = sim.device_bytes
+    err = np.abs(out["aa"] - out["ab"]).max() / np.abs(out["ab"]).max()
+    assert err <= AB_TOL[storage], err
+
+
+def test_aa_rejections_on_handle():
+    case = Case(load_golden("channel_cylinder_abb")[0])
+    with FluidLBM(case, storage="fp64", layout="aa") as sim:
+        sim.initialize()
+        with pytest.raises(capi.LbmError, match="AA population layout"):
+            sim.adjoint_forward(4, 2)

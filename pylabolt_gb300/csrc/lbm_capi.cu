@@ -53,7 +53,7 @@ struct LbmHandle {
   lbm::Geom g{};
   lbm::Params p{};
   cudaStream_t stream = nullptr;
-  std::vector<void*> allocs;
+  std::vector<std::pair<void*, size_t>> allocs;   // device allocations and their sizes
   size_t dev_bytes = 0;
   void* pop[2] = {nullptr, nullptr};      // first population plane
   void* pop_raw[2] = {nullptr, nullptr};  // allocation (one guard row each side)
@@ -142,8 +142,9 @@ struct LbmHandle {
   void release(void* q) {
     if (!q) return;
     for (auto it = allocs.begin(); it != allocs.end(); ++it)
-      if (*it == q) {
+      if (it->first == q) {
         cudaFree(q);
+        dev_bytes -= it->second;
         allocs.erase(it);
         return;
       }
@@ -156,7 +157,7 @@ struct LbmHandle {
     for (cudaEvent_t e : adj.ev)
       if (e) cudaEventDestroy(e);
     if (adj.aux) cudaStreamDestroy(adj.aux);
-    for (void* a : allocs) cudaFree(a);
+    for (auto& a : allocs) cudaFree(a.first);
     if (host_red) cudaFreeHost(host_red);
     if (err_host) cudaFreeHost(err_host);
     if (stream) cudaStreamDestroy(stream);
@@ -171,7 +172,7 @@ struct LbmHandle {
       return fail(LBM_ERR_ALLOC, "cudaMalloc(" + std::to_string(bytes) +
                                      " bytes): " + cudaGetErrorString(e));
     }
-    allocs.push_back(*p);
+    allocs.emplace_back(*p, bytes);
     dev_bytes += bytes;
     return LBM_OK;
   }
@@ -215,13 +216,7 @@ struct LbmHandle {
     if (stage_elems >= elems) return LBM_OK;
     if (stage) {
       LBM_CUDA(cudaStreamSynchronize(stream));
-      for (auto it = allocs.begin(); it != allocs.end(); ++it)
-        if (*it == stage) {
-          allocs.erase(it);
-          break;
-        }
-      dev_bytes -= stage_elems * sizeof(double);
-      cudaFree(stage);
+      release(stage);
       stage = nullptr;
       stage_elems = 0;
     }
@@ -352,6 +347,29 @@ struct LbmHandle {
     LBM_CUDA(cudaMemcpyAsync(adj.tr_self, trs.data(), n9, cudaMemcpyHostToDevice, stream));
     LBM_CUDA(cudaMemcpyAsync(adj.wall_rec, wr.data(), wr.size(), cudaMemcpyHostToDevice, stream));
     return wait();
+  }
+
+  // The residual's two sets of previous-step fields, allocated (zero, as
+  // after lbm_init_fields) by the first step that asks for a residual: runs
+  // without one keep six planes of compute type free.
+  int ensure_old() {
+    if (old[0]) return LBM_OK;
+    const size_t bytes = (size_t)g.plane * ks->compute_bytes;
+    for (int i = 0; i < 6; ++i) {
+      void* q = nullptr;
+      int rc = alloc(&q, bytes);
+      if (rc) {
+        for (int j = 0; j < i; ++j) {
+          release(old[j]);
+          old[j] = nullptr;
+        }
+        return rc;
+      }
+      old[i] = q;
+      LBM_CUDA(cudaMemsetAsync(old[i], 0, bytes, stream));
+    }
+    old_cur = 0;
+    return LBM_OK;
   }
 
   // Where the post-collision populations of the current state sit
@@ -733,8 +751,6 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   for (int i = 0; i < 2; ++i) h->pop[i] = static_cast<char*>(h->pop_raw[i]) + pitch * eb;
   for (int i = 0; i < 3; ++i)
     if ((rc = h->alloc(&h->mom[i], plane * cb))) return bail(rc);
-  for (int i = 0; i < 6; ++i)
-    if ((rc = h->alloc(&h->old[i], plane * cb))) return bail(rc);
   e = cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, c.device);
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("device attribute: ") + cudaGetErrorString(e)));
   e = cudaHostAlloc(reinterpret_cast<void**>(&h->err_host), sizeof(int), cudaHostAllocMapped);
@@ -778,9 +794,8 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
         (e = cudaMemsetAsync(h->side[i], 0, 3 * nrec1 * cb, h->stream)) != cudaSuccess)
       return bail(fail(LBM_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
   }
-  for (int i = 0; i < 6; ++i)
-    if ((i < 3 && (e = cudaMemsetAsync(h->mom[i], 0, plane * cb, h->stream)) != cudaSuccess) ||
-        (e = cudaMemsetAsync(h->old[i], 0, plane * cb, h->stream)) != cudaSuccess)
+  for (int i = 0; i < 3; ++i)
+    if ((e = cudaMemsetAsync(h->mom[i], 0, plane * cb, h->stream)) != cudaSuccess)
       return bail(fail(LBM_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
 
   lbm::Params& p = h->p;
@@ -866,7 +881,7 @@ int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout
   LBM_CUDA(h->ks->init(h->g, h->p, ds, ds + plane, h->pop[h->cur], h->mom[0], h->mom[1],
                        h->mom[2], h->stream));
   for (int i = 0; i < 6; ++i)
-    LBM_CUDA(cudaMemsetAsync(h->old[i], 0, plane * h->ks->compute_bytes, h->stream));
+    if (h->old[i]) LBM_CUDA(cudaMemsetAsync(h->old[i], 0, plane * h->ks->compute_bytes, h->stream));
   h->old_cur = 0;
   if (h->mov.n) {
     // registered obstacle state, static classes, then the obstacles placed,
@@ -951,6 +966,7 @@ int lbm_step_ex(LbmHandle* h, int64_t nsteps, int flags) {
                (flags & LBM_STEP_RESIDUAL ? lbm::F_RESIDUAL : 0);
   int64_t s = 0;
   int rc;
+  if ((flags & LBM_STEP_RESIDUAL) && (rc = h->ensure_old())) return rc;
   auto one = [&](int fl) {
     int r = h->step_full(fl);
     if (r) return r;
@@ -1009,13 +1025,7 @@ int lbm_adjoint_forward(LbmHandle* h, int64_t nsteps, int interval) {
   // (re)allocate the workspace when the plan changes
   if (!A.ready || A.interval != interval || (int64_t)A.ckpt.size() < nck) {
     for (auto* v : {&A.ckpt, &A.ckpt_side, &A.seg, &A.seg_side})
-      for (void* q : *v)
-        for (auto it = h->allocs.begin(); it != h->allocs.end(); ++it)
-          if (*it == q) {
-            cudaFree(q);
-            h->allocs.erase(it);
-            break;
-          }
+      for (void* q : *v) h->release(q);
     A.ckpt.assign(nck, nullptr);
     A.ckpt_side.assign(nck, nullptr);
     A.seg.assign(interval > 1 ? 2 * (interval - 1) : 0, nullptr);

@@ -120,3 +120,31 @@ def test_aa_rejections_on_handle():
         sim.initialize()
         with pytest.raises(capi.LbmError, match="AA population layout"):
             sim.adjoint_forward(4, 2)
+
+
+def test_device_bytes_accounting():
+    """The residual's previous-step fields are allocated by the first residual
+    step; freed and re-made workspaces (staging, adjoint plans) are counted
+    once."""
+    case = Case(load_golden("channel_cylinder_abb")[0])
+    with FluidLBM(case, storage="fp32_shifted") as sim:
+        sim.initialize()
+        b0 = sim.device_bytes
+        sim.step(2)
+        assert sim.device_bytes == b0
+        sim.step(1, residual=True)
+        b1 = sim.device_bytes
+        assert b1 > b0
+        sim.step(3, residual=True)
+        sim.populations()
+        b2 = sim.device_bytes
+        sim.populations()
+        assert sim.device_bytes == b2
+        sim.initialize()
+        sim.adjoint_forward(10, 2)
+        b3 = sim.device_bytes
+        sim.initialize()
+        sim.adjoint_forward(10, 3)
+        sim.initialize()
+        sim.adjoint_forward(10, 2)
+        assert sim.device_bytes == b3

@@ -413,9 +413,15 @@ struct LbmHandle {
   // advancing it) and keeps the fastest.
   int autotune() {
     tuned = true;
-    if (aa) return LBM_OK;   // in place: a trial launch would advance the state
     if (const char* f = std::getenv("LBM_VARIANT")) {
       int kind = -1, vec = 0, blk = 0, st = 0;
+      if (aa && std::sscanf(f, "%d,%d,%d,%d", &kind, &vec, &blk, &st) == 4) {
+        if (kind != 0 || vec != 1 || blk < 32 || blk > 256 || blk % 32)
+          return fail(LBM_ERR_ARG, std::string("LBM_VARIANT: the AA layout runs the scalar kernel "
+                                               "(0,1,block,stages) with 32 <= block <= 256: ") + f);
+        variant.block = blk;
+        return LBM_OK;
+      }
       if (std::sscanf(f, "%d,%d,%d,%d", &kind, &vec, &blk, &st) == 4) {
         for (int i = 0; i < ks->nvariants; ++i)
           if (ks->variants[i].kind == kind && ks->variants[i].vec == vec &&
@@ -428,6 +434,7 @@ struct LbmHandle {
         return fail(LBM_ERR_ARG, std::string("LBM_VARIANT does not name a candidate: ") + f);
       }
     }
+    if (aa) return LBM_OK;   // in place: a trial launch would advance the state
     variant = ks->variants[0];
     if (mov.n)
       for (int i = 0; i < ks->nvariants; ++i)
@@ -759,12 +766,12 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&h->err_dev), h->err_host, 0);
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaHostGetDevicePointer: ") + cudaGetErrorString(e)));
   h->variant = ks->variants[0];
-  if (aa) {   // the scalar kernel, 256 threads (its register cap is chosen per storage)
-    h->variant = lbm::Variant{0, 1, 256, c.precision == LBM_FP64 ? 0 : (c.collision == LBM_BGK ? 1 : 2)};
-    h->tuned = true;
+  if (aa) {   // the scalar kernel, 128 threads (its register cap is chosen per storage)
+    h->variant = lbm::Variant{0, 1, 128, c.precision == LBM_FP64 ? 0 : (c.collision == LBM_BGK ? 1 : 2)};
   }
   long long maxparts = ny;
   for (int i = 0; i < ks->nvariants; ++i) maxparts = std::max(maxparts, h->nparts_of(ks->variants[i]));
+  if (aa) maxparts = std::max(maxparts, h->nparts_of(lbm::Variant{0, 1, 32, 0}));   // smallest AA block
   if ((rc = h->alloc(reinterpret_cast<void**>(&h->partials), maxparts * 8 * sizeof(double))) ||
       (rc = h->alloc(reinterpret_cast<void**>(&h->red), 16 * sizeof(double))) ||
       (rc = h->alloc(reinterpret_cast<void**>(&h->scratch), lbm::kFinishBlocks * 8 * sizeof(double))))

@@ -126,7 +126,7 @@ def test_device_bytes_accounting():
     """The residual's previous-step fields are allocated by the first residual
     step; freed and re-made workspaces (staging, adjoint plans) are counted
     once."""
-    case = Case(load_golden("channel_cylinder_abb")[0])
+    case = Case(load_golden("cavity_lid_first")[0])
     with FluidLBM(case, storage="fp32_shifted") as sim:
         sim.initialize()
         b0 = sim.device_bytes

@@ -244,7 +244,7 @@ def run_gb300(args, world, rank, local):
             traffic = tr[key]["dram_bytes_per_launch"] * nodes / tr[key]["nodes"]
 
     # ---- end to end through the Python API, pinned host buffers -----------
-    e2e_steps = min(args.steps, 100)
+    e2e_steps = args.steps                          # the same K steps as the device-timed leg
     rho_h = torch.empty(case.density.shape, dtype=torch.float64, pin_memory=True).numpy()
     u_h = torch.empty(case.velocity.shape, dtype=torch.float64, pin_memory=True).numpy()
     rho_h[...] = case.density

@@ -635,24 +635,47 @@ __device__ __forceinline__ void node_outputs(const StepArgs& a, long long n, int
   }
 }
 
+// Warp sums of eight values in 9 shuffles instead of 8 x 5: a butterfly in
+// which every level halves the values a lane carries (4, 2, 1, then two
+// levels on the last one).  Lane l returns the warp sum of value
+// (l >> 2) & 7.  The pairing is fixed, so the sums are deterministic.
+template <class R>
+__device__ __forceinline__ R warp_sum8(const R v[8]) {
+  const int lane = threadIdx.x & 31;
+  const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+  R a4[4], a2[2];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const R send = b4 ? v[i] : v[i + 4];
+    const R keep = b4 ? v[i + 4] : v[i];
+    a4[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const R send = b3 ? a4[i] : a4[i + 2];
+    const R keep = b3 ? a4[i + 2] : a4[i];
+    a2[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+  R c = (b2 ? a2[1] : a2[0]) + __shfl_xor_sync(0xffffffffu, b2 ? a2[0] : a2[1], 4);
+  c += __shfl_xor_sync(0xffffffffu, c, 2);
+  c += __shfl_xor_sync(0xffffffffu, c, 1);
+  return c;
+}
+
 template <class T>
 __device__ __forceinline__ void block_residual(const StepArgs& a, T red[7]) {
   __shared__ double sh[32][8];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int i = 0; i < 7; ++i) {
-    const T v = warp_sum<T>(red[i]);
-    if (lane == 0) sh[wid][i] = double(v);
-  }
+  const T v[8] = {red[0], red[1], red[2], red[3], red[4], red[5], red[6], T(0)};
+  const T s = warp_sum8<T>(v);
+  if ((lane & 3) == 0) sh[wid][(lane >> 2) & 7] = double(s);
   __syncthreads();
-  if (threadIdx.x < 7) {
-    double s = 0;
+  if (threadIdx.x < 8) {
+    double t = 0;
     const int nw = blockDim.x >> 5;
-    for (int w = 0; w < nw; ++w) s += sh[w][threadIdx.x];
-    a.partials[((long long)blockIdx.y * gridDim.x + blockIdx.x) * 8 + threadIdx.x] = s;
+    for (int w = 0; w < nw; ++w) t += sh[w][threadIdx.x];
+    a.partials[((long long)blockIdx.y * gridDim.x + blockIdx.x) * 8 + threadIdx.x] = t;
   }
-  if (threadIdx.x == 7)
-    a.partials[((long long)blockIdx.y * gridDim.x + blockIdx.x) * 8 + 7] = 0.0;
 }
 
 // ---------------------------------------------------------------------------

@@ -208,6 +208,7 @@ def run_gb300(args, world, rank, local):
     sim = FluidLBM(case, device=device)
     sim.initialize()
     sim.step(args.warmup)
+    sim.step(1, residual=True)            # warms the residual step of the end-to-end leg
     sim.synchronize()
 
     def barrier():

@@ -89,6 +89,26 @@ struct Kernels {
   static dim3 node_grid(const Geom& g) {
     return dim3((g.nx + kStepBlock - 1) / kStepBlock, g.ny);
   }
+  // The scalar kernel with or without the residual's code.
+  template <int COLL, int FORC, bool RES>
+  static cudaError_t scalar(const StepArgs& a, Variant v, dim3 grid, cudaStream_t s) {
+    if (a.rho_dyn_out) {   // moving obstacles: the uncapped scalar kernel only
+      if (v.stages != 0) return cudaErrorInvalidValue;
+      step_kernel<S, COLL, FORC, 0, true, RES><<<grid, v.block, 0, s>>>(a);
+      return cudaGetLastError();
+    }
+    if (v.stages == 1 || v.stages == 2) {
+      if (v.block > 256) return cudaErrorInvalidValue;
+      if (v.stages == 1)
+        step_kernel<S, COLL, FORC, 1, false, RES><<<grid, v.block, 0, s>>>(a);
+      else
+        step_kernel<S, COLL, FORC, 2, false, RES><<<grid, v.block, 0, s>>>(a);
+    } else {
+      step_kernel<S, COLL, FORC, 0, false, RES><<<grid, v.block, 0, s>>>(a);
+    }
+    return cudaGetLastError();
+  }
+
   template <int COLL, int FORC>
   static cudaError_t step_t(const StepArgs& a, Variant v, int sms, cudaStream_t s) {
     const dim3 grid = step_grid(a.g, v, sms, sizeof(S));
@@ -127,21 +147,8 @@ struct Kernels {
       }
     }
     if (v.kind != 0) return cudaErrorInvalidValue;
-    if (a.rho_dyn_out) {   // moving obstacles: the uncapped scalar kernel only
-      if (v.stages != 0) return cudaErrorInvalidValue;
-      step_kernel<S, COLL, FORC, 0, true><<<grid, v.block, 0, s>>>(a);
-      return cudaGetLastError();
-    }
-    if (v.stages == 1 || v.stages == 2) {
-      if (v.block > 256) return cudaErrorInvalidValue;
-      if (v.stages == 1)
-        step_kernel<S, COLL, FORC, 1><<<grid, v.block, 0, s>>>(a);
-      else
-        step_kernel<S, COLL, FORC, 2><<<grid, v.block, 0, s>>>(a);
-    } else {
-      step_kernel<S, COLL, FORC, 0><<<grid, v.block, 0, s>>>(a);
-    }
-    return cudaGetLastError();
+    if (a.flags & F_RESIDUAL) return scalar<COLL, FORC, true>(a, v, grid, s);
+    return scalar<COLL, FORC, false>(a, v, grid, s);
   }
   static cudaError_t step(int coll, int forc, const StepArgs& a, Variant v, int sms,
                           cudaStream_t s) {

@@ -76,6 +76,8 @@ struct LbmHandle {
   cudaGraphExec_t gexec = nullptr;
   int gparity = 0;
   lbm::Variant variant{0, 1, 256, 0};
+  lbm::Variant res_variant{0, 1, 256, 0};   // shape of residual steps (tuned on the first)
+  bool res_tuned = false;
   int sms = 1;                 // multiprocessors of the device
   int* err_host = nullptr;     // mapped pinned word the kernels set on a failed wait
   int* err_dev = nullptr;
@@ -233,7 +235,45 @@ struct LbmHandle {
 
   // One fused step launch; advance=false leaves the state untouched (the
   // kernel only writes the other population buffer and side array).
-  int launch(int flags, bool advance = true) { return launch_v(flags, variant, advance); }
+  int launch(int flags, bool advance = true) {
+    return launch_v(flags, (flags & lbm::F_RESIDUAL) && res_tuned ? res_variant : variant, advance);
+  }
+
+  // Shape of residual steps: a residual step runs the scalar kernel's
+  // residual instantiation, whose best shape can differ from the plain
+  // step's.  Times every scalar candidate on the live state without
+  // advancing it (the other population buffer, side array and the residual's
+  // output set are written, all rewritten by the real step).
+  int tune_residual() {
+    res_tuned = true;
+    res_variant = variant;
+    if (aa || std::getenv("LBM_VARIANT")) return LBM_OK;
+    const char* t = std::getenv("LBM_TUNE");
+    if (t && t[0] == '0') return LBM_OK;
+    cudaEvent_t e0, e1;
+    LBM_CUDA(cudaEventCreate(&e0));
+    LBM_CUDA(cudaEventCreate(&e1));
+    double best = 1e30;
+    int rc = LBM_OK;
+    for (int pass = 0; pass < 2 && rc == LBM_OK; ++pass)
+      for (int i = 0; i < ks->nvariants && rc == LBM_OK; ++i) {
+        const lbm::Variant v = ks->variants[i];
+        if (v.kind != 0 || (mov.n && v.stages != 0)) continue;
+        if ((rc = launch_v(lbm::F_RESIDUAL, v, false))) break;
+        cudaEventRecord(e0, stream);
+        for (int r = 0; r < 4 && rc == LBM_OK; ++r) rc = launch_v(lbm::F_RESIDUAL, v, false);
+        cudaEventRecord(e1, stream);
+        if (rc == LBM_OK) rc = wait();
+        float ms = 0.f;
+        if (rc == LBM_OK && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms < best) {
+          best = ms;
+          res_variant = v;
+        }
+      }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+  }
 
   int launch_v(int flags, lbm::Variant v, bool advance) {
     const int rc = launch_bufs(flags, v, pop[cur], pop[cur ^ 1], side[cur], side[cur ^ 1], nullptr,
@@ -1005,11 +1045,13 @@ int lbm_step_ex(LbmHandle* h, int64_t nsteps, int flags) {
     --plain;
   }
   if (s < nsteps) {
+    if ((kflags & lbm::F_RESIDUAL) && !h->res_tuned && h->tuned && (rc = h->tune_residual())) return rc;
     if ((rc = one(kflags))) return rc;
   }
   if (flags & LBM_STEP_MOMENTS) h->has_moments = true;
   if (flags & LBM_STEP_RESIDUAL) {
-    LBM_CUDA(lbm::finish_reduce(h->partials, h->nparts_of(h->variant), h->scratch, h->red, h->stream));
+    const lbm::Variant rv = h->res_tuned ? h->res_variant : h->variant;
+    LBM_CUDA(lbm::finish_reduce(h->partials, h->nparts_of(rv), h->scratch, h->red, h->stream));
     LBM_CUDA(cudaMemcpyAsync(h->host_red, h->red, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     h->has_residual = true;
   }
@@ -1470,6 +1512,7 @@ int lbm_set_moving_obstacles(LbmHandle* h, const LbmMovingObstacle* obs, int n,
       break;
     }
   h->tuned = false;
+  h->res_tuned = false;
   if (h->gexec) {
     cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;

@@ -601,9 +601,23 @@ __device__ __forceinline__ void dynamic_links(typename Store<S>::T f[9], const S
 // residual terms are formed in the compute type T (FP32 for shifted storage:
 // GB300's FP64 rate is a small fraction of its FP32 rate) and summed in FP64
 // per block.
+// The residual's previous-step fields of node n.
 template <class T>
+__device__ __forceinline__ void load_old(const StepArgs& a, long long n, T o[3]) {
+  o[0] = static_cast<const T*>(a.rho_old)[n];
+  o[1] = static_cast<const T*>(a.ux_old)[n];
+  o[2] = static_cast<const T*>(a.uy_old)[n];
+}
+
+// RES: residual terms when the step's flags ask (RES_FLAG), never (RES_OFF),
+// or always with the previous-step fields already loaded in `pre` (RES_ON:
+// the scalar kernel's residual instantiation issues those loads with the
+// populations', so that their latency overlaps).
+enum { RES_FLAG = 0, RES_OFF = 1, RES_ON = 2 };
+
+template <class T, int RES = RES_FLAG>
 __device__ __forceinline__ void node_outputs(const StepArgs& a, long long n, int r, T rho,
-                                             T ux, T uy, T red[7]) {
+                                             T ux, T uy, T red[7], const T* pre = nullptr) {
   if (r >= 0) {
     T* side = static_cast<T*>(a.side_out);
     side[3 * r] = rho;
@@ -615,13 +629,17 @@ __device__ __forceinline__ void node_outputs(const StepArgs& a, long long n, int
     static_cast<T*>(a.ux)[n] = ux;
     static_cast<T*>(a.uy)[n] = uy;
   }
-  if (a.flags & F_RESIDUAL) {
+  if (RES == RES_ON || (RES == RES_FLAG && (a.flags & F_RESIDUAL))) {
     // compute_residues_kernels.py:6-73: sums over fluid nodes
-    const T* ro = static_cast<const T*>(a.rho_old);
-    const T* xo = static_cast<const T*>(a.ux_old);
-    const T* yo = static_cast<const T*>(a.uy_old);
+    T o[3];
+    if (RES == RES_ON) {
+      o[0] = pre[0];
+      o[1] = pre[1];
+      o[2] = pre[2];
+    } else {
+      load_old<T>(a, n, o);
+    }
     const T v[3] = {rho, ux, uy};
-    const T o[3] = {ro[n], xo[n], yo[n]};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const T d = v[c] - o[c];
@@ -681,7 +699,7 @@ __device__ __forceinline__ void block_residual(const StepArgs& a, T red[7]) {
 // ---------------------------------------------------------------------------
 // One node of the scalar kernel.  MOV: the case has moving obstacles
 // (class-4 nodes, the density kept for their bounce-back).
-template <class S, int COLL, int FORC, bool MOV>
+template <class S, int COLL, int FORC, bool MOV, bool RES>
 __device__ __forceinline__ void step_node(const StepArgs& a, int x, int y,
                                           typename Store<S>::T red[7]) {
   using T = typename Store<S>::T;
@@ -697,6 +715,8 @@ __device__ __forceinline__ void step_node(const StepArgs& a, int x, int y,
   const bool seg = g.segflag[y * g.nseg + (x >> 5)] != 0;
   if (seg) cls = g.cls[ni];
   if (cls == 2) return;
+  T old[3];
+  if (RES) load_old<T>(a, n, old);
   T f[9];
   int r = -1;
   if (cls == 1) r = g.recmap[ni];
@@ -722,23 +742,24 @@ __device__ __forceinline__ void step_node(const StepArgs& a, int x, int y,
   // moving obstacle are flagged a step before their nodes can enter class 4,
   // whose bounce-back then reads it
   if (MOV && seg) static_cast<T*>(a.rho_dyn_out)[ni] = rho;
-  node_outputs<T>(a, n, r, rho, ux, uy, red);
+  node_outputs<T, RES ? RES_ON : RES_OFF>(a, n, r, rho, ux, uy, red, old);
 }
 
 // Scalar kernel: one node per thread.  Used for FP64 (whose cost is its FP64
 // arithmetic, not memory) and as an autotuner candidate.
 // CAP = 1 asks for 8 resident blocks of 256 threads (at most 32 registers),
 // CAP = 2 for 6 (at most 40 registers; for the MRT collision).  MOV = true
-// (moving obstacles) is instantiated uncapped only.
-template <class S, int COLL, int FORC, int CAP, bool MOV = false>
+// (moving obstacles) is instantiated uncapped only.  RES: the step evaluates
+// the residual (F_RESIDUAL); the plain instantiation carries none of its code.
+template <class S, int COLL, int FORC, int CAP, bool MOV, bool RES>
 __global__ void __launch_bounds__(CAP ? 256 : 512, CAP == 1 ? 8 : (CAP == 2 ? 6 : 1))
     step_kernel(const StepArgs a) {
   using T = typename Store<S>::T;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   T red[7] = {0, 0, 0, 0, 0, 0, 0};
-  if (x < a.g.nx) step_node<S, COLL, FORC, MOV>(a, x, y, red);
-  if (a.flags & F_RESIDUAL) block_residual<decltype(red[0] + 0)>(a, red);
+  if (x < a.g.nx) step_node<S, COLL, FORC, MOV, RES>(a, x, y, red);
+  if (RES) block_residual<decltype(red[0] + 0)>(a, red);
 }
 
 // ---------------------------------------------------------------------------

@@ -79,6 +79,7 @@ struct LbmHandle {
   lbm::Variant res_variant{0, 1, 256, 0};   // shape of residual steps (tuned on the first)
   bool res_tuned = false;
   int sms = 1;                 // multiprocessors of the device
+  bool host_link = false;      // kernels may read / write the caller's pinned buffers directly
   int* err_host = nullptr;     // mapped pinned word the kernels set on a failed wait
   int* err_dev = nullptr;
   bool tuned = false;
@@ -226,6 +227,23 @@ struct LbmHandle {
     if (rc) return rc;
     stage_elems = elems;
     return LBM_OK;
+  }
+
+  // Device address of a caller's pinned (page-locked or registered) host
+  // buffer, which the transposing copy kernels then read or write directly
+  // over the host link: one pass instead of a copy into a staging buffer and
+  // a second pass.  Only where the device can also reach pageable memory
+  // (Grace-Blackwell's coherent link), so that any host address it is given
+  // stays reachable.  nullptr: stage through a copy.
+  template <class P>
+  P* host_direct(P* q) const {
+    if (!host_link) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost && at.devicePointer ? static_cast<P*>(at.devicePointer) : nullptr;
   }
 
   long long host_nodes(int layout) const {
@@ -800,6 +818,16 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
     if ((rc = h->alloc(&h->mom[i], plane * cb))) return bail(rc);
   e = cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, c.device);
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("device attribute: ") + cudaGetErrorString(e)));
+  {
+    int pageable = 0, same_va = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, c.device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&same_va, cudaDevAttrCanUseHostPointerForRegisteredMem, c.device) != cudaSuccess) {
+      cudaGetLastError();
+      pageable = same_va = 0;
+    }
+    const char* st = std::getenv("LBM_HOST_DIRECT");
+    h->host_link = pageable == 1 && same_va == 1 && st && st[0] == '1';
+  }
   e = cudaHostAlloc(reinterpret_cast<void**>(&h->err_host), sizeof(int), cudaHostAllocMapped);
   if (e != cudaSuccess) return bail(fail(LBM_ERR_ALLOC, std::string("cudaHostAlloc: ") + cudaGetErrorString(e)));
   *h->err_host = 0;
@@ -909,15 +937,23 @@ int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout
     return fail(LBM_ERR_ARG, "lbm_init_fields: unknown layout");
   LBM_CUDA(cudaSetDevice(h->cfg.device));
   const long long nh = h->host_nodes(layout), plane = h->g.plane;
-  int rc = h->ensure_stage(3 * nh + 3 * plane);
+  const double* rd = h->host_direct(rho);
+  const double* ud = h->host_direct(u);
+  const bool direct = rd && ud;
+  int rc = h->ensure_stage(direct ? 3 * plane : 3 * nh + 3 * plane);
   if (rc) return rc;
-  double* hs = h->stage;           // host order: rho [nh], u [nh][2]
-  double* ds = h->stage + 3 * nh;  // device order: rho [plane], u [2][plane]
-  LBM_CUDA(cudaMemcpyAsync(hs, rho, nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  LBM_CUDA(cudaMemcpyAsync(hs + nh, u, 2 * nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  double* ds = h->stage + (direct ? 0 : 3 * nh);   // device order: rho [plane], u [2][plane]
   LBM_CUDA(cudaMemsetAsync(ds, 0, 3 * plane * sizeof(double), h->stream));
-  LBM_CUDA(lbm::reorder(h->g, hs, ds, 1, layout, 1, h->stream));
-  LBM_CUDA(lbm::reorder(h->g, hs + nh, ds + plane, 2, layout, 1, h->stream));
+  if (direct) {   // transposed straight from the caller's pinned buffers
+    LBM_CUDA(lbm::reorder(h->g, rd, ds, 1, layout, 1, h->stream));
+    LBM_CUDA(lbm::reorder(h->g, ud, ds + plane, 2, layout, 1, h->stream));
+  } else {
+    double* hs = h->stage;   // host order: rho [nh], u [nh][2]
+    LBM_CUDA(cudaMemcpyAsync(hs, rho, nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    LBM_CUDA(cudaMemcpyAsync(hs + nh, u, 2 * nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    LBM_CUDA(lbm::reorder(h->g, hs, ds, 1, layout, 1, h->stream));
+    LBM_CUDA(lbm::reorder(h->g, hs + nh, ds + plane, 2, layout, 1, h->stream));
+  }
   if (h->mov.n) {   // static classes back before f_eq is written (a run may have moved obstacles)
     LBM_CUDA(cudaMemcpyAsync(const_cast<uint8_t*>(h->g.cls), h->mov.cls_static, plane,
                              cudaMemcpyDeviceToDevice, h->stream));
@@ -1266,6 +1302,17 @@ int lbm_get_moments(LbmHandle* h, double* rho, double* u, int layout) {
   if (!h->has_moments) return fail(LBM_ERR_STATE, "lbm_get_moments: no moments recorded (use LBM_STEP_MOMENTS)");
   LBM_CUDA(cudaSetDevice(h->cfg.device));
   const long long nh = h->host_nodes(layout), plane = h->g.plane;
+  double* rd = layout == LBM_LAYOUT_INNER ? h->host_direct(rho) : nullptr;
+  double* ud = layout == LBM_LAYOUT_INNER ? h->host_direct(u) : nullptr;
+  if (rd && ud) {   // transposed straight into the caller's pinned buffers
+    int rc = h->ensure_stage(3 * plane);
+    if (rc) return rc;
+    double* ds = h->stage;
+    LBM_CUDA(h->ks->moments_to_f64(h->g, h->mom[0], h->mom[1], h->mom[2], ds, h->stream));
+    LBM_CUDA(lbm::reorder(h->g, ds, rd, 1, layout, 0, h->stream));
+    LBM_CUDA(lbm::reorder(h->g, ds + plane, ud, 2, layout, 0, h->stream));
+    return h->wait();
+  }
   int rc = h->ensure_stage(3 * nh + 3 * plane);
   if (rc) return rc;
   double* hs = h->stage;

@@ -1241,22 +1241,31 @@ __global__ void init_kernel(const Geom g, const Params p, const double* __restri
     for (int k = 0; k < 9; ++k) Store<S>::st(f, k * g.plane + n, T(0), p);
     return;
   }
-  const double hu2 = p.half_inv_cs_2 * (ux * ux + uy * uy);
+  if constexpr (Store<S>::shifted) {
+    // g_eq = f_eq - w without cancellation: w (r e - 1) = w ((r - 1) + r (e - 1)),
+    // in FP32 (D2Q9 constants) from r - 1 formed in FP64: GB300's FP64 rate
+    // made the FP64 form 2 ms at 8192 x 2048, ten times the memory time, for a
+    // value that is rounded to FP32 (or FP16) anyway.
+    const float dr = float(r - 1.0), rf = float(r), fx = float(ux), fy = float(uy);
+    const float hu2 = 1.5f * (fx * fx + fy * fy);
 #pragma unroll
-  for (int k = 0; k < 9; ++k) {
-    const int cx = CXk(k), cy = CYk(k);
-    double cu = 0.0;
-    if (cx != 0 && cy != 0) cu = (cx > 0 ? ux : -ux) + (cy > 0 ? uy : -uy);
-    else if (cx != 0) cu = cx > 0 ? ux : -ux;
-    else if (cy != 0) cu = cy > 0 ? uy : -uy;
-    double e = (cx == 0 && cy == 0) ? 1.0 - hu2
-                                    : ((1.0 + p.inv_cs_2 * cu) + (p.half_inv_cs_4 * cu) * cu) - hu2;
-    if (Store<S>::shifted) {
-      // g_eq = f_eq - w computed without cancellation: w (r e - 1) = w ((r - 1) + r (e - 1))
-      const double em1 = (cx == 0 && cy == 0) ? -hu2
-                                              : (p.inv_cs_2 * cu + (p.half_inv_cs_4 * cu) * cu) - hu2;
-      Store<S>::st(f, k * g.plane + n, T(Wk(k) * ((r - 1.0) + r * em1)), p);
-    } else {
+    for (int k = 0; k < 9; ++k) {
+      const float cu = lin2r<float>(CXk(k), CYk(k), fx, fy);
+      const float em1 = k == 0 ? -hu2 : fmaf(cu, fmaf(4.5f, cu, 3.f), -hu2);
+      Store<S>::st(f, k * g.plane + n, T(float(Wk(k)) * fmaf(rf, em1, dr)), p);
+    }
+  } else {
+    // equilibrium_kernels.py:6-35, the reference's operation order
+    const double hu2 = p.half_inv_cs_2 * (ux * ux + uy * uy);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const int cx = CXk(k), cy = CYk(k);
+      double cu = 0.0;
+      if (cx != 0 && cy != 0) cu = (cx > 0 ? ux : -ux) + (cy > 0 ? uy : -uy);
+      else if (cx != 0) cu = cx > 0 ? ux : -ux;
+      else if (cy != 0) cu = cy > 0 ? uy : -uy;
+      const double e = (cx == 0 && cy == 0) ? 1.0 - hu2
+                                            : ((1.0 + p.inv_cs_2 * cu) + (p.half_inv_cs_4 * cu) * cu) - hu2;
       Store<S>::st(f, k * g.plane + n, T((Wk(k) * r) * e), p);
     }
   }

@@ -37,28 +37,52 @@ cudaError_t finish_reduce(const double* partials, long long nrows, double* scrat
   return cudaGetLastError();
 }
 
+// Host order <-> device order, as a tiled transpose: host arrays are x-major
+// (consecutive y contiguous), device planes y-major (consecutive x
+// contiguous).  A 32 x 32 tile passes through shared memory, so both sides
+// are read and written in contiguous runs; the host side may be the caller's
+// pinned buffer itself, read or written over the host link.
 // layout 0: inner ind = x*ny + y ; 1: padded ind = (x+1)*(ny+2) + (y+1)
-__global__ void reorder_kernel(const Geom g, const double* __restrict__ in,
-                               double* __restrict__ out, int ncomp, int layout,
-                               int to_device) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y;
-  if (x >= g.nx) return;
-  const long long hn = layout == 0 ? (long long)x * g.ny + y
-                                   : (long long)(x + 1) * (g.ny + 2) + (y + 1);
-  const long long dn = g.node(x, y);
+constexpr int kTile = 32, kTileRows = 8;
+
+__global__ void __launch_bounds__(kTile * kTileRows)
+    reorder_kernel(const Geom g, const double* __restrict__ in, double* __restrict__ out,
+                   int ncomp, int layout, int to_device) {
+  __shared__ double t[kTile][kTile + 1];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile;
+  const long long hy = layout == 0 ? g.ny : g.ny + 2;   // host stride of x
+  const int off = layout == 0 ? 0 : 1;
   for (int c = 0; c < ncomp; ++c) {
-    if (to_device)
-      out[c * g.plane + dn] = in[hn * ncomp + c];
-    else
-      out[hn * ncomp + c] = in[c * g.plane + dn];
+    if (to_device) {
+      for (int r = ty; r < kTile; r += kTileRows) {   // host rows: x = x0 + r, lanes along y
+        const int x = x0 + r, y = y0 + tx;
+        if (x < g.nx && y < g.ny) t[r][tx] = in[((x + off) * hy + y + off) * ncomp + c];
+      }
+      __syncthreads();
+      for (int r = ty; r < kTile; r += kTileRows) {   // device rows: y = y0 + r, lanes along x
+        const int x = x0 + tx, y = y0 + r;
+        if (x < g.nx && y < g.ny) out[c * g.plane + g.node(x, y)] = t[tx][r];
+      }
+    } else {
+      for (int r = ty; r < kTile; r += kTileRows) {
+        const int x = x0 + tx, y = y0 + r;
+        if (x < g.nx && y < g.ny) t[r][tx] = in[c * g.plane + g.node(x, y)];
+      }
+      __syncthreads();
+      for (int r = ty; r < kTile; r += kTileRows) {
+        const int x = x0 + r, y = y0 + tx;
+        if (x < g.nx && y < g.ny) out[((x + off) * hy + y + off) * ncomp + c] = t[tx][r];
+      }
+    }
+    __syncthreads();
   }
 }
 
 cudaError_t reorder(const Geom& g, const double* in, double* out, int ncomp,
                     int layout, int to_device, cudaStream_t s) {
-  dim3 grid((g.nx + kStepBlock - 1) / kStepBlock, g.ny);
-  reorder_kernel<<<grid, kStepBlock, 0, s>>>(g, in, out, ncomp, layout, to_device);
+  dim3 grid((g.nx + kTile - 1) / kTile, (g.ny + kTile - 1) / kTile);
+  reorder_kernel<<<grid, dim3(kTile, kTileRows), 0, s>>>(g, in, out, ncomp, layout, to_device);
   return cudaGetLastError();
 }
 

@@ -43,7 +43,8 @@ __device__ __forceinline__ long long mov_off(const Geom& g, int k) {
   return (long long)CYk(k) * g.pitch + CXk(k);
 }
 
-// f_eq(r, u) of node n into storage (init_kernel's arithmetic).
+// f_eq(r, u) of node n into storage, formed in FP64 (init_kernel's FP64 form;
+// a refill touches a few nodes per step).
 template <class S>
 __device__ __forceinline__ void store_feq(const Geom& g, const Params& p, S* f, long long n,
                                           double r, double ux, double uy) {

@@ -1,0 +1,69 @@
+"""Host transfers: by default a staging copy and a transposing kernel; with
+LBM_HOST_DIRECT=1 the transposing kernels read and write pinned caller
+buffers directly over the host link (where the device can reach host memory).
+All routes must give the same bits."""
+import numpy as np
+import pytest
+import torch
+
+from _golden import load_golden
+from pylabolt_gb300 import capi, workloads
+from pylabolt_gb300.config import Case
+from pylabolt_gb300.lbm import FluidLBM
+
+pytestmark = pytest.mark.gpu
+
+
+def _pinned(a):
+    t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+    t[...] = a
+    return t
+
+
+@pytest.mark.parametrize("storage", ["fp64", "fp32_shifted"])
+@pytest.mark.parametrize("shape", [(200, 97), (64, 64)])
+def test_pinned_and_pageable_routes_agree(storage, shape, monkeypatch):
+    nx, ny = shape
+    case = Case(workloads.cylinder(nx=nx, ny=ny, radius=8.0, center=(nx // 4, ny // 2 + 1)))
+    rng = np.random.default_rng(5)
+    rho = 1.0 + 1e-3 * rng.standard_normal((nx, ny))
+    u = 1e-3 * rng.standard_normal((nx, ny, 2))
+    out = {}
+    for route in ("pageable", "pinned", "direct"):
+        if route == "direct":
+            monkeypatch.setenv("LBM_HOST_DIRECT", "1")
+        with FluidLBM(case, storage=storage) as sim:
+            if route == "pageable":
+                sim.initialize(rho, u)
+            else:
+                sim.initialize(_pinned(rho), _pinned(u))
+            sim.step(7, moments=True)
+            if route == "pageable":
+                r, v = sim.moments()
+            else:
+                r, v = sim.moments(out=(_pinned(np.zeros(nx * ny)), _pinned(np.zeros((nx * ny, 2)))))
+            rp, vp = sim.moments(layout=capi.LAYOUT_PADDED)
+            out[route] = (r.copy(), v.copy(), rp, vp, sim.populations())
+    for route in ("pinned", "direct"):
+        for a, b in zip(out[route], out["pageable"]):
+            assert np.array_equal(a, b), route
+
+
+def test_padded_initial_fields_pinned():
+    case_d, d = load_golden("channel_cylinder_abb")
+    case = Case(case_d)
+    nx, ny = case.nx, case.ny
+    rho_p = np.zeros((nx + 2) * (ny + 2))
+    u_p = np.zeros(((nx + 2) * (ny + 2), 2))
+    inner = np.zeros((nx + 2, ny + 2), bool)
+    inner[1:-1, 1:-1] = True
+    rho_p[inner.ravel()] = case.density.ravel()
+    u_p[inner.ravel()] = case.velocity.reshape(-1, 2)
+    with FluidLBM(case, storage="fp64") as a, FluidLBM(case, storage="fp64") as b:
+        a.initialize()
+        check = capi.check
+        check(b.lib.lbm_init_fields(b.h, capi.ptr(_pinned(rho_p)), capi.ptr(_pinned(u_p)),
+                                    capi.LAYOUT_PADDED))
+        a.step(5)
+        b.step(5)
+        assert np.array_equal(a.populations(), b.populations())

@@ -260,8 +260,8 @@ typedef struct {
 
 /* Registers the moving obstacles (at most 32) and the gravity of their
  * motion; call after lbm_create.  lbm_init_fields must follow before the next
- * step (it places them).  Only the uncapped scalar step kernel serves a case
- * with moving obstacles. */
+ * step (it places them).  Only the scalar step kernel serves a case with
+ * moving obstacles. */
 int lbm_set_moving_obstacles(LbmHandle* h, const LbmMovingObstacle* obs, int n,
                              const double gravity[2]);
 

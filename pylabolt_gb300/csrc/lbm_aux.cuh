@@ -92,9 +92,15 @@ struct Kernels {
   // The scalar kernel with or without the residual's code.
   template <int COLL, int FORC, bool RES>
   static cudaError_t scalar(const StepArgs& a, Variant v, dim3 grid, cudaStream_t s) {
-    if (a.rho_dyn_out) {   // moving obstacles: the uncapped scalar kernel only
-      if (v.stages != 0) return cudaErrorInvalidValue;
-      step_kernel<S, COLL, FORC, 0, true, RES><<<grid, v.block, 0, s>>>(a);
+    if (a.rho_dyn_out) {   // moving obstacles: the scalar kernel's MOV instantiations
+      if (v.stages == 0)
+        step_kernel<S, COLL, FORC, 0, true, RES><<<grid, v.block, 0, s>>>(a);
+      else if (v.stages == 1 && v.block <= 256)
+        step_kernel<S, COLL, FORC, 1, true, RES><<<grid, v.block, 0, s>>>(a);
+      else if (v.stages == 2 && v.block <= 256)
+        step_kernel<S, COLL, FORC, 2, true, RES><<<grid, v.block, 0, s>>>(a);
+      else
+        return cudaErrorInvalidValue;
       return cudaGetLastError();
     }
     if (v.stages == 1 || v.stages == 2) {

@@ -276,7 +276,7 @@ struct LbmHandle {
     for (int pass = 0; pass < 2 && rc == LBM_OK; ++pass)
       for (int i = 0; i < ks->nvariants && rc == LBM_OK; ++i) {
         const lbm::Variant v = ks->variants[i];
-        if (v.kind != 0 || (mov.n && v.stages != 0)) continue;
+        if (v.kind != 0) continue;
         if ((rc = launch_v(lbm::F_RESIDUAL, v, false))) break;
         cudaEventRecord(e0, stream);
         for (int r = 0; r < 4 && rc == LBM_OK; ++r) rc = launch_v(lbm::F_RESIDUAL, v, false);
@@ -484,8 +484,8 @@ struct LbmHandle {
         for (int i = 0; i < ks->nvariants; ++i)
           if (ks->variants[i].kind == kind && ks->variants[i].vec == vec &&
               ks->variants[i].block == blk && ks->variants[i].stages == st) {
-            if (mov.n && (kind != 0 || st != 0))
-              return fail(LBM_ERR_ARG, "LBM_VARIANT: moving obstacles need the uncapped scalar kernel (kind 0, stages 0)");
+            if (mov.n && kind != 0)
+              return fail(LBM_ERR_ARG, "LBM_VARIANT: moving obstacles need the scalar kernel (kind 0)");
             variant = ks->variants[i];
             return LBM_OK;
           }
@@ -510,7 +510,7 @@ struct LbmHandle {
     int rc = LBM_OK;
     for (int i = 0; i < ks->nvariants && rc == LBM_OK; ++i) {
       const lbm::Variant v = ks->variants[i];
-      if (mov.n && (v.kind != 0 || v.stages != 0)) {   // class-4 links: the uncapped scalar kernel only
+      if (mov.n && v.kind != 0) {   // class-4 links: the scalar kernel only
         tune_ms[i] = 1e30;
         continue;
       }

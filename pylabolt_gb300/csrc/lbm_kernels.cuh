@@ -748,9 +748,10 @@ __device__ __forceinline__ void step_node(const StepArgs& a, int x, int y,
 // Scalar kernel: one node per thread.  Used for FP64 (whose cost is its FP64
 // arithmetic, not memory) and as an autotuner candidate.
 // CAP = 1 asks for 8 resident blocks of 256 threads (at most 32 registers),
-// CAP = 2 for 6 (at most 40 registers; for the MRT collision).  MOV = true
-// (moving obstacles) is instantiated uncapped only.  RES: the step evaluates
-// the residual (F_RESIDUAL); the plain instantiation carries none of its code.
+// CAP = 2 for 6 (at most 40 registers; for the MRT collision).  MOV = true:
+// the case has moving obstacles (a separate instantiation, so that cases
+// without them run the plain body).  RES: the step evaluates the residual
+// (F_RESIDUAL); the plain instantiation carries none of its code.
 template <class S, int COLL, int FORC, int CAP, bool MOV, bool RES>
 __global__ void __launch_bounds__(CAP ? 256 : 512, CAP == 1 ? 8 : (CAP == 2 ? 6 : 1))
     step_kernel(const StepArgs a) {

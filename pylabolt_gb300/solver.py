@@ -40,14 +40,15 @@ def _next_multiple(t, interval):
 class Solver:
     """One fluidLB run on one GPU.  `simulation`: the ``simulation`` module
     (or a dict with its dictionaries); `root`: directory that receives
-    ``metadata.json`` and ``output/``."""
+    ``metadata.json`` and ``output/``; `storage` / `layout` override
+    ``control_dict["storage"]`` / ``["population_layout"]``."""
 
-    def __init__(self, simulation, root=".", storage=None, device=0, verbose=True):
+    def __init__(self, simulation, root=".", storage=None, device=0, verbose=True, layout=None):
         self.verbose = verbose
         self.case = Case(simulation)
         self.geometry = Geometry(self.case)
         self.out = Output(self.case, self.geometry, root)
-        self.lbm = FluidLBM(self.case, storage=storage, device=device)
+        self.lbm = FluidLBM(self.case, storage=storage, device=device, layout=layout)
         nobs = len(self.case.obstacles)
         self.nobs = nobs
         self.residues = None

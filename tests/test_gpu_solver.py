@@ -34,10 +34,11 @@ def _numbers(text):
     return np.array([float(v) for v in re.findall(r"-?\d\.\d+e[+-]\d+", text)])
 
 
-def test_solver_run_matches_reference_output(tmp_path, monkeypatch, capsys):
+@pytest.mark.parametrize("layout", ["ab", "aa"])
+def test_solver_run_matches_reference_output(tmp_path, monkeypatch, capsys, layout):
     case, d, _ = _io_case()
     monkeypatch.setattr(output, "package_version", lambda: str(d["version"]))
-    s = solver.Solver(case, root=str(tmp_path), storage="fp64")
+    s = solver.Solver(case, root=str(tmp_path), storage="fp64", layout=layout)
     try:
         s.run()
     finally:

@@ -30,7 +30,7 @@ def _io():
 class GoldenLBM:
     """Stands in for FluidLBM: replays the golden values of the time reached."""
 
-    def __init__(self, case, storage=None, device=0):
+    def __init__(self, case, storage=None, device=0, layout=None):
         self.case = case
         _, self.d, self.g = _io()
         self.t = 0

@@ -704,13 +704,16 @@ __device__ __forceinline__ void step_node(const StepArgs& a, int x, int y,
                                           typename Store<S>::T red[7]) {
   using T = typename Store<S>::T;
   const Geom& g = a.g;
-  // 32-bit node index (plane < 2^31 is checked at create) with per-plane
-  // base pointers (uniform): one wide multiply-add per access instead of
-  // 64-bit index arithmetic
+  // 32-bit node index (plane < 2^31 is checked at create).  The bulk pulls
+  // and the stores address from this node's element of plane 0 with
+  // warp-uniform 64-bit offsets (k * plane - c_k . (1, pitch)): one 64-bit add
+  // per access.
   const int ni = (y + 1) * g.pitch + x;
   const long long n = ni;
   const S* __restrict__ fin = static_cast<const S*>(a.fin);
   S* __restrict__ fout = static_cast<S*>(a.fout);
+  const S* __restrict__ fn = fin + ni;
+  S* __restrict__ on = fout + ni;
   int cls = 0;
   const bool seg = g.segflag[y * g.nseg + (x >> 5)] != 0;
   if (seg) cls = g.cls[ni];
@@ -722,11 +725,11 @@ __device__ __forceinline__ void step_node(const StepArgs& a, int x, int y,
   if (cls == 1) r = g.recmap[ni];
   if (a.flags & F_NOPULL) {
 #pragma unroll
-    for (int k = 0; k < 9; ++k) f[k] = Store<S>::ldr(fin + k * g.plane, ni);
+    for (int k = 0; k < 9; ++k) f[k] = Store<S>::ldr(fn, k * g.plane);
   } else if (cls == 0) {
 #pragma unroll
     for (int k = 0; k < 9; ++k)
-      f[k] = Store<S>::ldr(fin + k * g.plane, ni - CYk(k) * g.pitch - CXk(k));
+      f[k] = Store<S>::ldr(fn, k * g.plane - (long long)(CYk(k) * g.pitch + CXk(k)));
   } else if (MOV && cls == 4) {
     f[0] = Store<S>::ldr(fin, ni);
     dynamic_links<S>(f, a, fin, ni);
@@ -737,7 +740,7 @@ __device__ __forceinline__ void step_node(const StepArgs& a, int x, int y,
   T rho, ux, uy;
   node_update<S, COLL, FORC>(f, a, n, rho, ux, uy, y * g.nseg + (x >> 5));
 #pragma unroll
-  for (int k = 0; k < 9; ++k) Store<S>::str(fout + k * g.plane, ni, f[k]);
+  for (int k = 0; k < 9; ++k) Store<S>::str(on, k * g.plane, f[k]);
   // density of every node of a flagged segment: the segments around a
   // moving obstacle are flagged a step before their nodes can enter class 4,
   // whose bounce-back then reads it
@@ -849,6 +852,7 @@ __global__ void __launch_bounds__(CAP ? 256 : 512, CAP == 1 ? 8 : (CAP == 2 ? 6 
     const int ni = (y + 1) * g.pitch + x;
     const long long n = ni;
     S* A = static_cast<S*>(a.fout);   // == a.fin
+    S* An = A + ni;                   // this node's element of plane 0 (uniform offsets below)
     int cls = 0;
     if (g.segflag[y * g.nseg + (x >> 5)]) cls = g.cls[ni];
     if (cls != 2) {
@@ -857,11 +861,11 @@ __global__ void __launch_bounds__(CAP ? 256 : 512, CAP == 1 ? 8 : (CAP == 2 ? 6 
       if (cls == 1) r = g.recmap[ni];
       if (!ODD && ((a.flags & F_NOPULL) || cls == 0)) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) f[k] = Store<S>::ldr(A + k * g.plane, ni);
+        for (int k = 0; k < 9; ++k) f[k] = Store<S>::ldr(An, k * g.plane);
       } else if (ODD && cls == 0) {
 #pragma unroll
         for (int k = 0; k < 9; ++k)
-          f[k] = Store<S>::ldr(A + INVk(k) * g.plane, ni - CYk(k) * g.pitch - CXk(k));
+          f[k] = Store<S>::ldr(An, INVk(k) * g.plane - (long long)(CYk(k) * g.pitch + CXk(k)));
       } else {
         f[0] = Store<S>::ldr(A, ni);
         special_links_aa<S, ODD>(f, a, A, n, r);
@@ -870,11 +874,11 @@ __global__ void __launch_bounds__(CAP ? 256 : 512, CAP == 1 ? 8 : (CAP == 2 ? 6 
       node_update<S, COLL, FORC>(f, a, n, rho, ux, uy, y * g.nseg + (x >> 5));
       if (!ODD) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) Store<S>::str(A + INVk(k) * g.plane, ni, f[k]);
+        for (int k = 0; k < 9; ++k) Store<S>::str(An, INVk(k) * g.plane, f[k]);
       } else {
 #pragma unroll
         for (int k = 0; k < 9; ++k)
-          Store<S>::str(A + k * g.plane, ni + CYk(k) * g.pitch + CXk(k), f[k]);
+          Store<S>::str(An, k * g.plane + (long long)(CYk(k) * g.pitch + CXk(k)), f[k]);
       }
       node_outputs<T>(a, n, r, rho, ux, uy, red);
     }

@@ -124,6 +124,23 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(value, dist, device):
+    """The largest `value` of all ranks (every rank receives it); `dist` is
+    torch.distributed or None for one process."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_mlups(world, nodes, steps, seconds):
+    """Units all ranks processed (replicas: `nodes` x `steps` each) per
+    second of the slowest rank, in MLUPS."""
+    return world * nodes * steps / seconds / 1e6
+
+
 def cpu_measure(case_dict, steps_budget_s=20.0, max_steps=None, warmup=1):
     """Times the C restatement of the reference CPU kernels on `case_dict`."""
     from oracle.setup import build_state
@@ -226,11 +243,8 @@ def run_gb300(args, world, rank, local):
     launches = sim.kernel_launches - launches0
     variant = sim.kernel_variant
     tuning = sim.tuning
-    if dist is not None:
-        t = torch.tensor([ms], device=f"cuda:{device}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    mlups = world * nodes * args.steps / (ms / 1e3) / 1e6
+    ms = max_over_ranks(ms, dist, f"cuda:{device}")
+    mlups = whole_job_mlups(world, nodes, args.steps, ms / 1e3)
     per_launch_ms = ms / args.steps
     peak, peak_kind = measured_peak()
     achieved = B_LU[args.storage] * nodes / (per_launch_ms / 1e3) / 1e9
@@ -259,8 +273,8 @@ def run_gb300(args, world, rank, local):
         sim.step(1, residual=True)
         sim.residual()                              # D2H of the step's residual
     rho_o, u_o = sim.moments(out=(rho_out, u_out))  # D2H of the final fields
-    t_e2e = time.perf_counter() - t0
-    e2e = {"value": world * nodes * e2e_steps / t_e2e / 1e6, "unit": "MLUPS",
+    t_e2e = max_over_ranks(time.perf_counter() - t0, dist, f"cuda:{device}")
+    e2e = {"value": whole_job_mlups(world, nodes, e2e_steps, t_e2e), "unit": "MLUPS",
            "h2d_bytes_per_step": int((rho_h.nbytes + u_h.nbytes) / e2e_steps),
            "d2h_bytes_per_step": int(8 * 8 + (rho_o.nbytes + u_o.nbytes) / e2e_steps),
            "steps": e2e_steps,

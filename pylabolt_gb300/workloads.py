@@ -39,15 +39,16 @@ def _base(nx, ny, kin_visc, precision="double", storage=None, model="BGK",
     }
 
 
-def cavity(n=128, re=100.0, lid=0.1, storage=None, lid_last=True):
+def cavity(n=128, re=100.0, lid=0.1, storage=None, lid_last=True, ny=None):
     """Lid-driven cavity, nu = U N / Re, tau = 3 nu + 1/2 (128^2, Re 100 ->
-    nu = 0.128, tau = 0.884)."""
+    nu = 0.128, tau = 0.884); `ny` (default n) makes it n wide and ny high."""
     kin_visc = lid * n / re
-    c = _base(n, n, kin_visc, storage=storage)
-    walls = {"wall": True, "segments": [[[0, 0], [0, n - 1]], [[n - 1, 0], [n - 1, n - 1]],
+    m = n if ny is None else ny
+    c = _base(n, m, kin_visc, storage=storage)
+    walls = {"wall": True, "segments": [[[0, 0], [0, m - 1]], [[n - 1, 0], [n - 1, m - 1]],
                                          [[0, 0], [n - 1, 0]]],
              "fluid": {"type": "bounce_back"}}
-    lid_d = {"wall": True, "segments": [[[0, n - 1], [n - 1, n - 1]]],
+    lid_d = {"wall": True, "segments": [[[0, m - 1], [n - 1, m - 1]]],
              "fluid": {"type": "fixed_velocity", "value": [lid, 0.0]}}
     if lid_last:
         c["boundary_dict"]["walls"] = walls

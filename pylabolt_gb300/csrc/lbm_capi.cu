@@ -942,6 +942,7 @@ int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout
   const bool direct = rd && ud;
   int rc = h->ensure_stage(direct ? 3 * plane : 3 * nh + 3 * plane);
   if (rc) return rc;
+  h->initialized = false;   // until the new state is complete
   double* ds = h->stage + (direct ? 0 : 3 * nh);   // device order: rho [plane], u [2][plane]
   LBM_CUDA(cudaMemsetAsync(ds, 0, 3 * plane * sizeof(double), h->stream));
   if (direct) {   // transposed straight from the caller's pinned buffers
@@ -1376,6 +1377,7 @@ int lbm_set_populations(LbmHandle* h, const double* pop_new) {
   const long long nh = h->host_nodes(LBM_LAYOUT_PADDED), plane = h->g.plane;
   int rc = h->ensure_stage(9 * nh + 9 * plane);
   if (rc) return rc;
+  h->initialized = false;   // until the new state is complete
   double* hs = h->stage;
   double* ds = h->stage + 9 * nh;
   LBM_CUDA(cudaMemcpyAsync(hs, pop_new, 9 * nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));

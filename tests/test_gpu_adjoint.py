@@ -22,7 +22,7 @@ FP32_RTOL = 1e-3      # FP32-shifted forward + FP32 adjoint vs FP64 reference
 # the non-equilibrium part is ~1e-7, where the FP32 trajectory's own rounding
 # is a percent of it: the FP32 model's tau-sensitivity differs by ~1%.
 FP32_TAU_RTOL = 2e-2
-FD_RTOL = 1e-4        # against central finite differences (the benchmark spec bound)
+FD_RTOL = 1e-4        # against central finite differences
 
 
 def _channel(forcing="guo_second_order", nx=24, ny=14, seed=5):

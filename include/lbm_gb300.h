@@ -123,7 +123,12 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
  * fluid nodes; solid nodes keep rho/u as given (reported by lbm_get_moments).
  * Replaces initialize_pop_density_based_second_order
  * (pylabolt/parallel/cpu/equilibrium_kernels.py:38-78) and the initial
- * fields of pylabolt/base/init_fields.py.  rho: [n], u: [n][2] in `layout`. */
+ * fields of pylabolt/base/init_fields.py.  rho: [n], u: [n][2] in `layout`.
+ * Host arrays are copied into a device staging buffer and transposed there;
+ * with LBM_HOST_DIRECT=1 (read at lbm_create) pinned host arrays are read in
+ * place by the transposing kernel over the host link, where the device can
+ * reach pageable memory (Grace-Blackwell), and lbm_get_moments writes pinned
+ * inner-layout arrays the same way.  The values are the same either way. */
 int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout);
 
 /* Sets a per-node body force field F[n][2] (inner layout) used instead of

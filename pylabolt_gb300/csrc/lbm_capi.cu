@@ -206,9 +206,13 @@ struct LbmHandle {
       if (el > timeout_s)
         return fail(LBM_ERR_TIMEOUT, "device work did not finish within " +
                                          std::to_string(timeout_s) + " s");
-      // poll without sleeping for the first 2 ms (a sleep costs ~50 us of
-      // timer slack, a step 0.2 ms), then every 200 us
-      if (el < 0.002)
+      // spin for the first 1 ms: a yield can hand the core to another
+      // runnable thread for a whole time slice on a busy host, a sleep costs
+      // ~50 us of timer slack, and a step takes 0.2 ms.  Then yield up to
+      // 5 ms, then poll every 200 us.
+      if (el < 0.001)
+        continue;
+      if (el < 0.005)
         std::this_thread::yield();
       else
         std::this_thread::sleep_for(std::chrono::microseconds(200));

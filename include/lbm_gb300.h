@@ -278,6 +278,17 @@ int lbm_get_moving_obstacles(LbmHandle* h, LbmMovingObstacle* out);
  * solid, 2 + i solid of moving obstacle i (registration order). */
 int lbm_get_node_flags(LbmHandle* h, uint8_t* flags);
 
+/* Checkpoint / restart of the step state (extension: the reference reads
+ * control_dict["checkpoint_interval"] but writes no checkpoint).  The state
+ * is the current population buffer (storage type, guard rows included), the
+ * boundary nodes' side array, the residual's previous-step fields when they
+ * exist, the time and the layout phase, behind a versioned header.  A state
+ * loads into a handle created with the same configuration and link table;
+ * the run then continues bit for bit.  Not with moving obstacles. */
+int lbm_state_size(LbmHandle* h, int64_t* bytes);
+int lbm_save_state(LbmHandle* h, void* out);        /* out: lbm_state_size bytes */
+int lbm_load_state(LbmHandle* h, const void* in);
+
 /* Number of completed steps since the last init. */
 int lbm_time(LbmHandle* h, int64_t* t);
 

@@ -87,7 +87,8 @@ EXPORTS = ["lbm_create", "lbm_init_fields", "lbm_set_body_force", "lbm_step",
            "lbm_synchronize", "lbm_last_error", "lbm_destroy", "lbm_conservation_noalloc",
            "lbm_adjoint_forward", "lbm_adjoint_backward", "lbm_set_omega_map",
            "lbm_set_force_links", "lbm_forces", "lbm_set_moving_obstacles",
-           "lbm_get_moving_obstacles", "lbm_get_node_flags"]
+           "lbm_get_moving_obstacles", "lbm_get_node_flags", "lbm_state_size",
+           "lbm_save_state", "lbm_load_state"]
 
 
 def lib_path():
@@ -134,6 +135,9 @@ def load(build=True):
         "lbm_set_moving_obstacles": [P, P, ctypes.c_int, P],
         "lbm_get_moving_obstacles": [P, P],
         "lbm_get_node_flags": [P, P],
+        "lbm_state_size": [P, ctypes.POINTER(i64)],
+        "lbm_save_state": [P, P],
+        "lbm_load_state": [P, P],
     }
     for name, argtypes in sig.items():
         fn = getattr(lib, name)

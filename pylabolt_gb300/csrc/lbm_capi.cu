@@ -1686,6 +1686,120 @@ int lbm_time_steps(LbmHandle* h, int64_t nsteps, double* ms) {
   return LBM_OK;
 }
 
+// ---- step state: save / restore -------------------------------------------
+namespace {
+struct StateHeader {
+  char magic[8];   // "LBMSTATE"
+  int32_t version;
+  int32_t nx, ny, precision, collision, forcing, layout, pitch, nrec;
+  int32_t cur, nopull, has_old, old_cur, reserved;
+  int64_t plane, t;
+  uint64_t pop_bytes, side_bytes, old_bytes;
+};
+constexpr int32_t kStateVersion = 1;
+
+StateHeader state_header(const LbmHandle* h) {
+  StateHeader H;
+  std::memset(&H, 0, sizeof H);
+  std::memcpy(H.magic, "LBMSTATE", 8);
+  H.version = kStateVersion;
+  H.nx = h->cfg.nx;
+  H.ny = h->cfg.ny;
+  H.precision = h->cfg.precision;
+  H.collision = h->cfg.collision;
+  H.forcing = h->cfg.forcing;
+  H.layout = h->cfg.layout;
+  H.pitch = h->g.pitch;
+  H.nrec = h->g.nrec;
+  H.cur = h->cur;
+  H.nopull = h->nopull ? 1 : 0;
+  H.has_old = h->old[0] ? 1 : 0;
+  H.old_cur = h->old_cur;
+  H.plane = h->g.plane;
+  H.t = h->t;
+  H.pop_bytes = h->state_bytes();
+  H.side_bytes = h->side_bytes();
+  H.old_bytes = H.has_old ? 6 * (uint64_t)h->g.plane * h->ks->compute_bytes : 0;
+  return H;
+}
+}  // namespace
+
+int lbm_state_size(LbmHandle* h, int64_t* bytes) {
+  if (!h || !bytes) return fail(LBM_ERR_ARG, "lbm_state_size: null argument");
+  const StateHeader H = state_header(h);
+  *bytes = (int64_t)(sizeof(StateHeader) + H.pop_bytes + H.side_bytes + H.old_bytes);
+  return LBM_OK;
+}
+
+int lbm_save_state(LbmHandle* h, void* out) {
+  if (!h || !out) return fail(LBM_ERR_ARG, "lbm_save_state: null argument");
+  if (!h->initialized) return fail(LBM_ERR_STATE, "lbm_save_state: not initialised");
+  if (h->mov.n) return fail(LBM_ERR_STATE, "lbm_save_state: not supported with moving obstacles");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  const StateHeader H = state_header(h);
+  char* o = static_cast<char*>(out);
+  std::memcpy(o, &H, sizeof H);
+  o += sizeof H;
+  LBM_CUDA(cudaMemcpyAsync(o, h->pop_raw[h->cur], H.pop_bytes, cudaMemcpyDeviceToHost, h->stream));
+  o += H.pop_bytes;
+  LBM_CUDA(cudaMemcpyAsync(o, h->side[h->cur], H.side_bytes, cudaMemcpyDeviceToHost, h->stream));
+  o += H.side_bytes;
+  for (int i = 0; i < 6 && H.has_old; ++i) {
+    const size_t b = H.old_bytes / 6;
+    LBM_CUDA(cudaMemcpyAsync(o, h->old[i], b, cudaMemcpyDeviceToHost, h->stream));
+    o += b;
+  }
+  return h->wait();
+}
+
+int lbm_load_state(LbmHandle* h, const void* in) {
+  if (!h || !in) return fail(LBM_ERR_ARG, "lbm_load_state: null argument");
+  if (h->mov.n) return fail(LBM_ERR_STATE, "lbm_load_state: not supported with moving obstacles");
+  StateHeader H;
+  std::memcpy(&H, in, sizeof H);
+  if (std::memcmp(H.magic, "LBMSTATE", 8) != 0 || H.version != kStateVersion)
+    return fail(LBM_ERR_ARG, "lbm_load_state: not a saved state of this library version");
+  const StateHeader M = state_header(h);
+  if (H.nx != M.nx || H.ny != M.ny || H.precision != M.precision || H.collision != M.collision ||
+      H.forcing != M.forcing || H.layout != M.layout || H.pitch != M.pitch || H.plane != M.plane ||
+      H.nrec != M.nrec || H.pop_bytes != M.pop_bytes || H.side_bytes != M.side_bytes ||
+      H.cur < 0 || H.cur > 1 || H.old_cur < 0 || H.old_cur > 1 ||
+      H.old_bytes != (H.has_old ? 6 * (uint64_t)h->g.plane * h->ks->compute_bytes : 0))
+    return fail(LBM_ERR_ARG, "lbm_load_state: the state was saved from a case with another grid, "
+                             "storage, collision, forcing, layout or link table");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  int rc;
+  if (H.has_old && (rc = h->ensure_old())) return rc;
+  h->initialized = false;   // until the state is complete
+  if (h->gexec) {           // graphs captured earlier hold the old buffer parity
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  h->cur = h->aa ? H.cur : 0;   // AA: the phase; two buffers: restore into buffer 0
+  const char* p = static_cast<const char*>(in) + sizeof H;
+  LBM_CUDA(cudaMemcpyAsync(h->pop_raw[h->cur], p, H.pop_bytes, cudaMemcpyHostToDevice, h->stream));
+  p += H.pop_bytes;
+  LBM_CUDA(cudaMemcpyAsync(h->side[h->cur], p, H.side_bytes, cudaMemcpyHostToDevice, h->stream));
+  p += H.side_bytes;
+  const size_t ob = (size_t)h->g.plane * h->ks->compute_bytes;
+  for (int i = 0; i < 6 && h->old[0]; ++i) {
+    if (H.has_old) {
+      LBM_CUDA(cudaMemcpyAsync(h->old[i], p, ob, cudaMemcpyHostToDevice, h->stream));
+      p += ob;
+    } else {
+      LBM_CUDA(cudaMemsetAsync(h->old[i], 0, ob, h->stream));
+    }
+  }
+  if ((rc = h->wait())) return rc;
+  h->old_cur = H.has_old ? H.old_cur : 0;
+  h->t = H.t;
+  h->nopull = H.nopull != 0;
+  h->has_moments = false;
+  h->has_residual = false;
+  h->initialized = true;
+  return LBM_OK;
+}
+
 int lbm_synchronize(LbmHandle* h, double timeout_s) {
   if (!h) return fail(LBM_ERR_ARG, "lbm_synchronize: null handle");
   LBM_CUDA(cudaSetDevice(h->cfg.device));

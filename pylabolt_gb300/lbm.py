@@ -239,6 +239,21 @@ class FluidLBM:
         check(self.lib.lbm_adjoint_backward(self.h, ptr(gu), ptr(gF), ctypes.byref(gtau), guw))
         return (gF.reshape(nx, ny, 2) if gF is not None else None), gtau.value, np.array(guw[:])
 
+    # -- checkpoint / restart (lbm_save_state / lbm_load_state)
+    def save_state(self):
+        """The step state as a uint8 array (populations, boundary side data,
+        residual history, time); `load_state` continues the run from it bit
+        for bit in a handle of the same case."""
+        n = ctypes.c_int64()
+        check(self.lib.lbm_state_size(self.h, ctypes.byref(n)))
+        buf = np.empty(n.value, dtype=np.uint8)
+        check(self.lib.lbm_save_state(self.h, ptr(buf)))
+        return buf
+
+    def load_state(self, state):
+        buf = np.ascontiguousarray(state, dtype=np.uint8)
+        check(self.lib.lbm_load_state(self.h, ptr(buf)))
+
     @property
     def time(self):
         t = ctypes.c_int64()

@@ -8,6 +8,12 @@ steps between two output events in one call (replayed CUDA graphs); steps
 with an event record what the event reads (moments for field output, the
 residual pass for the status line).  Outputs are the reference's files
 (pylabolt_gb300.output).
+
+Extension: ``control_dict["checkpoint_interval"]`` (read but unused by the
+reference) writes the step state every that many steps to
+``output/checkpoints/state_t<t>.npy`` (lbm_save_state), and a run whose
+``start_time`` has such a file continues from it bit for bit instead of
+starting from the initial fields.
 """
 import os
 import sys
@@ -49,6 +55,10 @@ class Solver:
         self.geometry = Geometry(self.case)
         self.out = Output(self.case, self.geometry, root)
         self.lbm = FluidLBM(self.case, storage=storage, device=device, layout=layout)
+        self.root = root
+        ci = self.case.checkpoint_interval
+        self.checkpoint_interval = ci if isinstance(ci, int) and not isinstance(ci, bool) and ci > 0 \
+            else None
         nobs = len(self.case.obstacles)
         self.nobs = nobs
         self.residues = None
@@ -73,7 +83,19 @@ class Solver:
             cands.append(_next_multiple(t, c.boundary_write_interval))
         if c.write_obstacle_data and c.obstacle_write_interval is not None:
             cands.append(_next_multiple(t, c.obstacle_write_interval))
+        if self.checkpoint_interval is not None and not c.moving:
+            cands.append(_next_multiple(t, self.checkpoint_interval))
         return min(cands)
+
+    def checkpoint_path(self, t):
+        return os.path.join(self.root, "output", "checkpoints", f"state_t{t}.npy")
+
+    def _checkpoint(self, t):
+        if self.checkpoint_interval is None or self.case.moving or t % self.checkpoint_interval:
+            return
+        path = self.checkpoint_path(t)
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        np.save(path, self.lbm.save_state())
 
     def _update_forces(self, obstacles, walls):
         """The reference computes obstacle forces every step when
@@ -118,9 +140,14 @@ class Solver:
         self.obstacle_forces = np.zeros((self.nobs, 3))
         self.wall_forces = np.zeros((len(self.out.walls), 2))
         self.lbm.initialize()
+        resume = self.checkpoint_path(c.start_time)
+        resumed = c.start_time > 0 and not c.moving and os.path.exists(resume)
+        if resumed:
+            self.lbm.load_state(np.load(resume))
+            self.log("Resuming from " + resume)
         # t = 0 forces and initial output (fluidLB.py:323-344)
         self._update_forces(self.out.obstacle_due(0), self.out.boundary_due(0))
-        if self.out.save_due(c.start_time):
+        if self.out.save_due(c.start_time) and not resumed:   # the first run wrote it
             rho, u = self.lbm.moments()
             if c.moving:
                 self.out.set_geometry(self._moving_geometry())
@@ -136,6 +163,7 @@ class Solver:
             std, save, bnd, obs = self._events(te)
             self.lbm.step(te - t, moments=save, residual=std)
             t = te
+            self._checkpoint(t)
             self._update_forces(obs, bnd)
             if std:
                 r = self.lbm.residual().astype(self.out.dtype)

@@ -51,6 +51,10 @@ int main(void) {
   double out[3];
   CHECK(lbm_residual(NULL, out) == LBM_ERR_ARG);
   CHECK(lbm_conservation_noalloc(NULL, NULL, NULL) == LBM_ERR_ARG);
+  int64_t nbytes = 0;
+  CHECK(lbm_state_size(NULL, &nbytes) == LBM_ERR_ARG);
+  CHECK(lbm_save_state(NULL, NULL) == LBM_ERR_ARG);
+  CHECK(lbm_load_state(NULL, NULL) == LBM_ERR_ARG);
   printf("ok\n");
   return 0;
 }

@@ -1,0 +1,102 @@
+"""Checkpoint / restart (lbm_save_state / lbm_load_state and the Solver's
+checkpoint_interval): a run saved at step 20 and continued in a fresh handle
+matches the uninterrupted run bit for bit -- fields, populations, residuals
+(the residual history travels with the state) -- for FP64 and FP32-shifted
+storage and both population layouts; mismatched cases are refused."""
+import os
+
+import numpy as np
+import pytest
+
+from _golden import load_golden
+from pylabolt_gb300 import capi, output, solver, workloads
+from pylabolt_gb300.config import Case
+from pylabolt_gb300.lbm import FluidLBM
+
+pytestmark = pytest.mark.gpu
+
+
+def _steps(sim, res):
+    sim.step(7, residual=True)
+    res.append(sim.residual())
+    sim.step(13, moments=True, residual=True)
+    res.append(sim.residual())
+
+
+@pytest.mark.parametrize("storage,layout", [("fp64", "ab"), ("fp32_shifted", "ab"),
+                                            ("fp64", "aa"), ("fp32_shifted", "aa")])
+@pytest.mark.parametrize("name", ["channel_cylinder_abb", "poiseuille_guo2"])
+def test_restart_is_bit_exact(name, storage, layout, monkeypatch):
+    # one launch shape for both handles: shapes may round FP32 differently
+    monkeypatch.setenv("LBM_VARIANT", "0,1,128,0" if storage == "fp64" else "0,1,128,1")
+    case = Case(load_golden(name)[0])
+    ra, rb = [], []
+    with FluidLBM(case, storage=storage, layout=layout) as a:
+        a.initialize()
+        _steps(a, ra)                      # t = 20
+        state = a.save_state()
+        assert a.time == 20
+        _steps(a, ra)                      # t = 40
+        pa = a.populations()
+        ma = a.moments()
+    with FluidLBM(case, storage=storage, layout=layout) as b:
+        b.initialize()
+        b.step(3)                          # whatever it held is replaced
+        b.load_state(state)
+        assert b.time == 20
+        _steps(b, rb)
+        assert np.array_equal(b.populations(), pa)
+        mb = b.moments()
+        assert np.array_equal(ma[0], mb[0]) and np.array_equal(ma[1], mb[1])
+    assert np.array_equal(np.array(ra[2:]), np.array(rb))
+
+
+def test_mismatched_state_is_refused():
+    a_case = Case(load_golden("channel_cylinder_abb")[0])
+    b_case = Case(load_golden("cavity_lid_first")[0])
+    with FluidLBM(a_case, storage="fp64") as a, FluidLBM(b_case, storage="fp64") as b, \
+            FluidLBM(a_case, storage="fp32_shifted") as c:
+        a.initialize()
+        b.initialize()
+        c.initialize()
+        state = a.save_state()
+        for other in (b, c):
+            with pytest.raises(capi.LbmError, match="another grid"):
+                other.load_state(state)
+        bad = state.copy()
+        bad[:8] = 0
+        with pytest.raises(capi.LbmError, match="not a saved state"):
+            a.load_state(bad)
+        b.step(2)                            # the refused handles still run
+        c.step(2)
+
+
+def test_solver_resumes_from_checkpoint(tmp_path, monkeypatch, capsys):
+    monkeypatch.setattr(output, "package_version", lambda: "0.0.0")
+    case = workloads.cavity(64)
+    case["control_dict"].update({"end_time": 60, "std_out_interval": 20, "save_interval": 30,
+                                 "checkpoint_interval": 20})
+    full = tmp_path / "full"
+    s = solver.Solver(case, root=str(full), storage="fp64", verbose=False)
+    try:
+        s.run()
+    finally:
+        s.close()
+    for t in (20, 40, 60):
+        assert os.path.exists(full / "output" / "checkpoints" / f"state_t{t}.npy")
+    # a second run directory holding the t = 20 checkpoint, started at 20
+    part = tmp_path / "part"
+    os.makedirs(part / "output" / "checkpoints")
+    os.link(full / "output" / "checkpoints" / "state_t20.npy",
+            part / "output" / "checkpoints" / "state_t20.npy")
+    case["control_dict"]["start_time"] = 20
+    s = solver.Solver(case, root=str(part), storage="fp64", verbose=False)
+    try:
+        s.run()
+    finally:
+        s.close()
+    for t in (30, 60):
+        zf = np.load(full / "output" / "fields" / f"t_{t}.npz")
+        zp = np.load(part / "output" / "fields" / f"t_{t}.npz")
+        for k in zf.files:
+            assert np.array_equal(zf[k], zp[k]), (t, k)

@@ -282,9 +282,11 @@ int lbm_get_node_flags(LbmHandle* h, uint8_t* flags);
  * control_dict["checkpoint_interval"] but writes no checkpoint).  The state
  * is the current population buffer (storage type, guard rows included), the
  * boundary nodes' side array, the residual's previous-step fields when they
- * exist, the time and the layout phase, behind a versioned header.  A state
- * loads into a handle created with the same configuration and link table;
- * the run then continues bit for bit.  Not with moving obstacles. */
+ * exist, the time and the layout phase, and with moving obstacles their
+ * device state (obstacles, node classes, solid / refill flags, solid velocity,
+ * bounce-back densities), behind a versioned header.  A state loads into a
+ * handle created with the same configuration, link table and number of moving
+ * obstacles (after lbm_init_fields); the run then continues bit for bit. */
 int lbm_state_size(LbmHandle* h, int64_t* bytes);
 int lbm_save_state(LbmHandle* h, void* out);        /* out: lbm_state_size bytes */
 int lbm_load_state(LbmHandle* h, const void* in);

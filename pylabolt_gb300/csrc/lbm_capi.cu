@@ -1692,11 +1692,31 @@ struct StateHeader {
   char magic[8];   // "LBMSTATE"
   int32_t version;
   int32_t nx, ny, precision, collision, forcing, layout, pitch, nrec;
-  int32_t cur, nopull, has_old, old_cur, reserved;
+  int32_t cur, nopull, has_old, old_cur, mov_n;
   int64_t plane, t;
-  uint64_t pop_bytes, side_bytes, old_bytes;
+  uint64_t pop_bytes, side_bytes, old_bytes, mov_bytes;
 };
-constexpr int32_t kStateVersion = 1;
+constexpr int32_t kStateVersion = 2;
+
+// Moving-obstacle part of the state: obstacles, node classes and segment
+// flags (they follow the obstacles), solid / refill flags, solid velocity and
+// the densities the next step's moving bounce-back reads.
+struct MovPart {
+  void* p;
+  size_t bytes;
+};
+std::vector<MovPart> mov_parts(LbmHandle* h) {
+  auto& M = h->mov;
+  const size_t plane = h->g.plane, cb = h->ks->compute_bytes;
+  if (!M.n) return {};
+  return {{M.obs, M.n * sizeof(lbm::MovObs)},
+          {const_cast<uint8_t*>(h->g.cls), plane},
+          {const_cast<uint8_t*>(h->g.segflag), (size_t)h->g.ny * h->g.nseg},
+          {M.dsolid, plane},
+          {M.fresh, plane},
+          {M.us, 2 * plane * cb},
+          {M.rho_dyn[h->cur], plane * cb}};
+}
 
 StateHeader state_header(const LbmHandle* h) {
   StateHeader H;
@@ -1715,6 +1735,8 @@ StateHeader state_header(const LbmHandle* h) {
   H.nopull = h->nopull ? 1 : 0;
   H.has_old = h->old[0] ? 1 : 0;
   H.old_cur = h->old_cur;
+  H.mov_n = h->mov.n;
+  for (const MovPart& m : mov_parts(const_cast<LbmHandle*>(h))) H.mov_bytes += m.bytes;
   H.plane = h->g.plane;
   H.t = h->t;
   H.pop_bytes = h->state_bytes();
@@ -1727,14 +1749,13 @@ StateHeader state_header(const LbmHandle* h) {
 int lbm_state_size(LbmHandle* h, int64_t* bytes) {
   if (!h || !bytes) return fail(LBM_ERR_ARG, "lbm_state_size: null argument");
   const StateHeader H = state_header(h);
-  *bytes = (int64_t)(sizeof(StateHeader) + H.pop_bytes + H.side_bytes + H.old_bytes);
+  *bytes = (int64_t)(sizeof(StateHeader) + H.pop_bytes + H.side_bytes + H.old_bytes + H.mov_bytes);
   return LBM_OK;
 }
 
 int lbm_save_state(LbmHandle* h, void* out) {
   if (!h || !out) return fail(LBM_ERR_ARG, "lbm_save_state: null argument");
   if (!h->initialized) return fail(LBM_ERR_STATE, "lbm_save_state: not initialised");
-  if (h->mov.n) return fail(LBM_ERR_STATE, "lbm_save_state: not supported with moving obstacles");
   LBM_CUDA(cudaSetDevice(h->cfg.device));
   const StateHeader H = state_header(h);
   char* o = static_cast<char*>(out);
@@ -1749,12 +1770,15 @@ int lbm_save_state(LbmHandle* h, void* out) {
     LBM_CUDA(cudaMemcpyAsync(o, h->old[i], b, cudaMemcpyDeviceToHost, h->stream));
     o += b;
   }
+  for (const MovPart& m : mov_parts(h)) {
+    LBM_CUDA(cudaMemcpyAsync(o, m.p, m.bytes, cudaMemcpyDeviceToHost, h->stream));
+    o += m.bytes;
+  }
   return h->wait();
 }
 
 int lbm_load_state(LbmHandle* h, const void* in) {
   if (!h || !in) return fail(LBM_ERR_ARG, "lbm_load_state: null argument");
-  if (h->mov.n) return fail(LBM_ERR_STATE, "lbm_load_state: not supported with moving obstacles");
   StateHeader H;
   std::memcpy(&H, in, sizeof H);
   if (std::memcmp(H.magic, "LBMSTATE", 8) != 0 || H.version != kStateVersion)
@@ -1763,10 +1787,11 @@ int lbm_load_state(LbmHandle* h, const void* in) {
   if (H.nx != M.nx || H.ny != M.ny || H.precision != M.precision || H.collision != M.collision ||
       H.forcing != M.forcing || H.layout != M.layout || H.pitch != M.pitch || H.plane != M.plane ||
       H.nrec != M.nrec || H.pop_bytes != M.pop_bytes || H.side_bytes != M.side_bytes ||
+      H.mov_n != M.mov_n || H.mov_bytes != M.mov_bytes ||
       H.cur < 0 || H.cur > 1 || H.old_cur < 0 || H.old_cur > 1 ||
       H.old_bytes != (H.has_old ? 6 * (uint64_t)h->g.plane * h->ks->compute_bytes : 0))
     return fail(LBM_ERR_ARG, "lbm_load_state: the state was saved from a case with another grid, "
-                             "storage, collision, forcing, layout or link table");
+                             "storage, collision, forcing, layout, link table or moving obstacles");
   LBM_CUDA(cudaSetDevice(h->cfg.device));
   int rc;
   if (H.has_old && (rc = h->ensure_old())) return rc;
@@ -1789,6 +1814,10 @@ int lbm_load_state(LbmHandle* h, const void* in) {
     } else {
       LBM_CUDA(cudaMemsetAsync(h->old[i], 0, ob, h->stream));
     }
+  }
+  for (const MovPart& m : mov_parts(h)) {   // after cur is set: rho_dyn[cur]
+    LBM_CUDA(cudaMemcpyAsync(m.p, p, m.bytes, cudaMemcpyHostToDevice, h->stream));
+    p += m.bytes;
   }
   if ((rc = h->wait())) return rc;
   h->old_cur = H.has_old ? H.old_cur : 0;

@@ -83,7 +83,7 @@ class Solver:
             cands.append(_next_multiple(t, c.boundary_write_interval))
         if c.write_obstacle_data and c.obstacle_write_interval is not None:
             cands.append(_next_multiple(t, c.obstacle_write_interval))
-        if self.checkpoint_interval is not None and not c.moving:
+        if self.checkpoint_interval is not None:
             cands.append(_next_multiple(t, self.checkpoint_interval))
         return min(cands)
 
@@ -91,7 +91,7 @@ class Solver:
         return os.path.join(self.root, "output", "checkpoints", f"state_t{t}.npy")
 
     def _checkpoint(self, t):
-        if self.checkpoint_interval is None or self.case.moving or t % self.checkpoint_interval:
+        if self.checkpoint_interval is None or t % self.checkpoint_interval:
             return
         path = self.checkpoint_path(t)
         os.makedirs(os.path.dirname(path), exist_ok=True)
@@ -141,7 +141,7 @@ class Solver:
         self.wall_forces = np.zeros((len(self.out.walls), 2))
         self.lbm.initialize()
         resume = self.checkpoint_path(c.start_time)
-        resumed = c.start_time > 0 and not c.moving and os.path.exists(resume)
+        resumed = c.start_time > 0 and os.path.exists(resume)
         if resumed:
             self.lbm.load_state(np.load(resume))
             self.log("Resuming from " + resume)

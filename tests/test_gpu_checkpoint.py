@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from _golden import load_golden
+from test_moving_cpu import disk_case
 from pylabolt_gb300 import capi, output, solver, workloads
 from pylabolt_gb300.config import Case
 from pylabolt_gb300.lbm import FluidLBM
@@ -100,3 +101,34 @@ def test_solver_resumes_from_checkpoint(tmp_path, monkeypatch, capsys):
         zp = np.load(part / "output" / "fields" / f"t_{t}.npz")
         for k in zf.files:
             assert np.array_equal(zf[k], zp[k]), (t, k)
+
+
+@pytest.mark.parametrize("kw", [{"v": (0.05, 0.02), "om": 0.01},
+                                {"v": (0.0, 0.0), "om": 0.0, "kind": "calculated", "density": 1.5}])
+def test_restart_with_moving_obstacles(kw, monkeypatch):
+    """The moving obstacles' device state travels with the step state: the
+    restarted run moves them and fills the nodes they leave exactly as the
+    uninterrupted one."""
+    monkeypatch.setenv("LBM_VARIANT", "0,1,128,0")
+    case = Case(disk_case(True, **kw))
+    with FluidLBM(case, storage="fp64") as a:
+        a.initialize()
+        a.step(25, residual=True)
+        state = a.save_state()
+        a.step(40, moments=True, residual=True)
+        ra = a.residual()
+        pa, fa, oa = a.populations(), a.node_flags(), a.moving_obstacles()[0]
+        ma = a.moments()
+    with FluidLBM(case, storage="fp64") as b:
+        b.initialize()
+        b.load_state(state)
+        b.step(40, moments=True, residual=True)
+        assert np.array_equal(b.residual(), ra)
+        assert np.array_equal(b.populations(), pa)
+        assert np.array_equal(b.node_flags(), fa)
+        ob = b.moving_obstacles()[0]
+        for k in ("center", "velocity", "force"):
+            assert np.array_equal(np.asarray(oa[k]), np.asarray(ob[k])), k
+        assert oa["omega"] == ob["omega"] and oa["torque"] == ob["torque"]
+        mb = b.moments()
+        assert np.array_equal(ma[0], mb[0]) and np.array_equal(ma[1], mb[1])

@@ -106,14 +106,30 @@ class Output:
         np.savez(os.path.join(self.field_dir, f"t_{t}.npz"), **out)
 
     # -- histories
-    def setup_histories(self):
+    @staticmethod
+    def _keep_until(path, t):
+        """A resumed run keeps a history file's header and its rows up to time
+        t (rows after t are written again).  True if the file was kept."""
+        if t is None or not os.path.exists(path):
+            return False
+        with open(path) as f:
+            lines = f.readlines()
+        kept = [l for l in lines if l.startswith("#") or (l.split() and float(l.split()[0]) <= t)]
+        with open(path, "w") as f:
+            f.writelines(kept)
+        return True
+
+    def setup_histories(self, resume_time=None):
         c = self.case
         if not (c.write_obstacle_data or c.write_boundary_data):
             return
         os.makedirs(self.history_dir, exist_ok=True)
         if c.write_obstacle_data:
             for o in c.obstacles:
-                with open(os.path.join(self.history_dir, o.name + ".dat"), "w") as f:
+                path = os.path.join(self.history_dir, o.name + ".dat")
+                if self._keep_until(path, resume_time):
+                    continue
+                with open(path, "w") as f:
                     f.write(f"{'#':5} {'PyLaBolt obstacle history'}\n"
                             f"{'#':5} {'ID':8}: {o.id}\n"
                             f"{'#':5} {'Name':8}: {o.name}\n"
@@ -124,7 +140,10 @@ class Output:
                             f"{'force_y':<30}{'torque':<30}\n")
         if c.write_boundary_data:
             for el in self.walls:
-                with open(os.path.join(self.history_dir, el.name + ".dat"), "w") as f:
+                path = os.path.join(self.history_dir, el.name + ".dat")
+                if self._keep_until(path, resume_time):
+                    continue
+                with open(path, "w") as f:
                     f.write(f"{'#':5} {'PyLaBolt boundary history'}\n"
                             f"{'#':5} {'Name':8}: {el.name}\n"
                             f"{'#':5} {'Columns':8}:\n")

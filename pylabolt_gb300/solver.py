@@ -135,27 +135,29 @@ class Solver:
         c = self.case
         self.log("\n" + "-" * 80)
         self.log("Running simulation...\n")
+        resume = self.checkpoint_path(c.start_time)
+        resumed = c.start_time > 0 and os.path.exists(resume)
         self.out.write_metadata()
-        self.out.setup_histories()
+        self.out.setup_histories(resume_time=c.start_time if resumed else None)
         self.obstacle_forces = np.zeros((self.nobs, 3))
         self.wall_forces = np.zeros((len(self.out.walls), 2))
         self.lbm.initialize()
-        resume = self.checkpoint_path(c.start_time)
-        resumed = c.start_time > 0 and os.path.exists(resume)
         if resumed:
             self.lbm.load_state(np.load(resume))
             self.log("Resuming from " + resume)
-        # t = 0 forces and initial output (fluidLB.py:323-344)
-        self._update_forces(self.out.obstacle_due(0), self.out.boundary_due(0))
-        if self.out.save_due(c.start_time) and not resumed:   # the first run wrote it
-            rho, u = self.lbm.moments()
-            if c.moving:
-                self.out.set_geometry(self._moving_geometry())
-            self.out.write_fields(c.start_time, rho, u)
-        if self.out.obstacle_due(0):
-            self.out.write_obstacles(0, self.obstacle_forces, self._moving_states())
-        if self.out.boundary_due(0):
-            self.out.write_walls(0, self.wall_forces)
+        # t = 0 forces and initial output (fluidLB.py:323-344); a resumed run
+        # continues after them (the run that wrote the checkpoint wrote them)
+        if not resumed:
+            self._update_forces(self.out.obstacle_due(0), self.out.boundary_due(0))
+            if self.out.save_due(c.start_time):
+                rho, u = self.lbm.moments()
+                if c.moving:
+                    self.out.set_geometry(self._moving_geometry())
+                self.out.write_fields(c.start_time, rho, u)
+            if self.out.obstacle_due(0):
+                self.out.write_obstacles(0, self.obstacle_forces, self._moving_states())
+            if self.out.boundary_due(0):
+                self.out.write_walls(0, self.wall_forces)
         t0 = time.perf_counter()
         t = c.start_time
         while t < c.end_time:

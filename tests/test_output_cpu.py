@@ -131,3 +131,41 @@ def test_cli_rejects_cpu_backend():
     from pylabolt_gb300.__main__ import main
     with pytest.raises(SystemExit, match="gpu backend only"):
         main(["-s", "fluidLB", "-b", "cpu"])
+
+
+class CheckpointLBM(GoldenLBM):
+    """GoldenLBM with a stand-in step state: the time it was saved at."""
+
+    def save_state(self):
+        return np.array([self.t], dtype=np.int64).view(np.uint8)
+
+    def load_state(self, state):
+        self.t = int(np.asarray(state).view(np.int64)[0])
+
+
+def test_checkpoints_scheduled_and_resumed(tmp_path, monkeypatch, capsys):
+    case, d, _ = _io()
+    case["control_dict"]["checkpoint_interval"] = 20
+    monkeypatch.setattr(solver, "FluidLBM", CheckpointLBM)
+    monkeypatch.setattr(output, "package_version", lambda: str(d["version"]))
+    s = solver.Solver(case, root=str(tmp_path))
+    s.run()
+    # checkpoint events join the output events without changing them
+    assert s.lbm.calls == [(20, False, False), (10, True, True), (10, False, False),
+                           (20, True, True)]
+    ck = tmp_path / "output" / "checkpoints"
+    assert sorted(os.listdir(ck)) == ["state_t20.npy", "state_t40.npy", "state_t60.npy"]
+    lines = [l for l in capsys.readouterr().out.splitlines() if l.startswith("time:")]
+    assert lines == d["status_lines"].tolist()
+    hist = tmp_path / "output" / "histories"
+    before = {h: (hist / h).read_text() for h in os.listdir(hist)}
+    # a run started at t = 30 resumes from that file: the histories keep their
+    # rows up to t = 30 and get the later ones again, as the first run wrote them
+    np.save(ck / "state_t30.npy", np.array([30], dtype=np.int64).view(np.uint8))
+    case["control_dict"]["start_time"] = 30
+    s = solver.Solver(case, root=str(tmp_path))
+    s.run()
+    assert s.lbm.calls == [(10, False, False), (20, True, True)]
+    assert "Resuming from" in capsys.readouterr().out
+    for h, text in before.items():
+        assert (hist / h).read_text() == text, h

@@ -9,8 +9,13 @@
  * Conventions
  *  - Every call returns an int status (LBM_OK == 0).  lbm_last_error() gives a
  *    message for the last failing call of the calling thread.
- *  - Host arrays are borrowed for the duration of the call only.  The library
- *    owns all device memory of a handle.
+ *  - Caller arrays are borrowed for the duration of the call only.  The library
+ *    owns all device memory of a handle.  The node, field and population
+ *    arrays of lbm_init_fields, lbm_set_body_force, lbm_get_moments,
+ *    lbm_get_populations, lbm_set_populations, lbm_forces and
+ *    lbm_adjoint_backward may be host memory (pageable or pinned) or device
+ *    memory (unified addressing picks the copy direction); device arrays
+ *    written by other streams must be complete before the call.
  *  - Node arrays on the host use the reference's inner-node order
  *    ind = x * ny + y (x-major, y fastest), i.e. the padded index
  *    (x+1)*(ny+2)+(y+1) of pylabolt/base/fields.py with the ghost ring removed,
@@ -298,14 +303,14 @@ int lbm_time(LbmHandle* h, int64_t* t);
 int lbm_kernel_launches(LbmHandle* h, int64_t* n);
 
 /* Launch shape of the fused step picked by the autotuner on the first step:
- * out = {kind (0 scalar, 1 vector, 2 TMA pipeline), nodes per thread,
+ * out = {kind (0 scalar, 1 vector, 2 TMA pipeline, 3 node pairs), nodes per thread,
  * threads per block, shared-memory stages}.  LBM_VARIANT="kind,vec,block,stages"
  * forces one candidate, LBM_TUNE=0 keeps the first.  (Extension: the
  * reference launches every kernel with 256 threads, backend.py:59-75.) */
 int lbm_kernel_variant(LbmHandle* h, int out[4]);
 
 /* Per-candidate mean step time (ms) measured by the autotuner; *n receives the
- * number of candidates (at most 12). */
+ * number of candidates (at most 16). */
 int lbm_tuning(LbmHandle* h, double* ms_per_candidate, int* n);
 
 /* Device bytes held by the handle. */
@@ -319,9 +324,11 @@ int lbm_time_steps(LbmHandle* h, int64_t nsteps, double* ms);
 int lbm_synchronize(LbmHandle* h, double timeout_s);
 
 /* A population array owned by the caller, in device memory: value of node
- * (x, y), direction k (D2Q9 order of pylabolt/base/lattice.py) at
- * pop[k*plane + y*pitch + x], stored as f (LBM_FP64), g = f - w_k
- * (LBM_FP32_SHIFTED) or g * fp16_scale (LBM_FP16_SHIFTED). */
+ * (x, y), direction k at pop[k*plane + y*pitch + x], stored as f (LBM_FP64),
+ * g = f - w_k (LBM_FP32_SHIFTED) or g * fp16_scale in IEEE half
+ * (LBM_FP16_SHIFTED).  Directions k = 0..8 have (cx, cy) = (0,0), (1,0),
+ * (0,1), (-1,0), (0,-1), (1,1), (-1,1), (-1,-1), (1,-1) and weights
+ * w_k = 4/9 (k = 0), 1/9 (k = 1..4), 1/36 (k = 5..8). */
 typedef struct {
   int32_t precision;
   int32_t nx, ny;
@@ -340,19 +347,22 @@ typedef struct {
  * ({sum f, sum cx f, sum cy f} over the nodes not excluded, FP64), for a
  * population array the caller owns, for callers that cannot allocate device
  * memory: code embedded in a host application that hands out all device
- * memory from its own pool, code running while a stream is captured (where
- * cudaMalloc is not permitted), or monitoring loops that cannot take
- * cudaMalloc's implicit synchronisation.  It allocates nothing: its scratch is
- * a fixed device array inside the library (LBM_NOALLOC_MAX_ROWS + 64 rows of
- * 8 doubles, about 0.5 MB, held by every GPU that loads the library until the
+ * memory from its own pool, or monitoring loops that cannot take cudaMalloc's
+ * implicit synchronisation.  It allocates nothing: its scratch is a fixed
+ * device array inside the library (LBM_NOALLOC_MAX_ROWS + 64 rows of 8
+ * doubles, about 0.5 MB, held by every GPU that loads the library until the
  * process exits).  out_device receives 3 doubles; the work is queued on
  * `stream` (a cudaStream_t, NULL for the default stream) and the call returns
  * without waiting.  ny above LBM_NOALLOC_MAX_ROWS is rejected (LBM_ERR_ARG).
- * The first call on each device looks up the scratch array's device address
- * (cudaGetSymbolAddress), so make that first call before any stream capture.
- * All calls share the one scratch array: calls whose work overlaps on the GPU
- * (other streams, or other host threads on the same device) race and must be
- * serialised by the caller. */
+ * The first call on each device, with that device current, looks up the
+ * scratch array's device address (cudaGetSymbolAddress) and keeps it for the
+ * life of the process, so make that first call before any stream capture;
+ * after a cudaDeviceReset of that device the kept address is stale and the
+ * entry point must not be called again in that process.  All calls share the
+ * one scratch array, which keeps the last call's partial sums (each call
+ * overwrites every row it reads, so nothing needs clearing): calls whose
+ * work overlaps on the GPU (other streams, or other host threads on the same
+ * device) race and must be serialised by the caller. */
 int lbm_conservation_noalloc(const LbmPopView* view, double* out_device, void* stream);
 
 /* Message of the last failing call on this thread ("" if none). */

@@ -10,9 +10,10 @@ reference's CPU kernels operate on, in the reference's own layout:
 * boundary elements with node lists on the first interior ring
   ``ind = (i+1)*(Ny+2) + (j+1)`` and the per-location out/inv direction lists
   -- pylabolt/base/boundary.py:63-127, :451-485;
-* circle obstacles rasterised by ``dist^2 <= r^2`` on global inner-node
+* circle obstacles rasterised by ``dist^2 <= r^2`` and ellipses by
+  ``(x'/a)^2 + (y'/b)^2 <= 1`` in the inclined frame, on global inner-node
   coordinates with the periodic minimum image --
-  pylabolt/parallel/cpu/obstacle_kernels.py:11-93;
+  pylabolt/parallel/cpu/obstacle_kernels.py:11-93,151-241;
 * initial fields ``fixed`` / ``func`` on non-ghost nodes --
   pylabolt/base/init_fields.py:274-375.  The extension type ``array`` takes an
   explicit inner-node array ``[Nx, Ny]`` (``[Nx, Ny, 2]`` for velocity).
@@ -181,14 +182,13 @@ def build_state(sim, periodic_mode="wrap"):
                 raise ValueError("segment is not on the domain edge: " + name)
             nodes = st.padded_index(xs, ys)
             st.elements.append(Element(f"{name}_{seg_no}", bc_type, loc, nodes, value))
-    # obstacles -- obstacle.py:392-588, obstacle_kernels.py:43-93
+    # obstacles -- obstacle.py:392-825, obstacle_kernels.py:43-93,151-241
     for name, od in sim.get("obstacle_dict", {}).items():
         if name == "options":
             continue
-        if od["type"] != "circle":
-            raise ValueError("oracle restates circle obstacles only")
+        if od["type"] not in ("circle", "ellipse"):
+            raise ValueError("oracle restates circle and ellipse obstacles only")
         cx, cy = (np.float64(c) for c in od["center"])
-        r = np.float64(od["radius"])
         lin = np.zeros(2)
         ang = np.float64(0)
         if not od["static"]:
@@ -205,7 +205,19 @@ def build_state(sim, periodic_mode="wrap"):
         if st.y_periodic:
             rym = np.where(np.abs(ry + ny) < np.abs(rym), ry + ny, rym)
             rym = np.where(np.abs(ry - ny) < np.abs(rym), ry - ny, rym)
-        inside = rxm * rxm + rym * rym <= r * r
+        if od["type"] == "circle":
+            r = np.float64(od["radius"])
+            inside = rxm * rxm + rym * rym <= r * r
+        else:
+            # is_ellipse -- obstacle_kernels.py:151-189, angle in degrees
+            # (obstacle.py:666-676)
+            a = np.float64(od["semi_major_axis"])
+            b = np.float64(od["semi_minor_axis"])
+            alpha = np.float64(od["inclination_angle"]) * np.pi / 180
+            ca, sa = np.cos(alpha), np.sin(alpha)
+            xp = rxm * ca + rym * sa
+            yp = -rxm * sa + rym * ca
+            inside = (xp * xp) / (a * a) + (yp * yp) / (b * b) <= 1
         hit = ind[inside]
         st.solid[hit] = True
         st.velocity[hit, 0] = lin[0] - ang * rym[inside]

@@ -7,7 +7,9 @@ of the last step as a torch tensor; gradients flow to the body-force field
 ``u_wall`` [2] of the case's fixed_velocity boundaries.  The forward pass runs
 on the GPU through the C-ABI (lbm_adjoint_forward), the backward pass is the
 discrete adjoint (lbm_adjoint_backward) with checkpoint-and-recompute every
-``interval`` steps.  PyTorch only carries the tensors and the graph.
+``interval`` steps.  PyTorch only carries the tensors and the graph.  CUDA
+tensors stay on the device: the body-force field, the velocity, dL/du and
+dL/dF pass through the C-ABI as device pointers, without a host round trip.
 """
 import copy
 
@@ -39,26 +41,48 @@ def case_with(case, tau=None, u_wall=None, force=None):
 class _LBMVelocity(torch.autograd.Function):
     @staticmethod
     def forward(ctx, force, tau, u_wall, case, nsteps, interval, storage):
-        c = case_with(case, tau=float(tau), u_wall=u_wall.detach().cpu().numpy(),
-                      force=force.detach().cpu().numpy() if force is not None else None)
-        sim = FluidLBM(c, storage=storage)
+        on_gpu = force is not None and force.is_cuda
+        if force is None:
+            c = case_with(case, tau=float(tau), u_wall=u_wall.detach().cpu().numpy())
+            sim = FluidLBM(c, storage=storage)
+        elif on_gpu:
+            # the case only needs to know that there is a body-force field;
+            # its values come from the device tensor
+            c = case_with(case, tau=float(tau), u_wall=u_wall.detach().cpu().numpy(),
+                          force=np.zeros((case.nx, case.ny, 2)))
+            f = force.detach().to(torch.float64).contiguous()
+            sim = FluidLBM(c, storage=storage, device=f.device.index or 0, body_force=f)
+        else:
+            c = case_with(case, tau=float(tau), u_wall=u_wall.detach().cpu().numpy(),
+                          force=force.detach().cpu().numpy())
+            sim = FluidLBM(c, storage=storage)
         sim.initialize()
         sim.adjoint_forward(nsteps, interval)
-        _, u = sim.moments()
         ctx.sim = sim
         ctx.has_force = force is not None
+        ctx.devices = (force.device if force is not None else None, tau.device, u_wall.device)
+        if on_gpu:
+            n = case.nx * case.ny
+            rho = torch.empty(n, dtype=torch.float64, device=force.device)
+            u = torch.empty((n, 2), dtype=torch.float64, device=force.device)
+            _, u = sim.moments(out=(rho, u))
+            return u
+        _, u = sim.moments()
         return torch.from_numpy(u).to(u_wall.device)
 
     @staticmethod
     def backward(ctx, grad_u):
         sim = ctx.sim
-        gF, gtau, guw = sim.adjoint_backward(grad_u.detach().cpu().numpy(),
+        dev_F, dev_tau, dev_uw = ctx.devices
+        gF, gtau, guw = sim.adjoint_backward(grad_u if grad_u.is_cuda else grad_u.detach().cpu().numpy(),
                                               want_force=ctx.has_force)
         sim.close()
-        dev = grad_u.device
-        out_F = torch.from_numpy(gF).to(dev) if (ctx.has_force and gF is not None) else None
-        return (out_F, torch.tensor(gtau, dtype=torch.float64, device=dev),
-                torch.from_numpy(guw).to(dev), None, None, None, None)
+        if ctx.has_force and gF is not None:
+            out_F = (gF if torch.is_tensor(gF) else torch.from_numpy(gF)).to(dev_F)
+        else:
+            out_F = None
+        return (out_F, torch.tensor(gtau, dtype=torch.float64, device=dev_tau),
+                torch.from_numpy(guw).to(dev_uw), None, None, None, None)
 
 
 def lbm_velocity(case, force=None, tau=None, u_wall=None, nsteps=100, interval=45,

@@ -112,9 +112,15 @@ class Obstacle:
         self.calculated = False
         self.rotation_allowed = False
         self.translation_allowed = False
-        r = float(radius) if radius is not None else 0.0
-        self.mass = np.pi * r * r * density
-        self.moment_of_inertia = self.mass * r * r / 2
+        if semi_axes is not None:
+            # obstacle.py:703-710
+            a, b = (float(v) for v in semi_axes)
+            self.mass = np.pi * a * b * density
+            self.moment_of_inertia = self.mass * (a * a + b * b) / 4
+        else:
+            r = float(radius) if radius is not None else 0.0
+            self.mass = np.pi * r * r * density
+            self.moment_of_inertia = self.mass * r * r / 2
 
 
 class Case:
@@ -385,19 +391,22 @@ class Case:
             d = od[name]
             if "type" not in d:
                 raise ValueError("type missing in obstacle: " + name)
-            if d["type"] != "circle":
+            if d["type"] == "ellipse":
+                self._check_ellipse(name, d)
+            elif d["type"] != "circle":
                 raise ValueError("Unsupported obstacle type: " + str(d["type"]))
-            for key in ("radius", "center", "density", "static"):
-                if key not in d:
-                    raise ValueError(f"{key} missing in obstacle: " + name)
-            if type(d["radius"]) not in (float, int):
-                raise ValueError("radius must be float or int for obstacle type circle: " + name)
-            if not isinstance(d["center"], list):
-                raise ValueError("center must be list for obstacle type circle: " + name)
-            if type(d["density"]) not in (float, int):
-                raise ValueError("density must be float or int for obstacle type circle: " + name)
-            if not isinstance(d["static"], (bool, np.bool_)):
-                raise ValueError("static must be True/False for obstacle type circle: " + name)
+            else:
+                for key in ("radius", "center", "density", "static"):
+                    if key not in d:
+                        raise ValueError(f"{key} missing in obstacle: " + name)
+                if type(d["radius"]) not in (float, int):
+                    raise ValueError("radius must be float or int for obstacle type circle: " + name)
+                if not isinstance(d["center"], list):
+                    raise ValueError("center must be list for obstacle type circle: " + name)
+                if type(d["density"]) not in (float, int):
+                    raise ValueError("density must be float or int for obstacle type circle: " + name)
+                if not isinstance(d["static"], (bool, np.bool_)):
+                    raise ValueError("static must be True/False for obstacle type circle: " + name)
             lin, ang = [0.0, 0.0], 0.0
             if not d["static"]:
                 if "solid_motion_dict" not in d:
@@ -417,8 +426,14 @@ class Case:
                     raise ValueError("linear_velocity must be list [ux, uy]: " + name)
                 if not isinstance(ang, (int, float)):
                     raise ValueError("angular_velocity must be int/float: " + name)
-            obs = Obstacle(oid, name, "circle", d["center"], float(d["radius"]),
-                           float(d["density"]), bool(d["static"]), lin, ang)
+            if d["type"] == "ellipse":
+                obs = Obstacle(oid, name, "ellipse", d["center"], None, float(d["density"]),
+                               bool(d["static"]), lin, ang,
+                               semi_axes=(float(d["semi_major_axis"]), float(d["semi_minor_axis"])),
+                               inclination=float(d["inclination_angle"]))
+            else:
+                obs = Obstacle(oid, name, "circle", d["center"], float(d["radius"]),
+                               float(d["density"]), bool(d["static"]), lin, ang)
             if not d["static"]:
                 sm = d["solid_motion_dict"]
                 obs.motion_type = sm["type"]
@@ -427,7 +442,14 @@ class Case:
                 obs.translation_allowed = sm["degree_of_freedom"] in ("translation", "both")
             self.obstacles.append(obs)
             moving = (not obs.static) and bool(opts.get("move_obstacles", False))
-            self._rasterise_circle(obs, solid=not moving)
+            if moving and obs.type != "circle":
+                raise ValueError("move_obstacles: only circles move on the device; obstacle " +
+                                 name + " is an ellipse (make it static, or leave "
+                                 "move_obstacles unset to keep it in place as a moving wall)")
+            if obs.type == "ellipse":
+                self._rasterise_ellipse(obs)
+            else:
+                self._rasterise_circle(obs, solid=not moving)
         if any(not o.static for o in self.obstacles) and not self.compute_force_torque:
             raise ValueError("If any obstacle is not static, "
                              "then compute_force_torque must be True")
@@ -439,10 +461,36 @@ class Case:
             raise ValueError("move_obstacles must be bool: True/False (default: False)")
         self.moving = [o for o in self.obstacles if not o.static] if self.move_obstacles else []
 
-    def _rasterise_circle(self, obs, solid=True):
-        """dist^2 <= r^2 with the periodic minimum image (obstacle_kernels.py:11-93);
-        solid nodes take the body velocity and density.  solid=False (a moving
-        obstacle) sets only the fields: the device places it."""
+    @staticmethod
+    def _check_ellipse(name, d):
+        """Keys, types and messages of the reference's Ellipse
+        (pylabolt/base/obstacle.py:591-701), in its order."""
+        for key in ("semi_major_axis", "semi_minor_axis"):
+            if key not in d:
+                raise ValueError(key + " missing in obstacle: " + name)
+            if type(d[key]) not in (float, int):
+                raise ValueError(key + " must be float or int for obstacle type ellipse: " + name)
+        if "inclination_angle" not in d:
+            raise ValueError("inclination_angle missing in obstacle: " + name)
+        if type(d["inclination_angle"]) not in (float, int):
+            raise ValueError("inclination_angle must be float or int for obstacle type ellipse "
+                             "representing angle in degrees: " + name)
+        if "center" not in d:
+            raise ValueError("center missing in obstacle: " + name)
+        if not isinstance(d["center"], list):
+            raise ValueError("center must be list for obstacle type ellipse: " + name)
+        if "density" not in d:
+            raise ValueError("density missing in obstacle: " + name)
+        if type(d["density"]) not in (float, int):
+            raise ValueError("density must be float or int for obstacle type ellipse: " + name)
+        if "static" not in d:
+            raise ValueError("static missing in obstacle: " + name)
+        if not isinstance(d["static"], (bool, np.bool_)):
+            raise ValueError("static must be True/False for obstacle type ellipse: " + name)
+
+    def _min_image_offsets(self, obs):
+        """Node offsets from the obstacle centre with the reference's periodic
+        minimum image (try r + N, then r - N), [nx, ny] each."""
         X, Y = np.meshgrid(np.arange(self.nx, dtype=np.float64),
                            np.arange(self.ny, dtype=np.float64), indexing="ij")
         rx = X - obs.center[0]
@@ -458,8 +506,9 @@ class Case:
             rym = np.where(np.abs(a) < np.abs(rym), a, rym)
             b = ry - self.ny
             rym = np.where(np.abs(b) < np.abs(rym), b, rym)
-        r = np.float64(obs.radius)
-        inside = rxm * rxm + rym * rym <= r * r
+        return rxm, rym
+
+    def _mark_solid(self, obs, inside, rxm, rym, solid=True):
         if solid:
             self.solid |= inside
             self.solid_id[inside] = obs.id
@@ -468,6 +517,29 @@ class Case:
         self.velocity[inside, 0] = lin[0] - ang * rym[inside]
         self.velocity[inside, 1] = lin[1] + ang * rxm[inside]
         self.density[inside] = obs.density
+
+    def _rasterise_ellipse(self, obs):
+        """(x'/a)^2 + (y'/b)^2 <= 1 in the frame turned by the inclination,
+        with the periodic minimum image (is_ellipse / construct_ellipse,
+        pylabolt/parallel/cpu/obstacle_kernels.py:151-241, same operation
+        order); solid nodes take the body velocity and density."""
+        a, b = (np.float64(v) for v in obs.semi_axes)
+        alpha = np.float64(obs.inclination) * np.pi / 180
+        cos_a, sin_a = np.cos(alpha), np.sin(alpha)
+        rxm, rym = self._min_image_offsets(obs)
+        xp = rxm * cos_a + rym * sin_a
+        yp = -rxm * sin_a + rym * cos_a
+        inside = (xp * xp) / (a * a) + (yp * yp) / (b * b) <= 1
+        self._mark_solid(obs, inside, rxm, rym)
+
+    def _rasterise_circle(self, obs, solid=True):
+        """dist^2 <= r^2 with the periodic minimum image (obstacle_kernels.py:11-93);
+        solid nodes take the body velocity and density.  solid=False (a moving
+        obstacle) sets only the fields: the device places it."""
+        rxm, rym = self._min_image_offsets(obs)
+        r = np.float64(obs.radius)
+        inside = rxm * rxm + rym * rym <= r * r
+        self._mark_solid(obs, inside, rxm, rym, solid)
 
     # ---- collision_dict -- collision_operator.py:46-104
     def _collision(self, cd):

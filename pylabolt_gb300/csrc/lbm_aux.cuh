@@ -115,6 +115,23 @@ struct Kernels {
     return cudaGetLastError();
   }
 
+  // The node-pair kernel (stages = register cap: 0 none, 1 40, 2 64).
+  template <int COLL, int FORC, bool RES>
+  static cudaError_t pair(const StepArgs& a, Variant v, dim3 grid, cudaStream_t s) {
+    if constexpr (Store<S>::shifted) {
+      if (v.stages == 0)
+        step_pair_kernel<S, COLL, FORC, 0, RES><<<grid, v.block, 0, s>>>(a);
+      else if (v.stages == 1)
+        step_pair_kernel<S, COLL, FORC, 1, RES><<<grid, v.block, 0, s>>>(a);
+      else if (v.stages == 2)
+        step_pair_kernel<S, COLL, FORC, 2, RES><<<grid, v.block, 0, s>>>(a);
+      else
+        return cudaErrorInvalidValue;
+      return cudaGetLastError();
+    }
+    return cudaErrorInvalidValue;
+  }
+
   template <int COLL, int FORC>
   static cudaError_t step_t(const StepArgs& a, Variant v, int sms, cudaStream_t s) {
     const dim3 grid = step_grid(a.g, v, sms, sizeof(S));
@@ -128,6 +145,11 @@ struct Kernels {
       return cudaGetLastError();
     }
     if constexpr (Store<S>::shifted) {
+      if (v.kind == 3) {   // node pairs (not for moving obstacles: class-4 nodes)
+        if (v.vec != 2 || v.block > 256 || a.rho_dyn_out) return cudaErrorInvalidValue;
+        if (a.flags & F_RESIDUAL) return pair<COLL, FORC, true>(a, v, grid, s);
+        return pair<COLL, FORC, false>(a, v, grid, s);
+      }
       if (v.kind == 2) {
         if (v.stages < 1 || v.stages > 8) return cudaErrorInvalidValue;
         const int smem = v.stages * tma_stage_bytes(sizeof(S));
@@ -243,12 +265,14 @@ struct Kernels {
       constexpr int V1 = sizeof(S) == 4 ? 4 : 8;
       constexpr int V2 = sizeof(S) == 4 ? 2 : 4;
       // kind 2: {threads, stages}; kind 1: {nodes per thread, threads};
-      // kind 0: {threads, register cap: 0 none, 1 32, 2 40}
+      // kind 0: {threads, register cap: 0 none, 1 32, 2 40};
+      // kind 3: node pairs {threads, register cap: 0 none, 1 40, 2 64}
       const Variant vs[] = {{2, 0, 256, 4}, {2, 0, 512, 3}, {2, 0, 256, 2}, {1, V1, 256, 0},
                             {1, V2, 256, 0}, {0, 1, 128, 0}, {0, 1, 256, 0}, {0, 1, 128, 1},
-                            {0, 1, 256, 1}, {0, 1, 128, 2}, {0, 1, 256, 2}};
-      k.nvariants = 11;
-      for (int i = 0; i < 11; ++i) k.variants[i] = vs[i];
+                            {0, 1, 256, 1}, {0, 1, 128, 2}, {0, 1, 256, 2}, {3, 2, 128, 0},
+                            {3, 2, 256, 0}, {3, 2, 128, 1}, {3, 2, 256, 2}};
+      k.nvariants = 15;
+      for (int i = 0; i < 15; ++i) k.variants[i] = vs[i];
     } else {
       const Variant vs[] = {{0, 1, 128, 0}, {0, 1, 256, 0}, {0, 1, 512, 0}};
       k.nvariants = 3;

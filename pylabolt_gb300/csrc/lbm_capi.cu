@@ -30,6 +30,17 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
+// 64-bit FNV-1a over n bytes, continuing from h.
+uint64_t fnv1a(uint64_t h, const void* p, size_t n) {
+  const unsigned char* b = static_cast<const unsigned char*>(p);
+  for (size_t i = 0; i < n; ++i) {
+    h ^= b[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+constexpr uint64_t kFnvSeed = 14695981039346656037ull;
+
 #define LBM_CUDA(expr)                                                         \
   do {                                                                         \
     cudaError_t e_ = (expr);                                                   \
@@ -53,6 +64,10 @@ struct LbmHandle {
   lbm::Geom g{};
   lbm::Params p{};
   cudaStream_t stream = nullptr;
+  // host transfers in column chunks: copies on `xfer`, transposes on `stream`
+  static constexpr int kXferChunks = 4;
+  cudaStream_t xfer = nullptr;
+  cudaEvent_t xev[kXferChunks + 1] = {};
   std::vector<std::pair<void*, size_t>> allocs;   // device allocations and their sizes
   size_t dev_bytes = 0;
   void* pop[2] = {nullptr, nullptr};      // first population plane
@@ -83,7 +98,10 @@ struct LbmHandle {
   int* err_host = nullptr;     // mapped pinned word the kernels set on a failed wait
   int* err_dev = nullptr;
   bool tuned = false;
-  double tune_ms[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double tune_ms[lbm::kMaxVariants] = {};
+  // hashes of what a saved state depends on besides the sizes: node classes,
+  // link table and relaxation parameters (lbm_create); the omega map
+  uint64_t case_hash = 0, omega_hash = 0;
   double timeout_s = 600.0;
   // host copies kept for the adjoint set-up
   std::vector<uint8_t> h_cls;
@@ -160,6 +178,9 @@ struct LbmHandle {
     for (cudaEvent_t e : adj.ev)
       if (e) cudaEventDestroy(e);
     if (adj.aux) cudaStreamDestroy(adj.aux);
+    for (cudaEvent_t e : xev)
+      if (e) cudaEventDestroy(e);
+    if (xfer) cudaStreamDestroy(xfer);
     for (auto& a : allocs) cudaFree(a.first);
     if (host_red) cudaFreeHost(host_red);
     if (err_host) cudaFreeHost(err_host);
@@ -217,6 +238,28 @@ struct LbmHandle {
       else
         std::this_thread::sleep_for(std::chrono::microseconds(200));
     }
+  }
+
+  // The copy stream and events of the chunked host transfers.
+  int ensure_xfer() {
+    if (xfer) return LBM_OK;
+    cudaStream_t st = nullptr;
+    LBM_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : xev) {
+      const cudaError_t r = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+      if (r != cudaSuccess) {
+        cudaStreamDestroy(st);
+        return fail(LBM_ERR_CUDA, std::string("cudaEventCreate: ") + cudaGetErrorString(r));
+      }
+    }
+    xfer = st;
+    return LBM_OK;
+  }
+  // First column of transfer chunk c (c = kXferChunks gives nx): multiples of
+  // the 32-column transpose tile.
+  int xfer_col(int c) const {
+    const int w = ((cfg.nx + kXferChunks - 1) / kXferChunks + 31) / 32 * 32;
+    return std::min(cfg.nx, c * w);
   }
 
   int ensure_stage(size_t elems) {
@@ -280,7 +323,8 @@ struct LbmHandle {
     for (int pass = 0; pass < 2 && rc == LBM_OK; ++pass)
       for (int i = 0; i < ks->nvariants && rc == LBM_OK; ++i) {
         const lbm::Variant v = ks->variants[i];
-        if (v.kind != 0) continue;
+        // the scalar and node-pair kernels have residual instantiations
+        if (v.kind != 0 && (v.kind != 3 || mov.n)) continue;
         if ((rc = launch_v(lbm::F_RESIDUAL, v, false))) break;
         cudaEventRecord(e0, stream);
         for (int r = 0; r < 4 && rc == LBM_OK; ++r) rc = launch_v(lbm::F_RESIDUAL, v, false);
@@ -536,7 +580,7 @@ struct LbmHandle {
     // twice, keeping each one's better mean (one short timing can be off by
     // a clock ramp or a neighbour's burst)
     if (rc == LBM_OK && ks->nvariants > 1) {
-      int order[12];
+      int order[lbm::kMaxVariants];
       for (int i = 0; i < ks->nvariants; ++i) order[i] = i;
       std::sort(order, order + ks->nvariants, [&](int x, int y) { return tune_ms[x] < tune_ms[y]; });
       const int top = std::min(3, ks->nvariants);
@@ -780,6 +824,20 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   h->ks = ks;
   h->h_cls = cls;
   h->h_links.assign(links, links + nlinks);
+  {   // field by field: the records' padding bytes are not part of the case
+    uint64_t hs = fnv1a(kFnvSeed, cls.data(), cls.size());
+    for (const LbmNodeLinks& L : h->h_links) {
+      hs = fnv1a(hs, &L.node, sizeof L.node);
+      hs = fnv1a(hs, L.src, sizeof L.src);
+      hs = fnv1a(hs, L.aux, sizeof L.aux);
+      hs = fnv1a(hs, L.param, sizeof L.param);
+      hs = fnv1a(hs, L.type, sizeof L.type);
+      hs = fnv1a(hs, &L.wall, sizeof L.wall);
+    }
+    const double rel[] = {c.omega, c.inv_cs_2, c.inv_cs_4, c.eps, c.gravity[0], c.gravity[1],
+                          c.mrt_s[0], c.mrt_s[1], c.mrt_s[2], c.mrt_s[3], c.fp16_scale};
+    h->case_hash = fnv1a(hs, rel, sizeof rel);
+  }
   auto bail = [&](int rc) {
     delete h;
     return rc;
@@ -952,10 +1010,32 @@ int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout
   if (direct) {   // transposed straight from the caller's pinned buffers
     LBM_CUDA(lbm::reorder(h->g, rd, ds, 1, layout, 1, h->stream));
     LBM_CUDA(lbm::reorder(h->g, ud, ds + plane, 2, layout, 1, h->stream));
+  } else if (layout == LBM_LAYOUT_INNER) {
+    // column chunks: chunk c is copied on the transfer stream while the
+    // handle's stream transposes chunk c - 1 (host order is x-major, so the
+    // columns x0 <= x < x1 are one contiguous run of each array)
+    if ((rc = h->ensure_xfer())) return rc;
+    double* hs = h->stage;   // host order: rho [nh], u [nh][2]
+    const long long ny = h->cfg.ny;
+    constexpr int NC = LbmHandle::kXferChunks;
+    LBM_CUDA(cudaEventRecord(h->xev[NC], h->stream));
+    LBM_CUDA(cudaStreamWaitEvent(h->xfer, h->xev[NC], 0));
+    for (int c = 0; c < NC; ++c) {
+      const int x0 = h->xfer_col(c), x1 = h->xfer_col(c + 1);
+      if (x0 >= x1) continue;
+      LBM_CUDA(cudaMemcpyAsync(hs + x0 * ny, rho + x0 * ny, (x1 - x0) * ny * sizeof(double),
+                               cudaMemcpyDefault, h->xfer));
+      LBM_CUDA(cudaMemcpyAsync(hs + nh + 2 * x0 * ny, u + 2 * x0 * ny, 2 * (x1 - x0) * ny * sizeof(double),
+                               cudaMemcpyDefault, h->xfer));
+      LBM_CUDA(cudaEventRecord(h->xev[c], h->xfer));
+      LBM_CUDA(cudaStreamWaitEvent(h->stream, h->xev[c], 0));
+      LBM_CUDA(lbm::reorder_cols(h->g, hs, ds, 1, layout, 1, x0, x1, h->stream));
+      LBM_CUDA(lbm::reorder_cols(h->g, hs + nh, ds + plane, 2, layout, 1, x0, x1, h->stream));
+    }
   } else {
     double* hs = h->stage;   // host order: rho [nh], u [nh][2]
-    LBM_CUDA(cudaMemcpyAsync(hs, rho, nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    LBM_CUDA(cudaMemcpyAsync(hs + nh, u, 2 * nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    LBM_CUDA(cudaMemcpyAsync(hs, rho, nh * sizeof(double), cudaMemcpyDefault, h->stream));
+    LBM_CUDA(cudaMemcpyAsync(hs + nh, u, 2 * nh * sizeof(double), cudaMemcpyDefault, h->stream));
     LBM_CUDA(lbm::reorder(h->g, hs, ds, 1, layout, 1, h->stream));
     LBM_CUDA(lbm::reorder(h->g, hs + nh, ds + plane, 2, layout, 1, h->stream));
   }
@@ -1002,7 +1082,7 @@ int lbm_set_body_force(LbmHandle* h, const double* force) {
   if (rc) return rc;
   double* hs = h->stage;
   double* ds = h->stage + 2 * nh;
-  LBM_CUDA(cudaMemcpyAsync(hs, force, 2 * nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(hs, force, 2 * nh * sizeof(double), cudaMemcpyDefault, h->stream));
   LBM_CUDA(cudaMemsetAsync(ds, 0, 2 * plane * sizeof(double), h->stream));
   LBM_CUDA(lbm::reorder(h->g, hs, ds, 2, LBM_LAYOUT_INNER, 1, h->stream));
   LBM_CUDA(h->ks->body_from_f64(h->g, ds, h->body, h->stream));
@@ -1036,6 +1116,7 @@ int lbm_set_omega_map(LbmHandle* h, const double* omega) {
   }
   LBM_CUDA(cudaMemcpyAsync(h->omega_seg, seg.data(), seg.size() * sizeof(float), cudaMemcpyHostToDevice,
                            h->stream));
+  h->omega_hash = fnv1a(kFnvSeed, seg.data(), seg.size() * sizeof(float));
   if (h->gexec) {   // graphs captured earlier hold the old argument
     cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
@@ -1212,7 +1293,7 @@ int lbm_adjoint_backward(LbmHandle* h, const double* grad_u, double* grad_force,
   const long long nh = (long long)g.nx * g.ny;
   int rc = h->ensure_stage(2 * nh);
   if (rc) return rc;
-  LBM_CUDA(cudaMemcpyAsync(h->stage, grad_u, 2 * nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(h->stage, grad_u, 2 * nh * sizeof(double), cudaMemcpyDefault, h->stream));
   LBM_CUDA(lbm::reorder(g, h->stage, A.grad_u, 2, LBM_LAYOUT_INNER, 1, h->stream));
   const int I = A.interval;
   const int64_t T = A.T;
@@ -1286,7 +1367,7 @@ int lbm_adjoint_backward(LbmHandle* h, const double* grad_u, double* grad_force,
     LBM_CUDA(h->ks->moments_to_f64(g, A.gF, static_cast<char*>(A.gF) + g.plane * h->ks->compute_bytes,
                                    A.gF, h->stage + 2 * nh, h->stream));
     LBM_CUDA(lbm::reorder(g, h->stage + 2 * nh, h->stage, 2, LBM_LAYOUT_INNER, 0, h->stream));
-    LBM_CUDA(cudaMemcpyAsync(grad_force, h->stage, 2 * nh * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    LBM_CUDA(cudaMemcpyAsync(grad_force, h->stage, 2 * nh * sizeof(double), cudaMemcpyDefault, h->stream));
     if ((rc = h->wait())) return rc;
   }
   double s[3] = {0, 0, 0};
@@ -1323,11 +1404,33 @@ int lbm_get_moments(LbmHandle* h, double* rho, double* u, int layout) {
   double* hs = h->stage;
   double* ds = h->stage + 3 * nh;
   LBM_CUDA(h->ks->moments_to_f64(h->g, h->mom[0], h->mom[1], h->mom[2], ds, h->stream));
-  LBM_CUDA(cudaMemsetAsync(hs, 0, 3 * nh * sizeof(double), h->stream));
+  if (layout == LBM_LAYOUT_INNER) {
+    // column chunks: chunk c goes to the host on the transfer stream while
+    // the handle's stream transposes chunk c + 1
+    if ((rc = h->ensure_xfer())) return rc;
+    const long long ny = h->cfg.ny;
+    constexpr int NC = LbmHandle::kXferChunks;
+    for (int c = 0; c < NC; ++c) {
+      const int x0 = h->xfer_col(c), x1 = h->xfer_col(c + 1);
+      if (x0 >= x1) continue;
+      LBM_CUDA(lbm::reorder_cols(h->g, ds, hs, 1, layout, 0, x0, x1, h->stream));
+      LBM_CUDA(lbm::reorder_cols(h->g, ds + plane, hs + nh, 2, layout, 0, x0, x1, h->stream));
+      LBM_CUDA(cudaEventRecord(h->xev[c], h->stream));
+      LBM_CUDA(cudaStreamWaitEvent(h->xfer, h->xev[c], 0));
+      LBM_CUDA(cudaMemcpyAsync(rho + x0 * ny, hs + x0 * ny, (x1 - x0) * ny * sizeof(double),
+                               cudaMemcpyDefault, h->xfer));
+      LBM_CUDA(cudaMemcpyAsync(u + 2 * x0 * ny, hs + nh + 2 * x0 * ny, 2 * (x1 - x0) * ny * sizeof(double),
+                               cudaMemcpyDefault, h->xfer));
+    }
+    LBM_CUDA(cudaEventRecord(h->xev[NC], h->xfer));
+    LBM_CUDA(cudaStreamWaitEvent(h->stream, h->xev[NC], 0));
+    return h->wait();
+  }
+  LBM_CUDA(cudaMemsetAsync(hs, 0, 3 * nh * sizeof(double), h->stream));   // ghosts of the padded layout
   LBM_CUDA(lbm::reorder(h->g, ds, hs, 1, layout, 0, h->stream));
   LBM_CUDA(lbm::reorder(h->g, ds + plane, hs + nh, 2, layout, 0, h->stream));
-  LBM_CUDA(cudaMemcpyAsync(rho, hs, nh * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  LBM_CUDA(cudaMemcpyAsync(u, hs + nh, 2 * nh * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(rho, hs, nh * sizeof(double), cudaMemcpyDefault, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(u, hs + nh, 2 * nh * sizeof(double), cudaMemcpyDefault, h->stream));
   return h->wait();
 }
 
@@ -1370,7 +1473,7 @@ int lbm_get_populations(LbmHandle* h, double* pop) {
   LBM_CUDA(h->ks->convert(h->g, h->p, h->pop[h->cur], ds, 0, h->aa_state(), h->stream));
   LBM_CUDA(cudaMemsetAsync(hs, 0, 9 * nh * sizeof(double), h->stream));
   LBM_CUDA(lbm::reorder(h->g, ds, hs, 9, LBM_LAYOUT_PADDED, 0, h->stream));
-  LBM_CUDA(cudaMemcpyAsync(pop, hs, 9 * nh * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(pop, hs, 9 * nh * sizeof(double), cudaMemcpyDefault, h->stream));
   return h->wait();
 }
 
@@ -1384,7 +1487,7 @@ int lbm_set_populations(LbmHandle* h, const double* pop_new) {
   h->initialized = false;   // until the new state is complete
   double* hs = h->stage;
   double* ds = h->stage + 9 * nh;
-  LBM_CUDA(cudaMemcpyAsync(hs, pop_new, 9 * nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(hs, pop_new, 9 * nh * sizeof(double), cudaMemcpyDefault, h->stream));
   LBM_CUDA(cudaMemsetAsync(ds, 0, 9 * plane * sizeof(double), h->stream));
   LBM_CUDA(lbm::reorder(h->g, hs, ds, 9, LBM_LAYOUT_PADDED, 1, h->stream));
   if (h->aa) h->cur = 0;   // AA: the next step is an even phase that reads the set values
@@ -1480,7 +1583,7 @@ int lbm_forces(LbmHandle* h, double* out) {
   a.aa_state = h->aa_state();
   a.out = F.out;
   LBM_CUDA(h->ks->forces(a, F.ngroups, h->stream));
-  LBM_CUDA(cudaMemcpyAsync(out, F.out, 3 * (size_t)F.ngroups * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(out, F.out, 3 * (size_t)F.ngroups * sizeof(double), cudaMemcpyDefault, h->stream));
   return h->wait();
 }
 
@@ -1695,8 +1798,13 @@ struct StateHeader {
   int32_t cur, nopull, has_old, old_cur, mov_n;
   int64_t plane, t;
   uint64_t pop_bytes, side_bytes, old_bytes, mov_bytes;
+  uint64_t case_hash, omega_hash;
+  // launch shapes of the saving handle (launch shapes round FP32 / FP16
+  // arithmetic differently, so a restart keeps them instead of re-tuning)
+  int32_t tuned, res_tuned;
+  int32_t variant[4], res_variant[4];   // kind, vec, block, stages
 };
-constexpr int32_t kStateVersion = 2;
+constexpr int32_t kStateVersion = 3;
 
 // Moving-obstacle part of the state: obstacles, node classes and segment
 // flags (they follow the obstacles), solid / refill flags, solid velocity and
@@ -1742,7 +1850,39 @@ StateHeader state_header(const LbmHandle* h) {
   H.pop_bytes = h->state_bytes();
   H.side_bytes = h->side_bytes();
   H.old_bytes = H.has_old ? 6 * (uint64_t)h->g.plane * h->ks->compute_bytes : 0;
+  H.case_hash = h->case_hash;
+  H.omega_hash = h->omega_hash;
+  H.tuned = h->tuned ? 1 : 0;
+  H.res_tuned = h->res_tuned ? 1 : 0;
+  const lbm::Variant* vs[2] = {&h->variant, &h->res_variant};
+  int32_t* outs[2] = {H.variant, H.res_variant};
+  for (int i = 0; i < 2; ++i) {
+    outs[i][0] = vs[i]->kind;
+    outs[i][1] = vs[i]->vec;
+    outs[i][2] = vs[i]->block;
+    outs[i][3] = vs[i]->stages;
+  }
   return H;
+}
+
+// A saved launch shape, if the handle may run it: one of the storage's
+// candidates, or for the AA layout the scalar kernel with 32..256 threads.
+bool valid_variant(const LbmHandle* h, const int32_t v[4], lbm::Variant* out) {
+  const lbm::Variant w{v[0], v[1], v[2], v[3]};
+  if (h->aa) {
+    if (w.kind != 0 || w.vec != 1 || w.block < 32 || w.block > 256 || w.block % 32) return false;
+    *out = w;
+    return true;
+  }
+  for (int i = 0; i < h->ks->nvariants; ++i) {
+    const lbm::Variant& c = h->ks->variants[i];
+    if (c.kind == w.kind && c.vec == w.vec && c.block == w.block && c.stages == w.stages) {
+      if (h->mov.n && c.kind != 0) return false;
+      *out = c;
+      return true;
+    }
+  }
+  return false;
 }
 }  // namespace
 
@@ -1792,6 +1932,13 @@ int lbm_load_state(LbmHandle* h, const void* in) {
       H.old_bytes != (H.has_old ? 6 * (uint64_t)h->g.plane * h->ks->compute_bytes : 0))
     return fail(LBM_ERR_ARG, "lbm_load_state: the state was saved from a case with another grid, "
                              "storage, collision, forcing, layout, link table or moving obstacles");
+  if (H.case_hash != M.case_hash || H.omega_hash != M.omega_hash)
+    return fail(LBM_ERR_ARG, "lbm_load_state: the state was saved from a case with another "
+                             "obstacle layout, link table, relaxation parameters or omega map");
+  lbm::Variant v_plain = h->variant, v_res = h->res_variant;
+  if ((H.tuned && !valid_variant(h, H.variant, &v_plain)) ||
+      (H.res_tuned && !valid_variant(h, H.res_variant, &v_res)))
+    return fail(LBM_ERR_ARG, "lbm_load_state: the saved launch shape is not one this handle runs");
   LBM_CUDA(cudaSetDevice(h->cfg.device));
   int rc;
   if (H.has_old && (rc = h->ensure_old())) return rc;
@@ -1823,6 +1970,16 @@ int lbm_load_state(LbmHandle* h, const void* in) {
   h->old_cur = H.has_old ? H.old_cur : 0;
   h->t = H.t;
   h->nopull = H.nopull != 0;
+  // the saved launch shapes continue the run in the same rounding; a shape
+  // not yet tuned when the state was saved is tuned by this handle
+  if (H.tuned) {
+    h->variant = v_plain;
+    h->tuned = true;
+  }
+  if (H.res_tuned) {
+    h->res_variant = v_res;
+    h->res_tuned = true;
+  }
   h->has_moments = false;
   h->has_residual = false;
   h->initialized = true;

@@ -170,6 +170,8 @@ struct MovArgs {
 //   kind 1: vector kernel, `vec` consecutive nodes per thread
 //   kind 2: persistent TMA-pipelined kernel: tiles of one row segment of
 //           kTmaRowBytes, `stages` shared-memory stages, `block` threads
+//   kind 3: node-pair kernel, two nodes per thread (vec = 2), `stages` its
+//           register cap
 struct Variant {
   int kind;
   int vec;
@@ -177,6 +179,7 @@ struct Variant {
   int stages;
 };
 
+constexpr int kMaxVariants = 16;     // autotuner candidates per storage at most
 constexpr int kTmaRowBytes = 4096;   // tile width in bytes of one plane row
 constexpr int kTmaHaloBytes = 16;    // TMA granule: halo on each side
 constexpr int kErrWaitTimeout = 1;   // err code: an mbarrier wait timed out
@@ -194,7 +197,7 @@ struct KernelSet {
   cudaError_t (*step)(int collision, int forcing, const StepArgs& a, Variant v,
                       int sms, cudaStream_t s);
   int nvariants;             // candidate launch shapes for the autotuner
-  Variant variants[12];
+  Variant variants[kMaxVariants];
   // f_eq(rho,u) into storage on fluid nodes (zeros on solids); moments get
   // rho/u on every node.  rho [plane], u [2][plane], FP64, device order.
   cudaError_t (*init)(const Geom& g, const Params& p, const double* rho,
@@ -259,6 +262,9 @@ inline dim3 step_grid(const Geom& g, Variant v, int sms, int elem_bytes) {
 // (ind = (x+1)*(ny+2)+(y+1)) order; device SoA [ncomp][plane].
 cudaError_t reorder(const Geom& g, const double* in, double* out, int ncomp,
                     int layout, int to_device, cudaStream_t s);
+// The same for the columns x_lo <= x < x_hi only.
+cudaError_t reorder_cols(const Geom& g, const double* in, double* out, int ncomp,
+                         int layout, int to_device, int x_lo, int x_hi, cudaStream_t s);
 
 // Sets the message lbm_last_error() returns on this thread.
 void record_error(const std::string& msg);

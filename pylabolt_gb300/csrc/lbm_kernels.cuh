@@ -887,6 +887,118 @@ __global__ void __launch_bounds__(CAP ? 256 : 512, CAP == 1 ? 8 : (CAP == 2 ? 6 
 }
 
 // ---------------------------------------------------------------------------
+// Node pairs: one thread updates nodes (x0, y) and (x0 + 1, y), x0 even, and
+// moves every population plane as one aligned word holding both nodes (two
+// halves for FP16 storage, two floats for FP32).  A direction with c_kx = 0
+// reads the word at x0 of its source row y - c_ky.  c_kx = +1 needs the
+// values at (x0 - 1, x0): the upper half of the word at x0 - 2 and the lower
+// half of the word at x0; c_kx = -1 needs (x0 + 1, x0 + 2): the upper half
+// of the word at x0 and the lower half of the word at x0 + 2.  The extra
+// word is a neighbouring thread's own word, so it comes from L1.  This halves
+// the per-node cost of addressing, class checks, loads, stores and the
+// float -> half packing, which bound the one-node-per-thread FP16 step (it
+// issues as many instructions per node as the FP32 one for half the bytes).
+//
+// A pair whose 32-node row segment holds any boundary, solid or padding node
+// (segflag), and every pair of a no-pull step, takes the per-node scalar path
+// for both nodes, so link records are handled exactly as by step_kernel.
+template <class S> struct PairIO;
+template <> struct PairIO<__half> {
+  using W = uint32_t;
+  __device__ static __forceinline__ W ld(const W* __restrict__ p, long long i) { return p[i]; }
+  // upper value of word a, lower value of word b
+  __device__ static __forceinline__ W mid(W a, W b) { return __byte_perm(a, b, 0x5432); }
+  __device__ static __forceinline__ void unpack(W w, float& lo, float& hi) {
+    __half2 h;
+    memcpy(&h, &w, 4);
+    const float2 t = __half22float2(h);
+    lo = t.x;
+    hi = t.y;
+  }
+  __device__ static __forceinline__ W pack(float lo, float hi) {
+    const __half2 h = __floats2half2_rn(lo, hi);
+    W w;
+    memcpy(&w, &h, 4);
+    return w;
+  }
+};
+template <> struct PairIO<float> {
+  using W = float2;
+  __device__ static __forceinline__ W ld(const W* __restrict__ p, long long i) { return p[i]; }
+  __device__ static __forceinline__ W mid(W a, W b) { return make_float2(a.y, b.x); }
+  __device__ static __forceinline__ void unpack(W w, float& lo, float& hi) {
+    lo = w.x;
+    hi = w.y;
+  }
+  __device__ static __forceinline__ W pack(float lo, float hi) { return make_float2(lo, hi); }
+};
+
+// Incoming word of direction K for the pair at word index wi (both nodes).
+template <class S, int K>
+__device__ __forceinline__ typename PairIO<S>::W pair_pull(const typename PairIO<S>::W* __restrict__ fw,
+                                                           const Geom& g, long long wi) {
+  using IO = PairIO<S>;
+  constexpr int cx = CXk(K), cy = CYk(K);
+  const long long r = (long long)K * (g.plane >> 1) - (long long)cy * (g.pitch >> 1) + wi;
+  if (cx == 0) return IO::ld(fw, r);
+  if (cx == 1) return IO::mid(IO::ld(fw, r - 1), IO::ld(fw, r));
+  return IO::mid(IO::ld(fw, r), IO::ld(fw, r + 1));
+}
+
+// CAP = 1 asks for 6 resident blocks of 256 threads (at most 40 registers),
+// CAP = 2 for 4 (at most 64).  RES: the residual instantiation.
+template <class S, int COLL, int FORC, int CAP, bool RES>
+__global__ void __launch_bounds__(256, CAP == 1 ? 6 : (CAP == 2 ? 4 : 1))
+    step_pair_kernel(const StepArgs a) {
+  using IO = PairIO<S>;
+  using W = typename IO::W;
+  const Geom& g = a.g;
+  const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int y = blockIdx.y;
+  float red[7] = {0, 0, 0, 0, 0, 0, 0};
+  if (x0 < g.nx) {
+    const int seg = y * g.nseg + (x0 >> 5);
+    if (g.segflag[seg] != 0 || (a.flags & F_NOPULL)) {
+      step_node<S, COLL, FORC, false, RES>(a, x0, y, red);
+      if (x0 + 1 < g.nx) step_node<S, COLL, FORC, false, RES>(a, x0 + 1, y, red);
+    } else {
+      // both nodes are bulk nodes: every source is inside the grid
+      const int ni = (y + 1) * g.pitch + x0;   // even: pitch and x0 are even
+      const long long n = ni;
+      const long long wi = ni >> 1;
+      const W* __restrict__ fw = reinterpret_cast<const W*>(static_cast<const S*>(a.fin));
+      W* __restrict__ ow = reinterpret_cast<W*>(static_cast<S*>(a.fout));
+      float old0[3], old1[3];
+      if (RES) {
+        load_old<float>(a, n, old0);
+        load_old<float>(a, n + 1, old1);
+      }
+      W w[9];
+      w[0] = pair_pull<S, 0>(fw, g, wi);
+      w[1] = pair_pull<S, 1>(fw, g, wi);
+      w[2] = pair_pull<S, 2>(fw, g, wi);
+      w[3] = pair_pull<S, 3>(fw, g, wi);
+      w[4] = pair_pull<S, 4>(fw, g, wi);
+      w[5] = pair_pull<S, 5>(fw, g, wi);
+      w[6] = pair_pull<S, 6>(fw, g, wi);
+      w[7] = pair_pull<S, 7>(fw, g, wi);
+      w[8] = pair_pull<S, 8>(fw, g, wi);
+      float f0[9], f1[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) IO::unpack(w[k], f0[k], f1[k]);
+      float rho0, ux0, uy0, rho1, ux1, uy1;
+      node_update<S, COLL, FORC>(f0, a, n, rho0, ux0, uy0, seg);
+      node_update<S, COLL, FORC>(f1, a, n + 1, rho1, ux1, uy1, seg);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) ow[(long long)k * (g.plane >> 1) + wi] = IO::pack(f0[k], f1[k]);
+      node_outputs<float, RES ? RES_ON : RES_OFF>(a, n, -1, rho0, ux0, uy0, red, old0);
+      node_outputs<float, RES ? RES_ON : RES_OFF>(a, n + 1, -1, rho1, ux1, uy1, red, old1);
+    }
+  }
+  if (RES) block_residual<float>(a, red);
+}
+
+// ---------------------------------------------------------------------------
 // Vector I/O of V consecutive nodes (16- or 8-byte aligned accesses).
 template <class S, int V> struct VecIO;
 template <int V> struct VecIO<float, V> {

@@ -47,32 +47,32 @@ constexpr int kTile = 32, kTileRows = 8;
 
 __global__ void __launch_bounds__(kTile * kTileRows)
     reorder_kernel(const Geom g, const double* __restrict__ in, double* __restrict__ out,
-                   int ncomp, int layout, int to_device) {
+                   int ncomp, int layout, int to_device, int x_lo, int x_hi) {
   __shared__ double t[kTile][kTile + 1];
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int x0 = blockIdx.x * kTile, y0 = blockIdx.y * kTile;
+  const int x0 = x_lo + blockIdx.x * kTile, y0 = blockIdx.y * kTile;
   const long long hy = layout == 0 ? g.ny : g.ny + 2;   // host stride of x
   const int off = layout == 0 ? 0 : 1;
   for (int c = 0; c < ncomp; ++c) {
     if (to_device) {
       for (int r = ty; r < kTile; r += kTileRows) {   // host rows: x = x0 + r, lanes along y
         const int x = x0 + r, y = y0 + tx;
-        if (x < g.nx && y < g.ny) t[r][tx] = in[((x + off) * hy + y + off) * ncomp + c];
+        if (x < x_hi && y < g.ny) t[r][tx] = in[((x + off) * hy + y + off) * ncomp + c];
       }
       __syncthreads();
       for (int r = ty; r < kTile; r += kTileRows) {   // device rows: y = y0 + r, lanes along x
         const int x = x0 + tx, y = y0 + r;
-        if (x < g.nx && y < g.ny) out[c * g.plane + g.node(x, y)] = t[tx][r];
+        if (x < x_hi && y < g.ny) out[c * g.plane + g.node(x, y)] = t[tx][r];
       }
     } else {
       for (int r = ty; r < kTile; r += kTileRows) {
         const int x = x0 + tx, y = y0 + r;
-        if (x < g.nx && y < g.ny) t[r][tx] = in[c * g.plane + g.node(x, y)];
+        if (x < x_hi && y < g.ny) t[r][tx] = in[c * g.plane + g.node(x, y)];
       }
       __syncthreads();
       for (int r = ty; r < kTile; r += kTileRows) {
         const int x = x0 + r, y = y0 + tx;
-        if (x < g.nx && y < g.ny) out[((x + off) * hy + y + off) * ncomp + c] = t[tx][r];
+        if (x < x_hi && y < g.ny) out[((x + off) * hy + y + off) * ncomp + c] = t[tx][r];
       }
     }
     __syncthreads();
@@ -81,8 +81,15 @@ __global__ void __launch_bounds__(kTile * kTileRows)
 
 cudaError_t reorder(const Geom& g, const double* in, double* out, int ncomp,
                     int layout, int to_device, cudaStream_t s) {
-  dim3 grid((g.nx + kTile - 1) / kTile, (g.ny + kTile - 1) / kTile);
-  reorder_kernel<<<grid, dim3(kTile, kTileRows), 0, s>>>(g, in, out, ncomp, layout, to_device);
+  return reorder_cols(g, in, out, ncomp, layout, to_device, 0, g.nx, s);
+}
+
+cudaError_t reorder_cols(const Geom& g, const double* in, double* out, int ncomp,
+                         int layout, int to_device, int x_lo, int x_hi, cudaStream_t s) {
+  if (x_lo < 0 || x_hi > g.nx || x_lo >= x_hi) return cudaErrorInvalidValue;
+  dim3 grid((x_hi - x_lo + kTile - 1) / kTile, (g.ny + kTile - 1) / kTile);
+  reorder_kernel<<<grid, dim3(kTile, kTileRows), 0, s>>>(g, in, out, ncomp, layout, to_device,
+                                                         x_lo, x_hi);
   return cudaGetLastError();
 }
 

@@ -3,12 +3,15 @@
 //
 // Why it exists: some callers of this library cannot allocate device memory.
 // Examples are in-situ analysis code embedded in a larger solver that hands
-// out all device memory from its own pool, code that runs while a stream is
-// being captured (where cudaMalloc is not permitted), and monitoring loops
-// that cannot afford cudaMalloc's implicit device synchronisation.  This entry
-// point takes device pointers to its input and output and keeps its scratch
-// (one partial-sum row per grid row plus the second reduction stage) in a
-// fixed, file-scope device array instead of allocating it.
+// out all device memory from its own pool, and monitoring loops that cannot
+// afford cudaMalloc's implicit device synchronisation.  This entry point
+// takes device pointers to its input and output and keeps its scratch (one
+// partial-sum row per grid row plus the second reduction stage) in a fixed,
+// file-scope device array instead of allocating it.
+//
+// The device address of that array is looked up once per device, on the
+// first call with that device current, and kept for the life of the process;
+// a cudaDeviceReset of the device makes it stale (the header says so).
 //
 // The scratch array below is part of the library image: every GPU that loads
 // liblbm_gb300.so holds it (about 0.5 MB) until the process exits.

@@ -39,10 +39,24 @@ def make_config(case, storage=None, device=0, layout=None):
     return cfg
 
 
+def _is_tensor(a):
+    return hasattr(a, "data_ptr") and hasattr(a, "is_cuda")
+
+
+def _dptr(a):
+    """ctypes pointer of a C-contiguous float64 array: a numpy array (host) or
+    a torch tensor (host or CUDA; the C-ABI picks the copy direction)."""
+    if _is_tensor(a):
+        if not a.is_contiguous() or str(a.dtype) != "torch.float64":
+            raise ValueError("tensor arguments must be contiguous float64")
+        return ctypes.c_void_p(a.data_ptr())
+    return ptr(a)
+
+
 class FluidLBM:
     """One fluidLB case resident on the GPU."""
 
-    def __init__(self, case, storage=None, device=0, layout=None):
+    def __init__(self, case, storage=None, device=0, layout=None, body_force=None):
         if not isinstance(case, Case):
             case = Case(case)
         self.case = case
@@ -58,7 +72,8 @@ class FluidLBM:
                                   ptr(self.links), len(self.links), ctypes.byref(h)))
         self.h = h
         if case.body_force_field is not None:
-            self.set_body_force(case.body_force_field)
+            # body_force: the same field as an array or tensor (e.g. on the GPU)
+            self.set_body_force(case.body_force_field if body_force is None else body_force)
         if case.moving:
             arr = (capi.LbmMovingObstacle * len(case.moving))()
             for a, o in zip(arr, case.moving):
@@ -105,8 +120,16 @@ class FluidLBM:
         check(self.lib.lbm_init_fields(self.h, ptr(rho), ptr(u), capi.LAYOUT_INNER))
 
     def set_body_force(self, force):
-        f = np.ascontiguousarray(force, dtype=np.float64)
-        check(self.lib.lbm_set_body_force(self.h, ptr(f)))
+        """[Nx, Ny, 2] body-force field: a numpy array or a float64 torch
+        tensor (a CUDA tensor is read on the device, after its stream)."""
+        if _is_tensor(force):
+            f = force.contiguous()
+            if f.is_cuda:
+                import torch
+                torch.cuda.current_stream(f.device).synchronize()
+        else:
+            f = np.ascontiguousarray(force, dtype=np.float64)
+        check(self.lib.lbm_set_body_force(self.h, _dptr(f)))
 
     # -- time stepping
     def step(self, nsteps=1, moments=False, residual=False):
@@ -135,6 +158,13 @@ class FluidLBM:
             u = np.empty((n, 2))
         else:
             rho, u = out
+            if _is_tensor(rho) and _is_tensor(u):   # e.g. CUDA tensors: filled on the device
+                if rho.numel() != n or u.numel() != 2 * n:
+                    raise ValueError("moments(out=...): tensors of the grid size")
+                check(self.lib.lbm_get_moments(self.h, _dptr(rho), _dptr(u), layout))
+                if layout == capi.LAYOUT_INNER:
+                    return rho.view(nx, ny), u.view(nx, ny, 2)
+                return rho, u
             if (rho.dtype != np.float64 or u.dtype != np.float64 or rho.size != n
                     or u.size != 2 * n or not rho.flags.c_contiguous or not u.flags.c_contiguous):
                 raise ValueError("moments(out=...): C-contiguous float64 arrays of the grid size")
@@ -230,14 +260,24 @@ class FluidLBM:
     def adjoint_backward(self, grad_u, want_force=True):
         """Reverse pass for dL/du of the last step ([Nx, Ny, 2]).  Returns
         (dL/dF [Nx, Ny, 2] or None, dL/dtau, dL/du_wall [2]).  dL/du at solid
-        nodes is ignored (their velocity is the body's, not computed)."""
+        nodes is ignored (their velocity is the body's, not computed).  A
+        float64 CUDA tensor grad_u is read on the device, and dL/dF is then a
+        CUDA tensor on the same device."""
         nx, ny = self.case.nx, self.case.ny
-        gu = np.ascontiguousarray(np.asarray(grad_u, dtype=np.float64).reshape(nx * ny, 2))
-        gF = np.empty((nx * ny, 2)) if (want_force and self.case.body_force_field is not None) else None
+        want_f = want_force and self.case.body_force_field is not None
+        if _is_tensor(grad_u) and grad_u.is_cuda:
+            import torch
+            gu = grad_u.detach().to(torch.float64).contiguous()
+            torch.cuda.current_stream(gu.device).synchronize()
+            gF = torch.empty((nx, ny, 2), dtype=torch.float64, device=gu.device) if want_f else None
+        else:
+            gu = np.ascontiguousarray(np.asarray(grad_u, dtype=np.float64).reshape(nx * ny, 2))
+            gF = np.empty((nx, ny, 2)) if want_f else None
         gtau = ctypes.c_double()
         guw = (ctypes.c_double * 2)()
-        check(self.lib.lbm_adjoint_backward(self.h, ptr(gu), ptr(gF), ctypes.byref(gtau), guw))
-        return (gF.reshape(nx, ny, 2) if gF is not None else None), gtau.value, np.array(guw[:])
+        check(self.lib.lbm_adjoint_backward(self.h, _dptr(gu), _dptr(gF) if gF is not None else None,
+                                            ctypes.byref(gtau), guw))
+        return gF, gtau.value, np.array(guw[:])
 
     # -- checkpoint / restart (lbm_save_state / lbm_load_state)
     def save_state(self):
@@ -269,7 +309,7 @@ class FluidLBM:
     @property
     def kernel_variant(self):
         """(kind, nodes per thread, threads per block, stages) of the fused
-        step; kind 0 scalar, 1 vector, 2 TMA pipeline."""
+        step; kind 0 scalar, 1 vector, 2 TMA pipeline, 3 node pairs."""
         out = (ctypes.c_int * 4)()
         check(self.lib.lbm_kernel_variant(self.h, out))
         return tuple(out[:])
@@ -277,7 +317,7 @@ class FluidLBM:
     @property
     def tuning(self):
         """Mean step time (ms) of every autotuner candidate."""
-        out = (ctypes.c_double * 12)()
+        out = (ctypes.c_double * 16)()
         n = ctypes.c_int()
         check(self.lib.lbm_tuning(self.h, out, ctypes.byref(n)))
         return list(out[:n.value])

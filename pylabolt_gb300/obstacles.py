@@ -10,9 +10,12 @@ and writes in every ``output/fields/t_<n>.npz``:
                       -1 elsewhere
 * ``solid_boundary``  solid node with a non-solid neighbour (:307-350)
 * ``fluid_boundary``  fluid node with a solid neighbour (:307-350)
-* ``surface_normals`` unit vector from the circle centre (minimum image on
-                      periodic axes) on the boundary nodes of each circle
-                      (compute_normals_circle :95-143)
+* ``surface_normals`` on the boundary nodes of each obstacle: the unit
+                      vector from a circle's centre (minimum image on
+                      periodic axes; compute_normals_circle :95-143), or an
+                      ellipse's unit gradient of (x'/a)^2 + (y'/b)^2 turned
+                      back by the inclination (compute_normals_ellipse
+                      :244-302)
 
 Ghost nodes carry what the reference's single-rank ``halo_exchange_cpu``
 leaves there before these kernels run (pylabolt/base/obstacle_operator.py:
@@ -98,6 +101,16 @@ class Geometry:
             cx, cy = centers.get(obs.id, obs.center)
             rx = _min_image(X - cx, nx, self.x_periodic)
             ry = _min_image(Y - cy, ny, self.y_periodic)
+            if obs.type == "ellipse":
+                a, b = (np.float64(v) for v in obs.semi_axes)
+                alpha = np.float64(obs.inclination) * np.pi / 180
+                cos_a, sin_a = np.cos(alpha), np.sin(alpha)
+                xp = rx * cos_a + ry * sin_a
+                yp = -rx * sin_a + ry * cos_a
+                gx = xp / (a * a)
+                gy = yp / (b * b)
+                rx = gx * cos_a - gy * sin_a
+                ry = gx * sin_a + gy * cos_a
             mag = np.sqrt(rx * rx + ry * ry)
             with np.errstate(invalid="ignore", divide="ignore"):
                 normals[..., 0] = np.where(sel, rx / mag, normals[..., 0])

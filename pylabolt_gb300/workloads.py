@@ -8,6 +8,8 @@ here from its stated shape and parameters, with seeded random perturbations.
 * ``cylinder``   channel with a cylinder, anti-bounce-back pressure inlet /
                  outlet, bounce-back walls and cylinder, seeded +-1e-4 velocity
                  perturbation (numpy default_rng(seed))
+* ``outlet_channel`` the same channel with a zero_gradient outlet
+* ``ellipse_channel`` the same channel with an inclined ellipse
 """
 import numpy as np
 
@@ -84,6 +86,20 @@ def poiseuille_profile(ny, gx, kin_visc):
     return gx / (2.0 * kin_visc) * y * (ny - y)
 
 
+def poiseuille_startup_profile(ny, gx, kin_visc, t, terms=200):
+    """u_x(y, t) of plane Poiseuille flow started from rest at t = 0 (walls at
+    y = -1/2 and y = ny - 1/2): the parabola minus its decaying Fourier
+    series, sum over odd n of 4 g H^2 / (nu (n pi)^3) sin(n pi y / H)
+    exp(-nu (n pi / H)^2 t)."""
+    h = float(ny)
+    y = np.arange(ny) + 0.5
+    u = gx / (2.0 * kin_visc) * y * (h - y)
+    for n in range(1, 2 * terms, 2):
+        u -= (4.0 * gx * h * h / (kin_visc * (n * np.pi) ** 3) * np.sin(n * np.pi * y / h) *
+              np.exp(-kin_visc * (n * np.pi / h) ** 2 * t))
+    return u
+
+
 def cylinder(nx=8192, ny=2048, model="BGK", storage=None, kin_visc=0.04, radius=128.0,
              center=(2048, 1027), rho_in=1.0005, rho_out=1.0, seed=0, amp=1e-4,
              rates=(1.4, 1.4, 1.2)):
@@ -107,6 +123,41 @@ def cylinder(nx=8192, ny=2048, model="BGK", storage=None, kin_visc=0.04, radius=
     rng = np.random.default_rng(seed)
     u0 = rng.uniform(-amp, amp, size=(nx, ny, 2))
     c["initial_fields_dict"]["default"]["fluid"]["velocity"] = {"type": "array", "value": u0}
+    return c
+
+
+def ellipse_channel(nx=512, ny=128, semi_axes=(24.0, 8.0), inclination=20.0, seed=0,
+                    kin_visc=0.04, rho_in=1.0005, storage=None, model="BGK"):
+    """The cylinder channel with an inclined ellipse (semi-axes a, b, angle
+    in degrees) at (nx/4, ny/2 + 3) in place of the cylinder."""
+    c = cylinder(nx=nx, ny=ny, model=model, storage=storage, kin_visc=kin_visc,
+                 rho_in=rho_in, seed=seed)
+    c["obstacle_dict"].pop("cylinder")
+    c["obstacle_dict"]["wing"] = {"type": "ellipse", "semi_major_axis": float(semi_axes[0]),
+                                  "semi_minor_axis": float(semi_axes[1]),
+                                  "inclination_angle": float(inclination),
+                                  "center": [nx // 4, ny // 2 + 3], "density": 1.0,
+                                  "static": True}
+    return c
+
+
+def outlet_channel(nx, ny, outlet_last=True, seed=0):
+    """The cylinder channel with a zero_gradient outlet in place of the
+    fixed-pressure one: anti-bounce-back inlet (rho 1.0005), bounce-back
+    walls, cylinder of radius ny/8 at (nx/4, ny/2 + 3).  outlet_last: the
+    outlet is listed after the walls and wins at its two corners, where its
+    sources leave the grid; otherwise the walls win there."""
+    c = cylinder(nx=nx, ny=ny, radius=ny / 8.0, center=(nx // 4, ny // 2 + 3), seed=seed)
+    b = c["boundary_dict"]
+    outlet = b.pop("outlet")
+    outlet["fluid"] = {"type": "zero_gradient"}
+    walls = b.pop("walls")
+    if outlet_last:
+        b["walls"] = walls
+        b["outlet"] = outlet
+    else:
+        b["outlet"] = outlet
+        b["walls"] = walls
     return c
 
 

@@ -1,8 +1,8 @@
 """Generate the case-validation fixture from the reference's own classes.
 
-Run in a container that has the reference checkout at /root/reference:
+Run where a checkout of the reference is available:
 
-    python tests/golden/make_config_golden.py [--ref /root/reference]
+    python tests/golden/make_config_golden.py --ref <path of the reference checkout>
 
 Each entry applies one mutation (a list of set / delete operations on a key
 path) to a valid golden case and records the message (all lines) the
@@ -30,7 +30,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 import make_golden as mg   # noqa: E402
 
-CYL, PER = "channel_cylinder_abb", "poiseuille_guo2"
+CYL, PER, ELL = "channel_cylinder_abb", "poiseuille_guo2", "channel_ellipses"
 B = "boundary_dict"
 O = "obstacle_dict"
 F = ["initial_fields_dict", "default", "fluid"]
@@ -97,6 +97,20 @@ MUTATIONS = [
     ("density a string", CYL, [("set", [O, "cyl", "density"], "1")]),
     ("static not bool", CYL, [("set", [O, "cyl", "static"], 1)]),
     ("moving without motion dict", CYL, [("set", [O, "cyl", "static"], False)]),
+    *[(f"no ellipse {k}", ELL, [("del", [O, "wing", k])])
+      for k in ("semi_major_axis", "semi_minor_axis", "inclination_angle", "center",
+                "density", "static")],
+    ("semi_major_axis a string", ELL, [("set", [O, "wing", "semi_major_axis"], "3")]),
+    ("semi_minor_axis a list", ELL, [("set", [O, "wing", "semi_minor_axis"], [1.5])]),
+    ("inclination a string", ELL, [("set", [O, "wing", "inclination_angle"], "30")]),
+    ("ellipse center a string", ELL, [("set", [O, "wing", "center"], "7,6.5")]),
+    ("ellipse density a string", ELL, [("set", [O, "wing", "density"], "1")]),
+    ("ellipse static not bool", ELL, [("set", [O, "wing", "static"], 0)]),
+    ("ellipse moving without motion dict", ELL, [("set", [O, "wing", "static"], False)]),
+    ("ellipse bad motion type", ELL, [("set", [O, "rotor", "solid_motion_dict", "type"],
+                                       "oscillating")]),
+    ("ellipse no angular velocity", ELL, [("del", [O, "rotor", "solid_motion_dict",
+                                                   "angular_velocity"])]),
     ("no collision_dict", CYL, [("del", ["collision_dict"])]),
     ("no collision fluid", CYL, [("del", ["collision_dict", "fluid"])]),
     ("no collision model", CYL, [("del", ["collision_dict", "fluid", "model"])]),
@@ -188,7 +202,7 @@ def reference_message(case):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="path of the reference checkout")
     args = ap.parse_args()
     mg.install_numba_stub()
     mg.install_mpi4py_stub()

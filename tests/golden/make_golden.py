@@ -1,8 +1,8 @@
 """Generate the golden fixtures for the fluidLB step from the reference itself.
 
-Run in a container that has the reference checkout at /root/reference:
+Run where a checkout of the reference is available:
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <path of the reference checkout>
 
 The reference needs ``numba``, which is not installed here, so a stand-in
 ``numba`` module is placed in ``sys.modules`` first: ``njit`` returns the
@@ -36,6 +36,20 @@ Deviations, each forced by a defect of the reference snapshot:
 * ``fixed_pressure_density_based`` receives the surface normal as an int array
   (the reference passes the float normal of boundary.py:63-78, which fails to
   index).
+
+Zero-gradient cases.  The reference has no ``zero_gradient`` kernel, but its
+single-rank CPU halo exchange (``MPIOperator.halo_exchange_cpu``,
+pylabolt/parallel/MPI_operator.py:155-314, with a one-rank communicator)
+copies the first inner column / row of the post-collision populations into
+the ghost column / row of a "periodic" edge instead of wrapping.  The pull
+stream then gives an edge node b, for every population i entering from
+outside, ``pop[b + n - c_i, i]``: exactly this package's ``zero_gradient``
+definition.  The ``zero_gradient_*`` cases are therefore run by the
+reference with ``periodic`` edges and the CPU self-copy halo, and stored with
+the same dictionaries in which those edges are ``zero_gradient`` (listed
+before the walls, so that the walls win at the corners as the wall kernels do
+after streaming in the reference).  ``ref_case_json`` holds the dictionaries
+the reference ran.
 
 Each case is written to ``tests/golden/<name>.npz`` with the case
 dictionaries (JSON), the initial padded fields the reference built, the
@@ -231,7 +245,80 @@ def make_cases():
     c["initial_fields_dict"]["default"]["fluid"]["density"] = {"type": "array",
                                                                "value": dens}
     cases["yperiodic_partial_edges"] = (c, 40, None)
+
+    # zero-gradient x edges (reference: periodic x with the CPU self-copy
+    # halo), bottom bounce-back, moving lid, cylinder, Guo linear, random start
+    nx, ny = 18, 10
+    c = base_case(nx, ny, 0.06, forcing="guo_linear", gravity=[1e-5, 0.0])
+    c["boundary_dict"]["ends"] = {"wall": False, "segments": [
+        [[0, 0], [0, ny - 1]], [[nx - 1, 0], [nx - 1, ny - 1]]],
+        "fluid": {"type": "periodic"}}
+    c["boundary_dict"]["bottom"] = {"wall": True, "segments": [[[0, 0], [nx - 1, 0]]],
+                                    "fluid": {"type": "bounce_back"}}
+    c["boundary_dict"]["lid"] = {"wall": True, "segments": [[[0, ny - 1], [nx - 1, ny - 1]]],
+                                 "fluid": {"type": "fixed_velocity", "value": [0.02, 0.0]}}
+    c["obstacle_dict"]["cyl"] = {"type": "circle", "radius": 2.0, "center": [8, 5],
+                                 "density": 1.0, "static": True}
+    pert = rng.uniform(-1e-3, 1e-3, (nx, ny, 2))
+    c["initial_fields_dict"]["default"]["fluid"]["velocity"] = {"type": "array",
+                                                                "value": pert}
+    cases["zero_gradient_x"] = (c, 60, "selfcopy")
+
+    # zero-gradient y edges next to a bounce-back wall (left) and a moving wall
+    # (right), Guo second order along y, random density
+    nx, ny = 10, 16
+    c = base_case(nx, ny, 0.09, forcing="guo_second_order", gravity=[0.0, 1e-5])
+    c["boundary_dict"]["ends"] = {"wall": False, "segments": [
+        [[0, 0], [nx - 1, 0]], [[0, ny - 1], [nx - 1, ny - 1]]],
+        "fluid": {"type": "periodic"}}
+    c["boundary_dict"]["left"] = {"wall": True, "segments": [[[0, 0], [0, ny - 1]]],
+                                  "fluid": {"type": "bounce_back"}}
+    c["boundary_dict"]["right"] = {"wall": True, "segments": [[[nx - 1, 0], [nx - 1, ny - 1]]],
+                                   "fluid": {"type": "fixed_velocity", "value": [0.0, 0.03]}}
+    dens = 1.0 + rng.uniform(-1e-3, 1e-3, (nx, ny))
+    c["initial_fields_dict"]["default"]["fluid"]["density"] = {"type": "array",
+                                                               "value": dens}
+    cases["zero_gradient_y"] = (c, 60, "selfcopy")
+
+    # channel with two inclined ellipses (one static, one non-static held in
+    # place, i.e. a moving wall), pressure inlet / outlet, Guo second order
+    nx, ny = 26, 14
+    c = base_case(nx, ny, 0.07, forcing="guo_second_order", gravity=[5e-6, 1e-6])
+    c["boundary_dict"]["inlet"] = {"wall": False, "segments": [[[0, 0], [0, ny - 1]]],
+                                   "fluid": {"type": "fixed_pressure", "value": 1.0004}}
+    c["boundary_dict"]["outlet"] = {"wall": False,
+                                    "segments": [[[nx - 1, 0], [nx - 1, ny - 1]]],
+                                    "fluid": {"type": "fixed_pressure", "value": 1.0}}
+    c["boundary_dict"]["walls"] = {"wall": True, "segments": [
+        [[0, 0], [nx - 1, 0]], [[0, ny - 1], [nx - 1, ny - 1]]],
+        "fluid": {"type": "bounce_back"}}
+    c["obstacle_dict"]["options"] = {"compute_force_torque": True}
+    c["obstacle_dict"]["wing"] = {"type": "ellipse", "semi_major_axis": 3.5,
+                                  "semi_minor_axis": 1.5, "inclination_angle": 30.0,
+                                  "center": [7, 6.5], "density": 1.0, "static": True}
+    c["obstacle_dict"]["rotor"] = {
+        "type": "ellipse", "semi_major_axis": 2.6, "semi_minor_axis": 1.7,
+        "inclination_angle": -50, "center": [17.5, 7], "density": 1.5, "static": False,
+        "solid_motion_dict": {"type": "fixed_velocity", "degree_of_freedom": "rotation",
+                              "linear_velocity": [0.0, 0.0], "angular_velocity": 0.004}}
+    pert = rng.uniform(-1e-4, 1e-4, (nx, ny, 2))
+    c["initial_fields_dict"]["default"]["fluid"]["velocity"] = {"type": "array",
+                                                                "value": pert}
+    cases["channel_ellipses"] = (c, 60, None)
     return cases
+
+
+def zero_gradient_twin(case):
+    """The same dictionaries with every ``periodic`` edge ``zero_gradient``."""
+    out = json.loads(jsonable(case))
+    for region, rd in case["initial_fields_dict"].items():
+        for fname, spec in rd["fluid"].items():
+            if spec["type"] == "array":
+                out["initial_fields_dict"][region]["fluid"][fname]["value"] = spec["value"]
+    for name, ud in out["boundary_dict"].items():
+        if name != "options" and ud["fluid"]["type"] == "periodic":
+            ud["fluid"] = {"type": "zero_gradient"}
+    return out
 
 
 # --------------------------------------------------------------------------
@@ -272,8 +359,12 @@ def jsonable(case):
     return json.dumps(conv(case))
 
 
-def run_case(name, case, nsteps, ref):
+def run_case(name, case, nsteps, ref, halo=None):
+    """Steps `case` with the reference's kernels.  halo None: the GPU periodic
+    wrap kernels; "selfcopy": the single-rank CPU halo exchange (the stored
+    case is then the zero_gradient twin)."""
     from pylabolt.base.state import State
+    from pylabolt.parallel.MPI_operator import MPIOperator
     import pylabolt.parallel.cpu.compute_fields_kernels as cfk
     import pylabolt.parallel.cpu.force_field_kernels as ffk
     import pylabolt.parallel.cpu.collision_kernels as colk
@@ -287,6 +378,7 @@ def run_case(name, case, nsteps, ref):
     with contextlib.redirect_stdout(io.StringIO()):
         state = State(sim, DummyComm(), 0, fluid=True)
     lat, fld, dom, ctl = state.lattice, state.fields, state.domain, state.control
+    mpi_op = MPIOperator(DummyComm(), state) if halo == "selfcopy" else None
     tau = state.transport.kin_visc * lat.inv_cs_2 + 0.5   # collision_operator.py:89
     omega = 1 / tau
     forcing = case["collision_dict"]["fluid"]["forcing_model"]
@@ -324,11 +416,14 @@ def run_case(name, case, nsteps, ref):
         collide(size, lat.cx, lat.cy, lat.weights, lat.no_of_directions, lat.inv_cs_2,
                 lat.inv_cs_4, fld.solid, fld.ghost_node, fld.density, fld.velocity,
                 fld.force_field, fld.pop_fluid, fld.pop_fluid_new, omega)
-        if state.boundary.x_periodic:
+        if mpi_op is not None:
+            # fluidLB.py:227-231 on the CPU backend: MPI_operator.py:155-259
+            mpi_op.halo_exchange_cpu(state, None, float_buffers=["pop_fluid"])
+        elif state.boundary.x_periodic:
             for tid in range(shape[1]):
                 _THREAD[0] = tid
                 gmk.exchange_y_vector(fld.pop_fluid, shape)
-        if state.boundary.y_periodic:
+        if mpi_op is None and state.boundary.y_periodic:
             for tid in range(shape[0]):
                 _THREAD[0] = tid
                 gmk.exchange_x_vector(fld.pop_fluid, shape)
@@ -369,6 +464,9 @@ def run_case(name, case, nsteps, ref):
             out[f"pop_t{t}"] = fld.pop_fluid.copy()
             out[f"pop_new_t{t}"] = fld.pop_fluid_new.copy()
 
+    stored = case if halo is None else zero_gradient_twin(case)
+    extra = {} if halo is None else {"ref_case_json": np.array(jsonable(case)),
+                                     "halo": np.array(halo)}
     geo = geometry_and_forces(case, {0: (pop_init, pop_new_init),
                                      **{t: (out[f"pop_t{t}"], out[f"pop_new_t{t}"])
                                         for t in checkpoints}})
@@ -379,7 +477,7 @@ def run_case(name, case, nsteps, ref):
                 arrays[f"init_{region}_{fname}"] = np.asarray(spec["value"])
     np.savez_compressed(
         os.path.join(HERE, name + ".npz"),
-        case_json=np.array(jsonable(case)), nsteps=np.array(nsteps),
+        case_json=np.array(jsonable(stored)), nsteps=np.array(nsteps), **extra,
         checkpoints=np.array(checkpoints), rho0=rho0, u0=u0, solid=solid0,
         residuals=np.array(resid), inv_cs_2=np.array(lat.inv_cs_2),
         inv_cs_4=np.array(lat.inv_cs_4), omega=np.array(omega), **arrays, **out, **geo)
@@ -421,16 +519,16 @@ def geometry_and_forces(case, states):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="path of the reference checkout")
     ap.add_argument("--only", default=None)
     args = ap.parse_args()
     install_numba_stub()
     install_mpi4py_stub()
     sys.path.insert(0, args.ref)
-    for name, (case, nsteps, _) in make_cases().items():
+    for name, (case, nsteps, halo) in make_cases().items():
         if args.only and name != args.only:
             continue
-        n = run_case(name, case, nsteps, args.ref)
+        n = run_case(name, case, nsteps, args.ref, halo)
         print(f"{name}: {n} steps written")
 
 

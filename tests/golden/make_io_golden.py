@@ -1,8 +1,8 @@
 """Generate the output-format fixture from the reference's own I/O code.
 
-Run in a container that has the reference checkout at /root/reference:
+Run where a checkout of the reference is available:
 
-    python tests/golden/make_io_golden.py [--ref /root/reference]
+    python tests/golden/make_io_golden.py --ref <path of the reference checkout>
 
 It builds the reference State of the ``channel_cylinder_abb`` golden case with
 output options switched on (std_out / save / history intervals of 30 steps,
@@ -57,7 +57,7 @@ def io_case():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="path of the reference checkout")
     args = ap.parse_args()
     mg.install_numba_stub()
     mg.install_mpi4py_stub()

@@ -27,7 +27,7 @@ def _inner_mask(nx, ny, solid_padded):
     return m.ravel() & ~solid_padded
 
 
-@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("name", golden_names(zero_gradient=False))
 def test_aa_fp64_bit_exact_vs_reference_fixtures(name):
     case_d, d = load_golden(name)
     case = Case(case_d)
@@ -48,7 +48,7 @@ def test_aa_fp64_bit_exact_vs_reference_fixtures(name):
         np.testing.assert_allclose(np.array(res), d["residuals"][:, 1:], rtol=RES_RTOL, atol=0)
 
 
-@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("name", golden_names(zero_gradient=False))
 def test_aa_forces_and_conservation_match_two_buffers(name):
     case = Case(load_golden(name)[0])
     with FluidLBM(case, storage="fp64") as ab, FluidLBM(case, storage="fp64", layout="aa") as aa:

@@ -75,6 +75,56 @@ def test_fp64_adjoint_cavity_wall_velocity():
     assert abs(gtau - gtau_ref) <= FP64_RTOL * abs(gtau_ref)
 
 
+def _torch_grads_cuda(case, T, gu, u_wall=None):
+    """_torch_grads with the plain-torch FP64 reference on the GPU (the full
+    512^2 grid keeps about 0.3 GB of autograd state per step)."""
+    dev = torch.device("cuda:0")
+    tl = TorchLBM(case, device=dev)
+    F = torch.tensor(case.body_force_field.reshape(-1, 2), device=dev, requires_grad=True) \
+        if case.body_force_field is not None else None
+    tau = torch.tensor(case.tau, dtype=torch.float64, device=dev, requires_grad=True)
+    uw = torch.tensor(u_wall, dtype=torch.float64, device=dev, requires_grad=True) \
+        if u_wall is not None else None
+    u = tl.run(T, 1.0 / tau, force=F, u_wall=uw)
+    (u * torch.tensor(gu.reshape(-1, 2), device=dev)).sum().backward()
+    out = (F.grad.cpu().numpy().reshape(case.nx, case.ny, 2) if F is not None else None,
+           float(tau.grad), uw.grad.cpu().numpy() if uw is not None else None)
+    del tl, F, tau, uw, u
+    torch.cuda.empty_cache()
+    return out
+
+
+def test_adjoint_channel_512_full_grid_against_torch_autograd():
+    """The 512x512 adjoint channel (tau 0.8, Gaussian-smoothed body force) on
+    its full grid, T = 100, checkpoints every 45 steps: the CUDA adjoint's
+    whole dL/dF field and dL/dtau against the plain-torch FP64 autograd of the
+    same forward -- FP64 to 1e-10, FP32-shifted to 1e-3."""
+    case = Case(workloads.adjoint_channel(seed=1))
+    T = 100
+    gu = np.random.default_rng(3).standard_normal((case.nx, case.ny, 2)) * 1e-3
+    gF_ref, gtau_ref, _ = _torch_grads_cuda(case, T, gu)
+    gF, gtau, _ = _cuda_grads(case, T, gu, "fp64", 45)
+    assert _close(gF, gF_ref, FP64_RTOL)
+    assert abs(gtau - gtau_ref) <= FP64_RTOL * abs(gtau_ref)
+    gF32, gtau32, _ = _cuda_grads(case, T, gu, "fp32_shifted", 45)
+    assert _close(gF32, gF_ref, FP32_RTOL)
+    assert abs(gtau32 - gtau_ref) <= FP32_TAU_RTOL * abs(gtau_ref)
+
+
+def test_adjoint_cavity_256_lid_velocity_against_torch_autograd():
+    """The 256x256 cavity variant (Re 400), T = 100: dL/du_wall and dL/dtau
+    against the plain-torch FP64 autograd, FP64 to 1e-10."""
+    case = Case(workloads.cavity(256, re=400.0))
+    T = 100
+    gu = np.random.default_rng(4).standard_normal((case.nx, case.ny, 2)) * 1e-3
+    gu[case.solid] = 0.0
+    U = case.elements[-1].value[0]
+    _, gtau_ref, guw_ref = _torch_grads_cuda(case, T, gu, u_wall=[U, 0.0])
+    _, gtau, guw = _cuda_grads(case, T, gu, "fp64", 45)
+    assert _close(guw, guw_ref, FP64_RTOL)
+    assert abs(gtau - gtau_ref) <= FP64_RTOL * abs(gtau_ref)
+
+
 def test_fp32_adjoint_close_to_fp64_reference():
     case = _channel()
     T = 60
@@ -169,3 +219,23 @@ def test_adjoint_cavity_256_lid_velocity_against_finite_differences():
     U, h = case.elements[-1].value[0], 1e-6
     fd = (loss(U + h) - loss(U - h)) / (2 * h)
     assert abs(guw[0] - fd) <= FD_RTOL * abs(fd), (guw[0], fd)
+
+
+def test_autograd_function_keeps_cuda_tensors_on_the_device():
+    """With a CUDA body-force tensor the velocity and dL/dF are CUDA tensors
+    (device pointers through the C-ABI, no host round trip), with the same
+    values as the host-tensor path."""
+    case = _channel()
+    dev = torch.device("cuda:0")
+    outs = []
+    for device in ("cpu", dev):
+        F = torch.tensor(case.body_force_field, device=device, requires_grad=True)
+        tau = torch.tensor(case.tau, dtype=torch.float64, device=device, requires_grad=True)
+        u = lbm_velocity(case, force=F, tau=tau, nsteps=40, interval=8, storage="fp64")
+        assert u.device.type == torch.device(device).type
+        loss = (u ** 2).mean()
+        loss.backward()
+        assert F.grad.device.type == torch.device(device).type
+        outs.append((u.detach().cpu().numpy(), F.grad.cpu().numpy(), float(tau.grad)))
+    (u0, g0, t0), (u1, g1, t1) = outs
+    assert np.array_equal(u0, u1) and np.array_equal(g0, g1) and t0 == t1

@@ -34,6 +34,39 @@ def test_batch_equals_single_cavities():
         assert np.abs(ub[i] - u64).max() <= 3e-5 * np.abs(u64).max()
 
 
+def _fp64_velocities(sides, res, lids, steps):
+    """Each cavity on its own FP64 handle; the handles' steps are queued on
+    their own streams before any result is read, so they run side by side."""
+    sims = []
+    try:
+        for i in range(len(sides)):
+            case = Case(workloads.cavity(int(sides[i]), re=float(res[i]), lid=float(lids[i])))
+            s = FluidLBM(case, storage="fp64")
+            sims.append(s)
+            s.initialize()
+            s.step(steps, moments=True)
+        return [s.moments()[1] for s in sims]
+    finally:
+        for s in sims:
+            s.close()
+
+
+def test_c4_distribution_32_cavities_vs_fp64():
+    """The first 32 cavities of the benchmark's draw (sides U{64..512}, Re
+    U[50, 1000], lid U[0.05, 0.1], seed 0) batched in FP32 shifted storage
+    against each cavity run alone in FP64."""
+    sides, res, lids = draw_cavities()
+    sides, res, lids = sides[:32], res[:32], lids[:32]
+    steps = 1000
+    with CavityBatch(sides, res, lids) as b:
+        b.initialize()
+        b.step(steps, moments=True)
+        ub = b.velocities()
+    u64 = _fp64_velocities(sides, res, lids, steps)
+    errs = [np.abs(ub[i] - u64[i]).max() / np.abs(u64[i]).max() for i in range(len(sides))]
+    assert max(errs) <= 1e-5, max(errs)
+
+
 def test_omega_map_rejects_mixed_segment():
     case = Case(workloads.cavity(64))
     with FluidLBM(case, storage="fp32_shifted") as s:

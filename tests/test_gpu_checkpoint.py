@@ -52,6 +52,51 @@ def test_restart_is_bit_exact(name, storage, layout, monkeypatch):
     assert np.array_equal(np.array(ra[2:]), np.array(rb))
 
 
+@pytest.mark.parametrize("storage", ["fp32_shifted", "fp16_shifted"])
+def test_restart_keeps_the_tuned_launch_shape(storage, monkeypatch):
+    """Without a pinned launch shape each handle runs the autotuner, and
+    shapes round FP32 / FP16 differently.  The saved state carries the
+    shapes of the saving handle, so a fresh handle continues bit for bit."""
+    monkeypatch.delenv("LBM_VARIANT", raising=False)
+    monkeypatch.delenv("LBM_TUNE", raising=False)
+    case = Case(workloads.cylinder(nx=512, ny=128, radius=16.0, center=(128, 67)))
+    ra, rb = [], []
+    with FluidLBM(case, storage=storage) as a:
+        a.initialize()
+        _steps(a, ra)
+        state = a.save_state()
+        shape = a.kernel_variant
+        _steps(a, ra)
+        pa = a.populations()
+    with FluidLBM(case, storage=storage) as b:
+        b.initialize()
+        b.load_state(state)
+        assert b.kernel_variant == shape
+        _steps(b, rb)
+        assert np.array_equal(b.populations(), pa)
+    assert np.array_equal(np.array(ra[2:]), np.array(rb))
+
+
+def test_state_of_another_obstacle_layout_or_viscosity_is_refused():
+    """Same grid, storage and number of link records, but the cylinder one
+    node higher, or another viscosity: the case hash in the state refuses
+    both."""
+    base = workloads.cylinder(nx=256, ny=64, radius=8.0, center=(64, 35))
+    moved = workloads.cylinder(nx=256, ny=64, radius=8.0, center=(64, 36))
+    visc = workloads.cylinder(nx=256, ny=64, radius=8.0, center=(64, 35), kin_visc=0.05)
+    with FluidLBM(Case(base), storage="fp64") as a:
+        a.initialize()
+        a.step(5)
+        state = a.save_state()
+        for other in (moved, visc):
+            with FluidLBM(Case(other), storage="fp64") as b:
+                b.initialize()
+                with pytest.raises(capi.LbmError, match="another"):
+                    b.load_state(state)
+                b.step(2)
+        a.load_state(state)                  # its own state still loads
+
+
 def test_mismatched_state_is_refused():
     a_case = Case(load_golden("channel_cylinder_abb")[0])
     b_case = Case(load_golden("cavity_lid_first")[0])

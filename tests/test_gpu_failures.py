@@ -34,3 +34,28 @@ def test_nonfinite_density_is_reported(storage, bad, layout):
         sim.step(3, residual=True)
         r = sim.residual()
         assert np.all(np.isfinite(r))
+
+
+def test_bounded_host_wait_gives_up_and_the_run_continues():
+    """The host's wait on the handle's stream is bounded.  With about 0.1 s of
+    queued FP64 steps, a 0.1 ms limit expires and lbm_synchronize returns
+    LBM_ERR_TIMEOUT; the queued work is not disturbed: a second wait with a
+    long limit succeeds and the fields equal those of a run that was never
+    interrupted.  (The work is finite, so nothing can hang.)"""
+    case = Case(workloads.cylinder(nx=2048, ny=1024, radius=32.0, center=(512, 515)))
+    with FluidLBM(case, storage="fp64") as a, FluidLBM(case, storage="fp64") as b:
+        for s in (a, b):
+            s.initialize()
+            s.step(2)
+            s.synchronize()
+        a.step(200)
+        with pytest.raises(capi.LbmError, match="did not finish") as e:
+            a.synchronize(timeout_s=1e-4)
+        assert e.value.status == capi.LBM_ERR_TIMEOUT
+        a.synchronize(600.0)
+        a.step(1, moments=True)
+        b.step(201, moments=True)
+        ra, ua = a.moments()
+        rb, ub = b.moments()
+        assert np.array_equal(ra, rb) and np.array_equal(ua, ub)
+        assert np.array_equal(a.populations(), b.populations())

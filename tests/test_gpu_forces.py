@@ -87,3 +87,46 @@ def test_cylinder_channel_forces_against_oracle():
         got = sim.forces()
     np.testing.assert_allclose(got["obstacles"][0], ref_cyl, rtol=FORCE_RTOL, atol=1e-14)
     np.testing.assert_allclose(got["walls"], np.array(ref_w), rtol=FORCE_RTOL, atol=1e-14)
+
+
+def test_ellipse_channel_against_c_oracle():
+    """512x128 channel with an ellipse (semi-axes 24 and 8, inclined 20
+    degrees) and anti-bounce-back inlet / outlet, 300 steps: FP64 fields bit
+    for bit against the C oracle, the ellipse's force and torque against the
+    oracle's restatement of the reference force kernel, FP32 shifted within
+    1e-5 of FP64."""
+    from oracle.clib import COracle
+    from oracle.setup import build_state
+    from oracle import lbm_np
+    from pylabolt_gb300 import workloads
+    from pylabolt_gb300.obstacles import Geometry
+    case_d = workloads.ellipse_channel(512, 128)
+    nsteps = 300
+    st = build_state(case_d)
+    co = COracle(st)
+    co.initialize()
+    co.run(nsteps)
+    case = Case(case_d)
+    assert case.solid.sum() > 0 and np.array_equal(case.solid, st.inner(st.solid))
+    geo = Geometry(case)
+    npad = (case.nx + 2) * (case.ny + 2)
+    o = case.obstacles[0]
+    ref = lbm_np.obstacle_force_torque(st.pop, st.pop_new, geo.solid.reshape(npad),
+                                       geo.solid_id.reshape(npad), geo.fluid_boundary.reshape(npad),
+                                       case.nx, case.ny, o.center, o.id, case.x_periodic,
+                                       case.y_periodic)
+    us = {}
+    for storage in ("fp64", "fp32_shifted"):
+        with FluidLBM(case, storage=storage) as sim:
+            sim.initialize()
+            sim.step(nsteps, moments=True)
+            rho, us[storage] = sim.moments()
+            if storage == "fp64":
+                m = ~case.solid
+                assert np.array_equal(rho[m], st.inner(st.density)[m])
+                assert np.array_equal(us[storage][m], st.inner(st.velocity)[m])
+                np.testing.assert_allclose(sim.forces()["obstacles"][0], ref, rtol=FORCE_RTOL,
+                                           atol=1e-14)
+    m = ~case.solid
+    err = np.abs(us["fp32_shifted"][m] - us["fp64"][m]).max() / np.abs(us["fp64"][m]).max()
+    assert err <= 1e-5, err

@@ -1,12 +1,13 @@
 """lbm_conservation_noalloc: the entry point for callers that cannot allocate
-device memory (for example code embedded in an application that owns the
-device memory pool, or code running during stream capture).
+device memory (for example code embedded in an application that hands out
+all device memory from its own pool).
 
 The test is the caller: it owns the input and output device buffers (through
 torch) and calls the entry point through the C-ABI.  The result must match
 lbm_conservation, the allocating entry point, on the same populations, within
 the FP64 round-off of a differently ordered sum -- on two calls in a row, and
-for FP64 and FP32-shifted views of the populations.
+for FP64, FP32-shifted and FP16-shifted views of the populations (the
+reduced storages within the rounding of their stored values).
 
 The file name makes pytest collect it last."""
 import ctypes
@@ -23,6 +24,7 @@ pytestmark = pytest.mark.gpu
 
 RTOL_FP64 = 1e-12      # same populations, different summation order
 RTOL_FP32 = 1e-6       # populations rounded to FP32 shifted storage
+FP16_SCALE = 4096.0    # FP16 view stores g * scale
 
 
 def _soa_view(pop_padded, nx, ny):
@@ -31,7 +33,7 @@ def _soa_view(pop_padded, nx, ny):
     return np.ascontiguousarray(p.transpose(2, 1, 0))
 
 
-def _noalloc(lib, soa, exclude, precision, torch):
+def _noalloc(lib, soa, exclude, precision, torch, fp16_scale=0.0):
     dev = torch.device("cuda:0")
     pop_d = torch.from_numpy(soa).to(dev)
     excl_d = torch.from_numpy(exclude).to(dev)
@@ -39,7 +41,7 @@ def _noalloc(lib, soa, exclude, precision, torch):
     nq, ny, nx = soa.shape
     view = capi.LbmPopView(precision=precision, nx=nx, ny=ny, reserved=0, pitch=nx,
                            plane=ny * nx, pop=pop_d.data_ptr(), exclude=excl_d.data_ptr(),
-                           fp16_scale=0.0)
+                           fp16_scale=fp16_scale)
     stream = torch.cuda.current_stream(dev).cuda_stream
     rc = lib.lbm_conservation_noalloc(ctypes.byref(view), ctypes.c_void_p(out_d.data_ptr()),
                                       ctypes.c_void_p(stream))
@@ -62,9 +64,19 @@ def test_noalloc_conservation_matches_allocating_entry_point():
             soa = _soa_view(sim.populations(), nx, ny)
             got = _noalloc(lib, soa, exclude, capi.LBM_FP64, torch)
             np.testing.assert_allclose(got, ref, rtol=RTOL_FP64, atol=1e-13 * abs(ref[0]))
-            g32 = (soa - np.array(capi_weights())[:, None, None]).astype(np.float32)
+            g = soa - np.array(capi_weights())[:, None, None]
+            g32 = g.astype(np.float32)
             got32 = _noalloc(lib, g32, exclude, capi.LBM_FP32_SHIFTED, torch)
             np.testing.assert_allclose(got32, ref, rtol=RTOL_FP32, atol=1e-6 * abs(ref[0]))
+            # FP16: each stored g * scale is rounded to half (relative 2^-11 at
+            # most, absolute 2^-25 for subnormals), so every sum is within
+            # 2^-11 sum |g| + count 2^-25 / scale of the FP64 one
+            g16 = (g * FP16_SCALE).astype(np.float16)
+            got16 = _noalloc(lib, g16, exclude, capi.LBM_FP16_SHIFTED, torch, FP16_SCALE)
+            gk = g[:, exclude == 0]
+            bound = (2.0 ** -11 * np.abs(gk).sum() + gk.size * 2.0 ** -25 / FP16_SCALE
+                     + 1e-12 * abs(ref[0]))
+            np.testing.assert_allclose(got16, ref, rtol=0, atol=bound)
 
 
 def test_noalloc_rejects_too_many_rows():

@@ -162,6 +162,28 @@ def cpu_measure(case_dict, steps_budget_s=20.0, max_steps=None, warmup=1):
     return nodes * n / dt / 1e6, n, dt
 
 
+def host_link_peak(nbytes, device):
+    """Pinned host <-> device copy bandwidth (GB/s, best of 5) of one
+    cudaMemcpyAsync of `nbytes` each way: the floor of the end-to-end leg's
+    transfers."""
+    import torch
+    n = nbytes // 8
+    h = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    d = torch.empty(n, dtype=torch.float64, device=f"cuda:{device}")
+    out = {}
+    for name, dst, src in (("h2d", d, h), ("d2h", h, d)):
+        best = float("inf")
+        for _ in range(5):
+            torch.cuda.synchronize(device)
+            t0 = time.perf_counter()
+            dst.copy_(src, non_blocking=True)
+            torch.cuda.synchronize(device)
+            best = min(best, time.perf_counter() - t0)
+        out[name] = nbytes / best / 1e9
+    del h, d
+    return out
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -266,20 +288,30 @@ def run_gb300(args, world, rank, local):
     u_h[...] = case.velocity
     rho_out = torch.empty(case.density.shape, dtype=torch.float64, pin_memory=True).numpy()
     u_out = torch.empty(case.velocity.shape, dtype=torch.float64, pin_memory=True).numpy()
-    barrier()
-    t0 = time.perf_counter()
-    sim.initialize(rho_h, u_h)                      # H2D of the initial fields
-    for _ in range(e2e_steps):
-        sim.step(1, residual=True)
-        sim.residual()                              # D2H of the step's residual
-    rho_o, u_o = sim.moments(out=(rho_out, u_out))  # D2H of the final fields
-    t_e2e = max_over_ranks(time.perf_counter() - t0, dist, f"cuda:{device}")
+    def end_to_end(nsteps):
+        barrier()
+        t0 = time.perf_counter()
+        sim.initialize(rho_h, u_h)                      # H2D of the initial fields
+        for _ in range(nsteps):
+            sim.step(1, residual=True)
+            sim.residual()                              # D2H of the step's residual
+        sim.moments(out=(rho_out, u_out))               # D2H of the final fields
+        return max_over_ranks(time.perf_counter() - t0, dist, f"cuda:{device}")
+
+    t_e2e = end_to_end(e2e_steps)
+    io_bytes = rho_h.nbytes + u_h.nbytes
+    link = host_link_peak(io_bytes, device)
     e2e = {"value": whole_job_mlups(world, nodes, e2e_steps, t_e2e), "unit": "MLUPS",
-           "h2d_bytes_per_step": int((rho_h.nbytes + u_h.nbytes) / e2e_steps),
-           "d2h_bytes_per_step": int(8 * 8 + (rho_o.nbytes + u_o.nbytes) / e2e_steps),
-           "steps": e2e_steps,
+           "h2d_bytes_per_step": int(io_bytes / e2e_steps),
+           "d2h_bytes_per_step": int(8 * 8 + (rho_out.nbytes + u_out.nbytes) / e2e_steps),
+           "steps": e2e_steps, "ms": t_e2e * 1e3,
+           "host_link_gbs": link,
+           "transfer_floor_ms": io_bytes / link["h2d"] / 1e6 + io_bytes / link["d2h"] / 1e6,
            "what": "FluidLBM.initialize(host rho,u) + per step lbm_step_ex(RESIDUAL) + "
                    "lbm_residual readback + final lbm_get_moments readback"}
+    if e2e_steps != 200:
+        t200 = end_to_end(200)
+        e2e["at_200_steps"] = {"value": whole_job_mlups(world, nodes, 200, t200), "ms": t200 * 1e3}
 
     extra = {}
     if not args.no_extra and rank == 0:

@@ -323,6 +323,15 @@ int lbm_time_steps(LbmHandle* h, int64_t nsteps, double* ms);
 /* Waits (bounded by timeout_s seconds) for all work of the handle. */
 int lbm_synchronize(LbmHandle* h, double timeout_s);
 
+/* Self-test of the device-side bounded waits (no counterpart in the
+ * reference, which only aborts: pylabolt/base/state.py:121-125).  Runs a
+ * kernel that waits on an mbarrier nobody arrives at, with the same bounded
+ * wait the pipelined step kernel uses, limited to limit_s (0 < limit_s <= 1).
+ * The wait gives up, the kernel sets the handle's error word and returns;
+ * the call then reports LBM_ERR_TIMEOUT like a step whose wait expired, with
+ * *waited_s the time the kernel waited.  The handle stays usable. */
+int lbm_selftest_bounded_wait(LbmHandle* h, double limit_s, double* waited_s);
+
 /* A population array owned by the caller, in device memory: value of node
  * (x, y), direction k at pop[k*plane + y*pitch + x], stored as f (LBM_FP64),
  * g = f - w_k (LBM_FP32_SHIFTED) or g * fp16_scale in IEEE half

@@ -88,7 +88,7 @@ EXPORTS = ["lbm_create", "lbm_init_fields", "lbm_set_body_force", "lbm_step",
            "lbm_adjoint_forward", "lbm_adjoint_backward", "lbm_set_omega_map",
            "lbm_set_force_links", "lbm_forces", "lbm_set_moving_obstacles",
            "lbm_get_moving_obstacles", "lbm_get_node_flags", "lbm_state_size",
-           "lbm_save_state", "lbm_load_state"]
+           "lbm_save_state", "lbm_load_state", "lbm_selftest_bounded_wait"]
 
 
 def lib_path():
@@ -125,6 +125,7 @@ def load(build=True):
         "lbm_tuning": [P, dbl, ctypes.POINTER(ctypes.c_int)],
         "lbm_time_steps": [P, i64, dbl],
         "lbm_synchronize": [P, ctypes.c_double],
+        "lbm_selftest_bounded_wait": [P, ctypes.c_double, dbl],
         "lbm_destroy": [P],
         "lbm_conservation_noalloc": [ctypes.POINTER(LbmPopView), P, P],
         "lbm_adjoint_forward": [P, i64, ctypes.c_int],

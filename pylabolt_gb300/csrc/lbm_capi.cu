@@ -510,6 +510,12 @@ struct LbmHandle {
     return LBM_OK;
   }
 
+  // Register cap of the scalar AA kernel (0 none for FP64; shifted storage:
+  // 1 (32 registers) for BGK, 2 (40) for MRT).
+  int aa_scalar_cap() const {
+    return cfg.precision == LBM_FP64 ? 0 : (cfg.collision == LBM_BGK ? 1 : 2);
+  }
+
   long long nparts_of(lbm::Variant v) const {
     const dim3 gr = lbm::step_grid(g, v, sms, ks->elem_bytes);
     return (long long)gr.x * gr.y;
@@ -522,10 +528,16 @@ struct LbmHandle {
     if (const char* f = std::getenv("LBM_VARIANT")) {
       int kind = -1, vec = 0, blk = 0, st = 0;
       if (aa && std::sscanf(f, "%d,%d,%d,%d", &kind, &vec, &blk, &st) == 4) {
-        if (kind != 0 || vec != 1 || blk < 32 || blk > 256 || blk % 32)
+        const bool scalar = kind == 0 && vec == 1;
+        const bool pairs = kind == 3 && vec == 2 && cfg.precision != LBM_FP64 && st >= 0 && st <= 2;
+        if (!(scalar || pairs) || blk < 32 || blk > 256 || blk % 32)
           return fail(LBM_ERR_ARG, std::string("LBM_VARIANT: the AA layout runs the scalar kernel "
-                                               "(0,1,block,stages) with 32 <= block <= 256: ") + f);
-        variant.block = blk;
+                                               "(0,1,block,cap) or, for shifted storage, the node-pair "
+                                               "kernel (3,2,block,cap), 32 <= block <= 256: ") + f);
+        if (scalar)
+          variant = lbm::Variant{0, 1, blk, aa_scalar_cap()};   // the storage's register cap
+        else
+          variant = lbm::Variant{3, 2, blk, st};
         return LBM_OK;
       }
       if (std::sscanf(f, "%d,%d,%d,%d", &kind, &vec, &blk, &st) == 4) {
@@ -896,8 +908,12 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&h->err_dev), h->err_host, 0);
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaHostGetDevicePointer: ") + cudaGetErrorString(e)));
   h->variant = ks->variants[0];
-  if (aa) {   // the scalar kernel, 128 threads (its register cap is chosen per storage)
-    h->variant = lbm::Variant{0, 1, 128, c.precision == LBM_FP64 ? 0 : (c.collision == LBM_BGK ? 1 : 2)};
+  if (aa) {
+    // no autotuner (a trial launch would advance the state in place): FP64
+    // runs the scalar kernel, shifted storage the node-pair kernel, 128
+    // threads under a 40-register cap, the fastest in a sweep at 8192x2048
+    // (FP32 86.2 GLUPS against 82.8 scalar, FP16 123.5 against 109.7)
+    h->variant = c.precision == LBM_FP64 ? lbm::Variant{0, 1, 128, 0} : lbm::Variant{3, 2, 128, 1};
   }
   long long maxparts = ny;
   for (int i = 0; i < ks->nvariants; ++i) maxparts = std::max(maxparts, h->nparts_of(ks->variants[i]));
@@ -1870,7 +1886,10 @@ StateHeader state_header(const LbmHandle* h) {
 bool valid_variant(const LbmHandle* h, const int32_t v[4], lbm::Variant* out) {
   const lbm::Variant w{v[0], v[1], v[2], v[3]};
   if (h->aa) {
-    if (w.kind != 0 || w.vec != 1 || w.block < 32 || w.block > 256 || w.block % 32) return false;
+    const bool scalar = w.kind == 0 && w.vec == 1;
+    const bool pairs = w.kind == 3 && w.vec == 2 && h->cfg.precision != LBM_FP64 && w.stages >= 0 &&
+                       w.stages <= 2;
+    if (!(scalar || pairs) || w.block < 32 || w.block > 256 || w.block % 32) return false;
     *out = w;
     return true;
   }
@@ -1984,6 +2003,23 @@ int lbm_load_state(LbmHandle* h, const void* in) {
   h->has_residual = false;
   h->initialized = true;
   return LBM_OK;
+}
+
+int lbm_selftest_bounded_wait(LbmHandle* h, double limit_s, double* waited_s) {
+  if (!h || !waited_s) return fail(LBM_ERR_ARG, "lbm_selftest_bounded_wait: null argument");
+  if (!(limit_s > 0.0 && limit_s <= 1.0))
+    return fail(LBM_ERR_ARG, "lbm_selftest_bounded_wait: limit_s must lie in (0, 1]");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  int rc = h->wait();   // earlier work first: its errors are not the test's
+  if (rc) return rc;
+  auto* waited = reinterpret_cast<unsigned long long*>(h->red + 15);
+  LBM_CUDA(lbm::bounded_wait_selftest(h->err_dev, limit_s, waited, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(h->host_red + 15, waited, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  rc = h->wait();
+  unsigned long long ns = 0;
+  std::memcpy(&ns, h->host_red + 15, sizeof ns);
+  *waited_s = ns * 1e-9;
+  return rc;
 }
 
 int lbm_synchronize(LbmHandle* h, double timeout_s) {

@@ -170,8 +170,8 @@ struct MovArgs {
 //   kind 1: vector kernel, `vec` consecutive nodes per thread
 //   kind 2: persistent TMA-pipelined kernel: tiles of one row segment of
 //           kTmaRowBytes, `stages` shared-memory stages, `block` threads
-//   kind 3: node-pair kernel, two nodes per thread (vec = 2), `stages` its
-//           register cap
+//   kind 3: node-pair kernel, two nodes per thread along x for each of
+//           vec / 2 rows, `stages` its register cap
 struct Variant {
   int kind;
   int vec;
@@ -254,6 +254,11 @@ inline dim3 step_grid(const Geom& g, Variant v, int sms, int elem_bytes) {
     if (blocks > tiles) blocks = tiles;
     return dim3((unsigned)blocks, 1);
   }
+  if (v.kind == 3) {   // node pairs: two nodes per thread along x, vec / 2 rows
+    const int rows = v.vec / 2;
+    return dim3((unsigned)((g.pitch + 2LL * v.block - 1) / (2LL * v.block)),
+                (unsigned)((g.ny + rows - 1) / rows));
+  }
   const long long per_block = (long long)v.block * v.vec;
   return dim3((unsigned)((g.pitch + per_block - 1) / per_block), (unsigned)g.ny);
 }
@@ -265,6 +270,12 @@ cudaError_t reorder(const Geom& g, const double* in, double* out, int ncomp,
 // The same for the columns x_lo <= x < x_hi only.
 cudaError_t reorder_cols(const Geom& g, const double* in, double* out, int ncomp,
                          int layout, int to_device, int x_lo, int x_hi, cudaStream_t s);
+
+// Launches the bounded-wait self-test kernel (one mbarrier nobody arrives
+// at): *err (device-visible) gets kErrWaitTimeout after limit_s, *waited_ns
+// (device-visible) the time waited.
+cudaError_t bounded_wait_selftest(int* err, double limit_s, unsigned long long* waited_ns,
+                                  cudaStream_t s);
 
 // Sets the message lbm_last_error() returns on this thread.
 void record_error(const std::string& msg);

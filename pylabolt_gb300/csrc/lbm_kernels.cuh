@@ -840,49 +840,54 @@ __device__ __forceinline__ void special_links_aa(typename Store<S>::T f[9], cons
   }
 }
 
+// One node of the AA kernel (either phase).
+template <class S, int COLL, int FORC, bool ODD>
+__device__ __forceinline__ void aa_node(const StepArgs& a, int x, int y,
+                                        typename Store<S>::T red[7]) {
+  using T = typename Store<S>::T;
+  const Geom& g = a.g;
+  const int ni = (y + 1) * g.pitch + x;
+  const long long n = ni;
+  S* A = static_cast<S*>(a.fout);   // == a.fin
+  S* An = A + ni;                   // this node's element of plane 0 (uniform offsets below)
+  int cls = 0;
+  if (g.segflag[y * g.nseg + (x >> 5)]) cls = g.cls[ni];
+  if (cls == 2) return;
+  T f[9];
+  int r = -1;
+  if (cls == 1) r = g.recmap[ni];
+  if (!ODD && ((a.flags & F_NOPULL) || cls == 0)) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) f[k] = Store<S>::ldr(An, k * g.plane);
+  } else if (ODD && cls == 0) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+      f[k] = Store<S>::ldr(An, INVk(k) * g.plane - (long long)(CYk(k) * g.pitch + CXk(k)));
+  } else {
+    f[0] = Store<S>::ldr(A, ni);
+    special_links_aa<S, ODD>(f, a, A, n, r);
+  }
+  T rho, ux, uy;
+  node_update<S, COLL, FORC>(f, a, n, rho, ux, uy, y * g.nseg + (x >> 5));
+  if (!ODD) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Store<S>::str(An, INVk(k) * g.plane, f[k]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+      Store<S>::str(An, k * g.plane + (long long)(CYk(k) * g.pitch + CXk(k)), f[k]);
+  }
+  node_outputs<T>(a, n, r, rho, ux, uy, red);
+}
+
 template <class S, int COLL, int FORC, int CAP, bool ODD>
 __global__ void __launch_bounds__(CAP ? 256 : 512, CAP == 1 ? 8 : (CAP == 2 ? 6 : 1))
     step_aa_kernel(const StepArgs a) {
   using T = typename Store<S>::T;
-  const Geom& g = a.g;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   T red[7] = {0, 0, 0, 0, 0, 0, 0};
-  if (x < g.nx) {
-    const int ni = (y + 1) * g.pitch + x;
-    const long long n = ni;
-    S* A = static_cast<S*>(a.fout);   // == a.fin
-    S* An = A + ni;                   // this node's element of plane 0 (uniform offsets below)
-    int cls = 0;
-    if (g.segflag[y * g.nseg + (x >> 5)]) cls = g.cls[ni];
-    if (cls != 2) {
-      T f[9];
-      int r = -1;
-      if (cls == 1) r = g.recmap[ni];
-      if (!ODD && ((a.flags & F_NOPULL) || cls == 0)) {
-#pragma unroll
-        for (int k = 0; k < 9; ++k) f[k] = Store<S>::ldr(An, k * g.plane);
-      } else if (ODD && cls == 0) {
-#pragma unroll
-        for (int k = 0; k < 9; ++k)
-          f[k] = Store<S>::ldr(An, INVk(k) * g.plane - (long long)(CYk(k) * g.pitch + CXk(k)));
-      } else {
-        f[0] = Store<S>::ldr(A, ni);
-        special_links_aa<S, ODD>(f, a, A, n, r);
-      }
-      T rho, ux, uy;
-      node_update<S, COLL, FORC>(f, a, n, rho, ux, uy, y * g.nseg + (x >> 5));
-      if (!ODD) {
-#pragma unroll
-        for (int k = 0; k < 9; ++k) Store<S>::str(An, INVk(k) * g.plane, f[k]);
-      } else {
-#pragma unroll
-        for (int k = 0; k < 9; ++k)
-          Store<S>::str(An, k * g.plane + (long long)(CYk(k) * g.pitch + CXk(k)), f[k]);
-      }
-      node_outputs<T>(a, n, r, rho, ux, uy, red);
-    }
-  }
+  if (x < a.g.nx) aa_node<S, COLL, FORC, ODD>(a, x, y, red);
   if (a.flags & F_RESIDUAL) block_residual<decltype(red[0] + 0)>(a, red);
 }
 
@@ -933,23 +938,98 @@ template <> struct PairIO<float> {
   __device__ static __forceinline__ W pack(float lo, float hi) { return make_float2(lo, hi); }
 };
 
-// Incoming word of direction K for the pair at word index wi (both nodes).
+// Incoming word of direction K for the pair whose word of plane `plane_k` in
+// its own row is at fp + plane_k * plane/2: the word c_ky rows away, combined
+// with its neighbour for c_kx != 0 (both nodes).
 template <class S, int K>
-__device__ __forceinline__ typename PairIO<S>::W pair_pull(const typename PairIO<S>::W* __restrict__ fw,
-                                                           const Geom& g, long long wi) {
+__device__ __forceinline__ typename PairIO<S>::W pair_pull(const typename PairIO<S>::W* __restrict__ fp,
+                                                           const Geom& g, int plane_k = K) {
   using IO = PairIO<S>;
   constexpr int cx = CXk(K), cy = CYk(K);
-  const long long r = (long long)K * (g.plane >> 1) - (long long)cy * (g.pitch >> 1) + wi;
-  if (cx == 0) return IO::ld(fw, r);
-  if (cx == 1) return IO::mid(IO::ld(fw, r - 1), IO::ld(fw, r));
-  return IO::mid(IO::ld(fw, r), IO::ld(fw, r + 1));
+  const typename PairIO<S>::W* p =
+      fp + ((long long)plane_k * (g.plane >> 1) - (long long)cy * (g.pitch >> 1));
+  if (cx == 0) return IO::ld(p, 0);
+  if (cx == 1) return IO::mid(IO::ld(p, -1), IO::ld(p, 0));
+  return IO::mid(IO::ld(p, 0), IO::ld(p, 1));
+}
+
+// One pair of the node-pair kernel (row y, nodes x0 and x0 + 1).
+template <class S, int COLL, int FORC, bool RES>
+__device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, float red[7]) {
+  using IO = PairIO<S>;
+  using W = typename IO::W;
+  const Geom& g = a.g;
+  const int seg = y * g.nseg + (x0 >> 5);
+  if (g.segflag[seg] != 0 || (a.flags & F_NOPULL)) {
+    step_node<S, COLL, FORC, false, RES>(a, x0, y, red);
+    if (x0 + 1 < g.nx) step_node<S, COLL, FORC, false, RES>(a, x0 + 1, y, red);
+    return;
+  }
+  // both nodes are bulk nodes: every source is inside the grid
+  const int ni = (y + 1) * g.pitch + x0;   // even: pitch and x0 are even
+  const long long n = ni;
+  const long long wi = ni >> 1;
+  const W* __restrict__ fp = reinterpret_cast<const W*>(static_cast<const S*>(a.fin)) + wi;
+  W* __restrict__ op = reinterpret_cast<W*>(static_cast<S*>(a.fout)) + wi;
+  float old0[3], old1[3];
+  if (RES) {
+    load_old<float>(a, n, old0);
+    load_old<float>(a, n + 1, old1);
+  }
+  W w[9];
+  w[0] = pair_pull<S, 0>(fp, g);
+  w[1] = pair_pull<S, 1>(fp, g);
+  w[2] = pair_pull<S, 2>(fp, g);
+  w[3] = pair_pull<S, 3>(fp, g);
+  w[4] = pair_pull<S, 4>(fp, g);
+  w[5] = pair_pull<S, 5>(fp, g);
+  w[6] = pair_pull<S, 6>(fp, g);
+  w[7] = pair_pull<S, 7>(fp, g);
+  w[8] = pair_pull<S, 8>(fp, g);
+  float f0[9], f1[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) IO::unpack(w[k], f0[k], f1[k]);
+  float rho0, ux0, uy0, rho1, ux1, uy1;
+  node_update<S, COLL, FORC>(f0, a, n, rho0, ux0, uy0, seg);
+  node_update<S, COLL, FORC>(f1, a, n + 1, rho1, ux1, uy1, seg);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) op[(long long)k * (g.plane >> 1)] = IO::pack(f0[k], f1[k]);
+  node_outputs<float, RES ? RES_ON : RES_OFF>(a, n, -1, rho0, ux0, uy0, red, old0);
+  node_outputs<float, RES ? RES_ON : RES_OFF>(a, n + 1, -1, rho1, ux1, uy1, red, old1);
 }
 
 // CAP = 1 asks for 6 resident blocks of 256 threads (at most 40 registers),
-// CAP = 2 for 4 (at most 64).  RES: the residual instantiation.
-template <class S, int COLL, int FORC, int CAP, bool RES>
+// CAP = 2 for 4 (at most 64).  RES: the residual instantiation.  ROWS: rows
+// y0 .. y0 + ROWS - 1 one after the other per thread (fewer, longer-lived
+// blocks).
+template <class S, int COLL, int FORC, int CAP, bool RES, int ROWS>
 __global__ void __launch_bounds__(256, CAP == 1 ? 6 : (CAP == 2 ? 4 : 1))
     step_pair_kernel(const StepArgs a) {
+  const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  float red[7] = {0, 0, 0, 0, 0, 0, 0};
+  if (x0 < a.g.nx) {
+#pragma unroll 1
+    for (int r = 0; r < ROWS; ++r) {
+      const int y = blockIdx.y * ROWS + r;
+      if (y < a.g.ny) pair_step<S, COLL, FORC, RES>(a, x0, y, red);
+    }
+  }
+  if (RES) block_residual<float>(a, red);
+}
+
+// Node pairs in the AA layout.  Even phase: both nodes' own slots, aligned
+// words in and out (plane k in, plane kbar out).  Odd phase: the pull of
+// plane kbar from x0 - c_kx as in pair_pull, and pushes to x0 + c_kx of plane
+// k: aligned words for c_kx = 0, otherwise one value per node (the two
+// targets straddle two words whose other halves belong to the neighbouring
+// pairs).  Every slot is still read and written by one node only: the word
+// loads of the odd phase also bring in a neighbour's half, which that
+// neighbour may rewrite in the same phase, but only the own half is used.
+// Flagged segments, and every pair of a no-pull step in the odd phase, take
+// aa_node.
+template <class S, int COLL, int FORC, int CAP, bool ODD>
+__global__ void __launch_bounds__(256, CAP == 1 ? 6 : (CAP == 2 ? 4 : 1))
+    step_aa_pair_kernel(const StepArgs a) {
   using IO = PairIO<S>;
   using W = typename IO::W;
   const Geom& g = a.g;
@@ -958,44 +1038,56 @@ __global__ void __launch_bounds__(256, CAP == 1 ? 6 : (CAP == 2 ? 4 : 1))
   float red[7] = {0, 0, 0, 0, 0, 0, 0};
   if (x0 < g.nx) {
     const int seg = y * g.nseg + (x0 >> 5);
-    if (g.segflag[seg] != 0 || (a.flags & F_NOPULL)) {
-      step_node<S, COLL, FORC, false, RES>(a, x0, y, red);
-      if (x0 + 1 < g.nx) step_node<S, COLL, FORC, false, RES>(a, x0 + 1, y, red);
+    if (g.segflag[seg] != 0 || (ODD && (a.flags & F_NOPULL))) {
+      aa_node<S, COLL, FORC, ODD>(a, x0, y, red);
+      if (x0 + 1 < g.nx) aa_node<S, COLL, FORC, ODD>(a, x0 + 1, y, red);
     } else {
-      // both nodes are bulk nodes: every source is inside the grid
-      const int ni = (y + 1) * g.pitch + x0;   // even: pitch and x0 are even
+      const int ni = (y + 1) * g.pitch + x0;
       const long long n = ni;
-      const long long wi = ni >> 1;
-      const W* __restrict__ fw = reinterpret_cast<const W*>(static_cast<const S*>(a.fin));
-      W* __restrict__ ow = reinterpret_cast<W*>(static_cast<S*>(a.fout));
-      float old0[3], old1[3];
-      if (RES) {
-        load_old<float>(a, n, old0);
-        load_old<float>(a, n + 1, old1);
-      }
+      W* __restrict__ Ap = reinterpret_cast<W*>(static_cast<S*>(a.fout)) + (ni >> 1);   // plane 0 word
+      const long long wp = g.plane >> 1;
       W w[9];
-      w[0] = pair_pull<S, 0>(fw, g, wi);
-      w[1] = pair_pull<S, 1>(fw, g, wi);
-      w[2] = pair_pull<S, 2>(fw, g, wi);
-      w[3] = pair_pull<S, 3>(fw, g, wi);
-      w[4] = pair_pull<S, 4>(fw, g, wi);
-      w[5] = pair_pull<S, 5>(fw, g, wi);
-      w[6] = pair_pull<S, 6>(fw, g, wi);
-      w[7] = pair_pull<S, 7>(fw, g, wi);
-      w[8] = pair_pull<S, 8>(fw, g, wi);
+      if (!ODD) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) w[k] = IO::ld(Ap, k * wp);
+      } else {
+        w[0] = pair_pull<S, 0>(Ap, g, INVk(0));
+        w[1] = pair_pull<S, 1>(Ap, g, INVk(1));
+        w[2] = pair_pull<S, 2>(Ap, g, INVk(2));
+        w[3] = pair_pull<S, 3>(Ap, g, INVk(3));
+        w[4] = pair_pull<S, 4>(Ap, g, INVk(4));
+        w[5] = pair_pull<S, 5>(Ap, g, INVk(5));
+        w[6] = pair_pull<S, 6>(Ap, g, INVk(6));
+        w[7] = pair_pull<S, 7>(Ap, g, INVk(7));
+        w[8] = pair_pull<S, 8>(Ap, g, INVk(8));
+      }
       float f0[9], f1[9];
 #pragma unroll
       for (int k = 0; k < 9; ++k) IO::unpack(w[k], f0[k], f1[k]);
       float rho0, ux0, uy0, rho1, ux1, uy1;
       node_update<S, COLL, FORC>(f0, a, n, rho0, ux0, uy0, seg);
       node_update<S, COLL, FORC>(f1, a, n + 1, rho1, ux1, uy1, seg);
+      if (!ODD) {
 #pragma unroll
-      for (int k = 0; k < 9; ++k) ow[(long long)k * (g.plane >> 1) + wi] = IO::pack(f0[k], f1[k]);
-      node_outputs<float, RES ? RES_ON : RES_OFF>(a, n, -1, rho0, ux0, uy0, red, old0);
-      node_outputs<float, RES ? RES_ON : RES_OFF>(a, n + 1, -1, rho1, ux1, uy1, red, old1);
+        for (int k = 0; k < 9; ++k) Ap[INVk(k) * wp] = IO::pack(f0[k], f1[k]);
+      } else {
+        S* An = static_cast<S*>(a.fout) + ni;   // node x0's element of plane 0
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          if (CXk(k) == 0) {   // both targets in one word, c_ky rows away
+            Ap[k * wp + (long long)CYk(k) * (g.pitch >> 1)] = IO::pack(f0[k], f1[k]);
+          } else {
+            const long long t = k * g.plane + (long long)(CYk(k) * g.pitch + CXk(k));
+            Store<S>::str(An, t, f0[k]);
+            Store<S>::str(An, t + 1, f1[k]);
+          }
+        }
+      }
+      node_outputs<float, RES_FLAG>(a, n, -1, rho0, ux0, uy0, red);
+      node_outputs<float, RES_FLAG>(a, n + 1, -1, rho1, ux1, uy1, red);
     }
   }
-  if (RES) block_residual<float>(a, red);
+  if (a.flags & F_RESIDUAL) block_residual<float>(a, red);
 }
 
 // ---------------------------------------------------------------------------
@@ -1203,11 +1295,12 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 // Waits for `parity` of the barrier; false after ~1 s (then *err is set).
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, int* err) {
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, int* err,
+                                                  unsigned long long limit_ns = 1000000000ull) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
   while (!mbar_try_wait(bar, parity)) {
-    if (global_ns() - t0 > 1000000000ull) {
+    if (global_ns() - t0 > limit_ns) {
       atomicExch(err, kErrWaitTimeout);
       return false;
     }

@@ -79,6 +79,30 @@ __global__ void __launch_bounds__(kTile * kTileRows)
   }
 }
 
+// Self-test of the bounded wait: one thread waits on an mbarrier that
+// expects one arrival nobody makes.  The wait must give up after limit_ns,
+// set kErrWaitTimeout in *err and return; *waited_ns receives how long it
+// waited.  The barrier is invalidated before the block exits.
+__global__ void bounded_wait_selftest_kernel(int* err, unsigned long long limit_ns,
+                                             unsigned long long* waited_ns) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x != 0) return;
+  const uint32_t b = smem_u32(&bar);
+  mbar_init(b, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  const unsigned long long t0 = global_ns();
+  const bool got = mbar_wait_bounded(b, 0, err, limit_ns);
+  *waited_ns = global_ns() - t0;
+  if (got) atomicExch(err, 0);
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(b) : "memory");
+}
+
+cudaError_t bounded_wait_selftest(int* err, double limit_s, unsigned long long* waited_ns,
+                                  cudaStream_t s) {
+  bounded_wait_selftest_kernel<<<1, 32, 0, s>>>(err, (unsigned long long)(limit_s * 1e9), waited_ns);
+  return cudaGetLastError();
+}
+
 cudaError_t reorder(const Geom& g, const double* in, double* out, int ncomp,
                     int layout, int to_device, cudaStream_t s) {
   return reorder_cols(g, in, out, ncomp, layout, to_device, 0, g.nx, s);

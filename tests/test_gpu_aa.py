@@ -172,3 +172,47 @@ def test_aa_fp64_matches_two_buffers(which):
             rb, ub = ab.moments()
             assert np.array_equal(ra, rb) and np.array_equal(ua, ub)
             assert np.array_equal(aa.populations(), ab.populations())
+
+
+@pytest.mark.parametrize("storage", ["fp32_shifted", "fp16_shifted"])
+@pytest.mark.parametrize("coll", ["BGK", "MRT"])
+def test_aa_node_pairs_match_scalar_aa(storage, coll, monkeypatch):
+    """The AA node-pair kernel (two nodes per thread; aligned words in the
+    even phase, pulls of word pairs and per-node pushes in the odd phase) on a
+    grid wide enough for its fast path, odd and even step counts, with
+    moment and residual steps: the same fields and residuals as the
+    one-node-per-thread AA kernel, and the two-buffer run within AB_TOL."""
+    case = Case(workloads.cylinder(nx=512, ny=128, radius=16.0, center=(128, 67), model=coll))
+    fluid = ~case.solid
+    outs = []
+    for layout, v in (("aa", "0,1,128,1"), ("aa", "3,2,128,1"), ("aa", "3,2,256,0"),
+                      ("ab", "0,1,128,1")):
+        monkeypatch.setenv("LBM_VARIANT", v)
+        with FluidLBM(case, storage=storage, layout=layout) as sim:
+            sim.initialize()
+            res = []
+            for n in (1, 20, 37):
+                sim.step(n, moments=True, residual=True)
+                res.append(sim.residual())
+            want = tuple(int(i) for i in v.split(","))
+            assert sim.kernel_variant[:3] == want[:3]
+            outs.append((sim.moments()[1], np.array(res)))
+    u0, r0 = outs[0]
+    for u, r in outs[1:3]:
+        assert np.abs(u - u0)[fluid].max() <= 1e-6 * np.abs(u0[fluid]).max()
+        np.testing.assert_allclose(r, r0, rtol=1e-5)
+    uab = outs[3][0]
+    assert np.abs(u0 - uab)[fluid].max() <= AB_TOL[storage] * np.abs(uab[fluid]).max()
+
+
+def test_aa_default_launch_shape():
+    """Without LBM_VARIANT the AA layout runs the node-pair kernel for shifted
+    storage and the scalar kernel for FP64."""
+    import os
+    assert "LBM_VARIANT" not in os.environ
+    case = Case(load_golden("channel_cylinder_abb")[0])
+    for storage, shape in (("fp64", (0, 1, 128, 0)), ("fp32_shifted", (3, 2, 128, 1))):
+        with FluidLBM(case, storage=storage, layout="aa") as sim:
+            sim.initialize()
+            sim.step(3)
+            assert sim.kernel_variant == shape

@@ -59,3 +59,21 @@ def test_bounded_host_wait_gives_up_and_the_run_continues():
         rb, ub = b.moments()
         assert np.array_equal(ra, rb) and np.array_equal(ua, ub)
         assert np.array_equal(a.populations(), b.populations())
+
+
+def test_device_bounded_wait_gives_up_and_the_handle_stays_usable():
+    """A kernel waits on an mbarrier that nothing arrives at, with the bounded
+    wait of the pipelined step kernel limited to 20 ms: it gives up, sets the
+    handle's error word and returns; the call reports LBM_ERR_TIMEOUT, and the
+    handle then steps and reports a finite residual (no fault, no hang)."""
+    import ctypes
+    case = Case(workloads.cavity(32))
+    with FluidLBM(case, storage="fp32_shifted") as sim:
+        sim.initialize()
+        waited = ctypes.c_double()
+        rc = sim.lib.lbm_selftest_bounded_wait(sim.h, 0.02, ctypes.byref(waited))
+        assert rc == capi.LBM_ERR_TIMEOUT
+        assert "mbarrier" in sim.lib.lbm_last_error().decode()
+        assert 0.02 <= waited.value < 1.0
+        sim.step(5, residual=True)
+        assert np.all(np.isfinite(sim.residual()))

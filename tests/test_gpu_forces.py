@@ -125,8 +125,10 @@ def test_ellipse_channel_against_c_oracle():
                 m = ~case.solid
                 assert np.array_equal(rho[m], st.inner(st.density)[m])
                 assert np.array_equal(us[storage][m], st.inner(st.velocity)[m])
+                # the torque (4e-4) is a sum of ~10^3 arm x momentum terms of
+                # either sign, summed in another order on the GPU: 1e-13 absolute
                 np.testing.assert_allclose(sim.forces()["obstacles"][0], ref, rtol=FORCE_RTOL,
-                                           atol=1e-14)
+                                           atol=1e-13)
     m = ~case.solid
     err = np.abs(us["fp32_shifted"][m] - us["fp64"][m]).max() / np.abs(us["fp64"][m]).max()
     assert err <= 1e-5, err

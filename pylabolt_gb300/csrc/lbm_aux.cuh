@@ -115,16 +115,14 @@ struct Kernels {
     return cudaGetLastError();
   }
 
-  // The node-pair kernel: vec = 2 x rows per thread (2 or 4), stages = its
-  // register cap (0 none, 1 40, 2 64).
+  // The node-pair kernel (stages = register cap: 0 none, 1 40, 2 64).
   template <int COLL, int FORC, bool RES>
   static cudaError_t pair(const StepArgs& a, Variant v, dim3 grid, cudaStream_t s) {
     if constexpr (Store<S>::shifted) {
-      switch (v.stages * 10 + v.vec) {
-        case 2: step_pair_kernel<S, COLL, FORC, 0, RES, 1><<<grid, v.block, 0, s>>>(a); break;
-        case 12: step_pair_kernel<S, COLL, FORC, 1, RES, 1><<<grid, v.block, 0, s>>>(a); break;
-        case 22: step_pair_kernel<S, COLL, FORC, 2, RES, 1><<<grid, v.block, 0, s>>>(a); break;
-        case 14: step_pair_kernel<S, COLL, FORC, 1, RES, 2><<<grid, v.block, 0, s>>>(a); break;
+      switch (v.stages) {
+        case 0: step_pair_kernel<S, COLL, FORC, 0, RES><<<grid, v.block, 0, s>>>(a); break;
+        case 1: step_pair_kernel<S, COLL, FORC, 1, RES><<<grid, v.block, 0, s>>>(a); break;
+        case 2: step_pair_kernel<S, COLL, FORC, 2, RES><<<grid, v.block, 0, s>>>(a); break;
         default: return cudaErrorInvalidValue;
       }
       return cudaGetLastError();
@@ -168,7 +166,7 @@ struct Kernels {
     }
     if constexpr (Store<S>::shifted) {
       if (v.kind == 3) {   // node pairs (not for moving obstacles: class-4 nodes)
-        if ((v.vec != 2 && v.vec != 4) || v.block > 256 || a.rho_dyn_out) return cudaErrorInvalidValue;
+        if (v.vec != 2 || v.block > 256 || a.rho_dyn_out) return cudaErrorInvalidValue;
         if (a.flags & F_RESIDUAL) return pair<COLL, FORC, true>(a, v, grid, s);
         return pair<COLL, FORC, false>(a, v, grid, s);
       }
@@ -288,14 +286,14 @@ struct Kernels {
       constexpr int V2 = sizeof(S) == 4 ? 2 : 4;
       // kind 2: {threads, stages}; kind 1: {nodes per thread, threads};
       // kind 0: {threads, register cap: 0 none, 1 32, 2 40};
-      // kind 3: node pairs {2 x rows per thread, threads, register cap: 0 none,
+      // kind 3: node pairs {2 nodes per thread, threads, register cap: 0 none,
       // 1 40, 2 64}
       const Variant vs[] = {{2, 0, 256, 4}, {2, 0, 512, 3}, {2, 0, 256, 2}, {1, V1, 256, 0},
                             {1, V2, 256, 0}, {0, 1, 128, 0}, {0, 1, 256, 0}, {0, 1, 128, 1},
                             {0, 1, 256, 1}, {0, 1, 128, 2}, {0, 1, 256, 2}, {3, 2, 128, 0},
-                            {3, 2, 256, 0}, {3, 2, 128, 1}, {3, 2, 256, 2}, {3, 4, 128, 1}};
-      k.nvariants = 16;
-      for (int i = 0; i < 16; ++i) k.variants[i] = vs[i];
+                            {3, 2, 256, 0}, {3, 2, 128, 1}, {3, 2, 256, 2}};
+      k.nvariants = 15;
+      for (int i = 0; i < 15; ++i) k.variants[i] = vs[i];
     } else {
       const Variant vs[] = {{0, 1, 128, 0}, {0, 1, 256, 0}, {0, 1, 512, 0}};
       k.nvariants = 3;

@@ -378,6 +378,7 @@ struct LbmHandle {
     a.rho_dyn_out = rdout;
     a.aa = aa_phase;
     a.flags = flags;
+    lbm::fill_offsets(a, ks->elem_bytes);
     LBM_CUDA(ks->step(cfg.collision, cfg.forcing, a, v, sms, on ? on : stream));
     return LBM_OK;
   }
@@ -873,12 +874,16 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   g.nrec = (int)nlinks;
   const size_t eb = ks->elem_bytes, cb = ks->compute_bytes;
   const size_t nrec1 = std::max<int64_t>(nlinks, 1);
-  void *d_cls, *d_seg, *d_recmap, *d_rtype, *d_rsrc, *d_rparam, *d_raux;
+  void *d_cls, *d_seg, *d_recmap, *d_rtype, *d_rsrc, *d_rparam, *d_raux, *d_rpf;
+  std::vector<float2> rpf(rparam.size());
+  for (size_t i = 0; i < rparam.size(); ++i)
+    rpf[i] = make_float2((float)rparam[i], (float)(rparam[i] - 1.0));
   int rc;
   if ((rc = h->alloc(&d_cls, plane)) || (rc = h->alloc(&d_seg, segflag.size())) ||
       (rc = h->alloc(&d_recmap, plane * sizeof(int))) || (rc = h->alloc(&d_rtype, 9 * nrec1)) ||
       (rc = h->alloc(&d_rsrc, 9 * nrec1 * sizeof(int))) ||
       (rc = h->alloc(&d_rparam, 9 * nrec1 * sizeof(double))) ||
+      (rc = h->alloc(&d_rpf, 9 * nrec1 * sizeof(float2))) ||
       (rc = h->alloc(&d_raux, 9 * nrec1 * sizeof(int))) ||
       (rc = h->alloc(&h->pop_raw[0], (9 * plane + 2 * pitch) * eb)) ||
       (!aa && (rc = h->alloc(&h->pop_raw[1], (9 * plane + 2 * pitch) * eb))) ||
@@ -930,6 +935,7 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   g.rtype = (const int8_t*)d_rtype;
   g.rsrc = (const int*)d_rsrc;
   g.rparam = (const double*)d_rparam;
+  g.rpf = (const float2*)d_rpf;
   g.raux = (const int*)d_raux;
   auto up = [&](void* d, const void* src, size_t bytes) {
     return cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, h->stream);
@@ -940,6 +946,7 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
       (e = up(d_rtype, rtype.data(), rtype.size())) != cudaSuccess ||
       (e = up(d_rsrc, rsrc.data(), rsrc.size() * sizeof(int))) != cudaSuccess ||
       (e = up(d_rparam, rparam.data(), rparam.size() * sizeof(double))) != cudaSuccess ||
+      (e = up(d_rpf, rpf.data(), rpf.size() * sizeof(float2))) != cudaSuccess ||
       (e = up(d_raux, raux.data(), raux.size() * sizeof(int))) != cudaSuccess)
     return bail(fail(LBM_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(e)));
   for (int i = 0; i < 2; ++i) {

@@ -25,6 +25,9 @@ struct Geom {
   const int8_t* rtype;       // [nrec*9] link kind
   const int* rsrc;           // [nrec*9] PULL source node (device index)
   const double* rparam;      // [nrec*9]
+  const float2* rpf;         // [nrec*9] FP32 (param, param - 1), rounded from
+                             // FP64 on the host: the shifted paths read these,
+                             // so that no FP64 conversion runs in the step
   const int* raux;           // [nrec*9] ABB: record index of node x+n
 #ifdef __CUDACC__
   __host__ __device__
@@ -86,7 +89,27 @@ struct StepArgs {
   int aa;                  // 0: two buffers (fin -> fout); AA layout (fin == fout):
                            // 1 even phase, 2 odd phase
   int flags;
+  // Byte offsets of direction k from a node's element of plane 0, filled on
+  // the host so that the node-pair kernels add a constant per access instead
+  // of forming it: the pull source (plane k, row y - c_ky), the plane k of the
+  // node itself, the AA odd phase's pull (plane kbar, row y - c_ky) and push
+  // (plane k, node + c_k).
+  long long off_pull[9], off_plane[9], off_aa_pull[9], off_aa_push[9];
 };
+
+// Fills the byte offsets of StepArgs for storage elements of `eb` bytes.
+inline void fill_offsets(StepArgs& a, int eb) {
+  static const int cx[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+  static const int cy[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+  static const int inv[9] = {0, 3, 4, 1, 2, 7, 8, 5, 6};
+  const long long P = a.g.plane, R = a.g.pitch;
+  for (int k = 0; k < 9; ++k) {
+    a.off_pull[k] = (k * P - cy[k] * R) * eb;
+    a.off_plane[k] = k * P * eb;
+    a.off_aa_pull[k] = (inv[k] * P - cy[k] * R) * eb;
+    a.off_aa_push[k] = (k * P + cy[k] * R + cx[k]) * eb;
+  }
+}
 
 // Arguments of one reverse (adjoint) step; see lbm_adjoint.cuh.
 struct AdjArgs {
@@ -170,8 +193,8 @@ struct MovArgs {
 //   kind 1: vector kernel, `vec` consecutive nodes per thread
 //   kind 2: persistent TMA-pipelined kernel: tiles of one row segment of
 //           kTmaRowBytes, `stages` shared-memory stages, `block` threads
-//   kind 3: node-pair kernel, two nodes per thread along x for each of
-//           vec / 2 rows, `stages` its register cap
+//   kind 3: node-pair kernel, two nodes per thread along x (vec = 2),
+//           `stages` its register cap
 struct Variant {
   int kind;
   int vec;
@@ -253,11 +276,6 @@ inline dim3 step_grid(const Geom& g, Variant v, int sms, int elem_bytes) {
     long long blocks = (long long)sms * per_sm;
     if (blocks > tiles) blocks = tiles;
     return dim3((unsigned)blocks, 1);
-  }
-  if (v.kind == 3) {   // node pairs: two nodes per thread along x, vec / 2 rows
-    const int rows = v.vec / 2;
-    return dim3((unsigned)((g.pitch + 2LL * v.block - 1) / (2LL * v.block)),
-                (unsigned)((g.ny + rows - 1) / rows));
   }
   const long long per_block = (long long)v.block * v.vec;
   return dim3((unsigned)((g.pitch + per_block - 1) / per_block), (unsigned)g.ny);

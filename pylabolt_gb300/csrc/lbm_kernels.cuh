@@ -98,10 +98,10 @@ template <> struct Store<__half> {
     p[i] = __float2half_rn(v);
   }
   __device__ static __forceinline__ T ld(const __half* __restrict__ p, long long i, const Params& q) {
-    return __half2float(p[i]) * float(q.inv_scale);
+    return __half2float(p[i]) * q.f_inv_scale;
   }
   __device__ static __forceinline__ void st(__half* __restrict__ p, long long i, T v, const Params& q) {
-    p[i] = __float2half_rn(v * float(q.scale));
+    p[i] = __float2half_rn(v * q.f_scale);
   }
 };
 
@@ -373,7 +373,7 @@ __device__ __forceinline__ typename Store<S>::T special_link(
     const T rho = side[3 * r];
     if (!SH)
       return raw - ((T(2.0 * Wk(KB)) * rho) * T(p.inv_cs_2)) * T(g.rparam[li]);
-    return raw - (T(2.0 * Wk(KB)) * rho * T(3)) * T(g.rparam[li]);
+    return raw - (T(2.0 * Wk(KB)) * rho * T(3)) * g.rpf[li].x;
   }
   // LINK_ABB -- fluid_boundary_kernels.py:100-152
   const int ra = g.raux[li];
@@ -382,15 +382,20 @@ __device__ __forceinline__ typename Store<S>::T special_link(
   const T uey = uy + T(0.5) * (uy - side[3 * ra + 2]);
   const T u2 = uex * uex + uey * uey;
   const T cu = lin2<CXk(KB), CYk(KB)>(uex, uey);
-  const T rho_w = T(g.rparam[li]);
+  T rho_w;
+  if constexpr (SH)
+    rho_w = g.rpf[li].x;
+  else
+    rho_w = g.rparam[li];
   if (!SH) {
     const T temp = (T(2.0 * Wk(KB)) * rho_w) *
                    ((T(1) + (T(p.half_inv_cs_4) * cu) * cu) - T(p.half_inv_cs_2) * u2);
     return -raw + temp;
   }
-  // rho_w - 1 is formed in FP64: rounding rho_w itself to FP32 would shift the
-  // imposed density difference by up to 6e-8 absolute.
-  const T drho_w = T(g.rparam[li] - 1.0);
+  // rho_w - 1 is formed in FP64 (on the host, rpf.y): rounding rho_w itself
+  // to FP32 would shift the imposed density difference by up to 6e-8
+  // absolute.
+  const T drho_w = g.rpf[li].y;
   return -raw + T(2.0 * Wk(KB)) * (drho_w + rho_w * (T(4.5) * cu * cu - T(1.5) * u2));
 }
 
@@ -803,7 +808,7 @@ __device__ __forceinline__ typename Store<S>::T special_link_aa(
     const T rho = side[3 * r];
     if (!SH)
       return raw - ((T(2.0 * Wk(KB)) * rho) * T(p.inv_cs_2)) * T(g.rparam[li]);
-    return raw - (T(2.0 * Wk(KB)) * rho * T(3)) * T(g.rparam[li]);
+    return raw - (T(2.0 * Wk(KB)) * rho * T(3)) * g.rpf[li].x;
   }
   const int ra = g.raux[li];
   const T ux = side[3 * r + 1], uy = side[3 * r + 2];
@@ -811,13 +816,17 @@ __device__ __forceinline__ typename Store<S>::T special_link_aa(
   const T uey = uy + T(0.5) * (uy - side[3 * ra + 2]);
   const T u2 = uex * uex + uey * uey;
   const T cu = lin2<CXk(KB), CYk(KB)>(uex, uey);
-  const T rho_w = T(g.rparam[li]);
+  T rho_w;
+  if constexpr (SH)
+    rho_w = g.rpf[li].x;
+  else
+    rho_w = g.rparam[li];
   if (!SH) {
     const T temp = (T(2.0 * Wk(KB)) * rho_w) *
                    ((T(1) + (T(p.half_inv_cs_4) * cu) * cu) - T(p.half_inv_cs_2) * u2);
     return -raw + temp;
   }
-  const T drho_w = T(g.rparam[li] - 1.0);
+  const T drho_w = g.rpf[li].y;
   return -raw + T(2.0 * Wk(KB)) * (drho_w + rho_w * (T(4.5) * cu * cu - T(1.5) * u2));
 }
 
@@ -938,16 +947,15 @@ template <> struct PairIO<float> {
   __device__ static __forceinline__ W pack(float lo, float hi) { return make_float2(lo, hi); }
 };
 
-// Incoming word of direction K for the pair whose word of plane `plane_k` in
-// its own row is at fp + plane_k * plane/2: the word c_ky rows away, combined
+// Incoming word of direction K for the pair whose plane-0 element is at byte
+// address `fb`: the word `off` bytes away (a plane and c_ky rows), combined
 // with its neighbour for c_kx != 0 (both nodes).
 template <class S, int K>
-__device__ __forceinline__ typename PairIO<S>::W pair_pull(const typename PairIO<S>::W* __restrict__ fp,
-                                                           const Geom& g, int plane_k = K) {
+__device__ __forceinline__ typename PairIO<S>::W pair_pull(const char* __restrict__ fb, long long off) {
   using IO = PairIO<S>;
-  constexpr int cx = CXk(K), cy = CYk(K);
-  const typename PairIO<S>::W* p =
-      fp + ((long long)plane_k * (g.plane >> 1) - (long long)cy * (g.pitch >> 1));
+  using W = typename IO::W;
+  constexpr int cx = CXk(K);
+  const W* p = reinterpret_cast<const W*>(fb + off);
   if (cx == 0) return IO::ld(p, 0);
   if (cx == 1) return IO::mid(IO::ld(p, -1), IO::ld(p, 0));
   return IO::mid(IO::ld(p, 0), IO::ld(p, 1));
@@ -968,24 +976,23 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, floa
   // both nodes are bulk nodes: every source is inside the grid
   const int ni = (y + 1) * g.pitch + x0;   // even: pitch and x0 are even
   const long long n = ni;
-  const long long wi = ni >> 1;
-  const W* __restrict__ fp = reinterpret_cast<const W*>(static_cast<const S*>(a.fin)) + wi;
-  W* __restrict__ op = reinterpret_cast<W*>(static_cast<S*>(a.fout)) + wi;
+  const char* __restrict__ fb = reinterpret_cast<const char*>(static_cast<const S*>(a.fin) + ni);
+  char* __restrict__ ob = reinterpret_cast<char*>(static_cast<S*>(a.fout) + ni);
   float old0[3], old1[3];
   if (RES) {
     load_old<float>(a, n, old0);
     load_old<float>(a, n + 1, old1);
   }
   W w[9];
-  w[0] = pair_pull<S, 0>(fp, g);
-  w[1] = pair_pull<S, 1>(fp, g);
-  w[2] = pair_pull<S, 2>(fp, g);
-  w[3] = pair_pull<S, 3>(fp, g);
-  w[4] = pair_pull<S, 4>(fp, g);
-  w[5] = pair_pull<S, 5>(fp, g);
-  w[6] = pair_pull<S, 6>(fp, g);
-  w[7] = pair_pull<S, 7>(fp, g);
-  w[8] = pair_pull<S, 8>(fp, g);
+  w[0] = pair_pull<S, 0>(fb, a.off_pull[0]);
+  w[1] = pair_pull<S, 1>(fb, a.off_pull[1]);
+  w[2] = pair_pull<S, 2>(fb, a.off_pull[2]);
+  w[3] = pair_pull<S, 3>(fb, a.off_pull[3]);
+  w[4] = pair_pull<S, 4>(fb, a.off_pull[4]);
+  w[5] = pair_pull<S, 5>(fb, a.off_pull[5]);
+  w[6] = pair_pull<S, 6>(fb, a.off_pull[6]);
+  w[7] = pair_pull<S, 7>(fb, a.off_pull[7]);
+  w[8] = pair_pull<S, 8>(fb, a.off_pull[8]);
   float f0[9], f1[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) IO::unpack(w[k], f0[k], f1[k]);
@@ -993,27 +1000,21 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, floa
   node_update<S, COLL, FORC>(f0, a, n, rho0, ux0, uy0, seg);
   node_update<S, COLL, FORC>(f1, a, n + 1, rho1, ux1, uy1, seg);
 #pragma unroll
-  for (int k = 0; k < 9; ++k) op[(long long)k * (g.plane >> 1)] = IO::pack(f0[k], f1[k]);
+  for (int k = 0; k < 9; ++k) *reinterpret_cast<W*>(ob + a.off_plane[k]) = IO::pack(f0[k], f1[k]);
   node_outputs<float, RES ? RES_ON : RES_OFF>(a, n, -1, rho0, ux0, uy0, red, old0);
   node_outputs<float, RES ? RES_ON : RES_OFF>(a, n + 1, -1, rho1, ux1, uy1, red, old1);
 }
 
 // CAP = 1 asks for 6 resident blocks of 256 threads (at most 40 registers),
-// CAP = 2 for 4 (at most 64).  RES: the residual instantiation.  ROWS: rows
-// y0 .. y0 + ROWS - 1 one after the other per thread (fewer, longer-lived
-// blocks).
-template <class S, int COLL, int FORC, int CAP, bool RES, int ROWS>
+// CAP = 2 for 4 (at most 64).  RES: the residual instantiation.  (Two rows per
+// thread, one after the other, ran no faster: 131.8 against 131.5 GLUPS in
+// FP16, 87.6 against 91.0 in FP32.)
+template <class S, int COLL, int FORC, int CAP, bool RES>
 __global__ void __launch_bounds__(256, CAP == 1 ? 6 : (CAP == 2 ? 4 : 1))
     step_pair_kernel(const StepArgs a) {
   const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
   float red[7] = {0, 0, 0, 0, 0, 0, 0};
-  if (x0 < a.g.nx) {
-#pragma unroll 1
-    for (int r = 0; r < ROWS; ++r) {
-      const int y = blockIdx.y * ROWS + r;
-      if (y < a.g.ny) pair_step<S, COLL, FORC, RES>(a, x0, y, red);
-    }
-  }
+  if (x0 < a.g.nx) pair_step<S, COLL, FORC, RES>(a, x0, blockIdx.y, red);
   if (RES) block_residual<float>(a, red);
 }
 
@@ -1044,22 +1045,21 @@ __global__ void __launch_bounds__(256, CAP == 1 ? 6 : (CAP == 2 ? 4 : 1))
     } else {
       const int ni = (y + 1) * g.pitch + x0;
       const long long n = ni;
-      W* __restrict__ Ap = reinterpret_cast<W*>(static_cast<S*>(a.fout)) + (ni >> 1);   // plane 0 word
-      const long long wp = g.plane >> 1;
+      char* __restrict__ Ab = reinterpret_cast<char*>(static_cast<S*>(a.fout) + ni);   // plane 0 element
       W w[9];
       if (!ODD) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) w[k] = IO::ld(Ap, k * wp);
+        for (int k = 0; k < 9; ++k) w[k] = *reinterpret_cast<const W*>(Ab + a.off_plane[k]);
       } else {
-        w[0] = pair_pull<S, 0>(Ap, g, INVk(0));
-        w[1] = pair_pull<S, 1>(Ap, g, INVk(1));
-        w[2] = pair_pull<S, 2>(Ap, g, INVk(2));
-        w[3] = pair_pull<S, 3>(Ap, g, INVk(3));
-        w[4] = pair_pull<S, 4>(Ap, g, INVk(4));
-        w[5] = pair_pull<S, 5>(Ap, g, INVk(5));
-        w[6] = pair_pull<S, 6>(Ap, g, INVk(6));
-        w[7] = pair_pull<S, 7>(Ap, g, INVk(7));
-        w[8] = pair_pull<S, 8>(Ap, g, INVk(8));
+        w[0] = pair_pull<S, 0>(Ab, a.off_aa_pull[0]);
+        w[1] = pair_pull<S, 1>(Ab, a.off_aa_pull[1]);
+        w[2] = pair_pull<S, 2>(Ab, a.off_aa_pull[2]);
+        w[3] = pair_pull<S, 3>(Ab, a.off_aa_pull[3]);
+        w[4] = pair_pull<S, 4>(Ab, a.off_aa_pull[4]);
+        w[5] = pair_pull<S, 5>(Ab, a.off_aa_pull[5]);
+        w[6] = pair_pull<S, 6>(Ab, a.off_aa_pull[6]);
+        w[7] = pair_pull<S, 7>(Ab, a.off_aa_pull[7]);
+        w[8] = pair_pull<S, 8>(Ab, a.off_aa_pull[8]);
       }
       float f0[9], f1[9];
 #pragma unroll
@@ -1069,17 +1069,18 @@ __global__ void __launch_bounds__(256, CAP == 1 ? 6 : (CAP == 2 ? 4 : 1))
       node_update<S, COLL, FORC>(f1, a, n + 1, rho1, ux1, uy1, seg);
       if (!ODD) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) Ap[INVk(k) * wp] = IO::pack(f0[k], f1[k]);
+        for (int k = 0; k < 9; ++k)
+          *reinterpret_cast<W*>(Ab + a.off_plane[INVk(k)]) = IO::pack(f0[k], f1[k]);
       } else {
-        S* An = static_cast<S*>(a.fout) + ni;   // node x0's element of plane 0
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
+          char* t = Ab + a.off_aa_push[k];
           if (CXk(k) == 0) {   // both targets in one word, c_ky rows away
-            Ap[k * wp + (long long)CYk(k) * (g.pitch >> 1)] = IO::pack(f0[k], f1[k]);
+            *reinterpret_cast<W*>(t) = IO::pack(f0[k], f1[k]);
           } else {
-            const long long t = k * g.plane + (long long)(CYk(k) * g.pitch + CXk(k));
-            Store<S>::str(An, t, f0[k]);
-            Store<S>::str(An, t + 1, f1[k]);
+            S* ts = reinterpret_cast<S*>(t);
+            Store<S>::str(ts, 0, f0[k]);
+            Store<S>::str(ts, 1, f1[k]);
           }
         }
       }

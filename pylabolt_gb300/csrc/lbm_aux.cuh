@@ -115,7 +115,7 @@ struct Kernels {
     return cudaGetLastError();
   }
 
-  // The node-pair kernel (stages = register cap: 0 none, 1 40, 2 64).
+  // The node-pair kernel (stages = register cap: 0 none, 1 40, 2 64, 3 32).
   template <int COLL, int FORC, bool RES>
   static cudaError_t pair(const StepArgs& a, Variant v, dim3 grid, cudaStream_t s) {
     if constexpr (Store<S>::shifted) {
@@ -123,6 +123,7 @@ struct Kernels {
         case 0: step_pair_kernel<S, COLL, FORC, 0, RES><<<grid, v.block, 0, s>>>(a); break;
         case 1: step_pair_kernel<S, COLL, FORC, 1, RES><<<grid, v.block, 0, s>>>(a); break;
         case 2: step_pair_kernel<S, COLL, FORC, 2, RES><<<grid, v.block, 0, s>>>(a); break;
+        case 3: step_pair_kernel<S, COLL, FORC, 3, RES><<<grid, v.block, 0, s>>>(a); break;
         default: return cudaErrorInvalidValue;
       }
       return cudaGetLastError();
@@ -287,13 +288,13 @@ struct Kernels {
       // kind 2: {threads, stages}; kind 1: {nodes per thread, threads};
       // kind 0: {threads, register cap: 0 none, 1 32, 2 40};
       // kind 3: node pairs {2 nodes per thread, threads, register cap: 0 none,
-      // 1 40, 2 64}
+      // 1 40, 2 64, 3 32}
       const Variant vs[] = {{2, 0, 256, 4}, {2, 0, 512, 3}, {2, 0, 256, 2}, {1, V1, 256, 0},
                             {1, V2, 256, 0}, {0, 1, 128, 0}, {0, 1, 256, 0}, {0, 1, 128, 1},
                             {0, 1, 256, 1}, {0, 1, 128, 2}, {0, 1, 256, 2}, {3, 2, 128, 0},
-                            {3, 2, 256, 0}, {3, 2, 128, 1}, {3, 2, 256, 2}};
-      k.nvariants = 15;
-      for (int i = 0; i < 15; ++i) k.variants[i] = vs[i];
+                            {3, 2, 256, 0}, {3, 2, 128, 1}, {3, 2, 256, 2}, {3, 2, 128, 3}};
+      k.nvariants = 16;
+      for (int i = 0; i < 16; ++i) k.variants[i] = vs[i];
     } else {
       const Variant vs[] = {{0, 1, 128, 0}, {0, 1, 256, 0}, {0, 1, 512, 0}};
       k.nvariants = 3;

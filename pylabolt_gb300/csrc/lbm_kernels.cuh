@@ -961,6 +961,37 @@ __device__ __forceinline__ typename PairIO<S>::W pair_pull(const char* __restric
   return IO::mid(IO::ld(p, 0), IO::ld(p, 1));
 }
 
+// Moment output and residual terms of a bulk pair (nodes n, n + 1; n even),
+// the two nodes' values moved as one 8-byte word per field (node_outputs does
+// the same per node).  o2: the previous residual step's fields (RES).
+template <bool RES>
+__device__ __forceinline__ void pair_outputs(const StepArgs& a, long long n, float rho0, float ux0,
+                                             float uy0, float rho1, float ux1, float uy1,
+                                             float red[7], const float2 o2[3]) {
+  const float2 v[3] = {make_float2(rho0, rho1), make_float2(ux0, ux1), make_float2(uy0, uy1)};
+  if (a.flags & F_MOMENTS) {
+    *reinterpret_cast<float2*>(static_cast<float*>(a.rho) + n) = v[0];
+    *reinterpret_cast<float2*>(static_cast<float*>(a.ux) + n) = v[1];
+    *reinterpret_cast<float2*>(static_cast<float*>(a.uy) + n) = v[2];
+  }
+  if (RES) {
+    // compute_residues_kernels.py:6-73: sums over fluid nodes
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float d0 = v[c].x - o2[c].x, d1 = v[c].y - o2[c].y;
+      red[2 * c] += d0 * d0;
+      red[2 * c] += d1 * d1;
+      red[2 * c + 1] += o2[c].x * o2[c].x;
+      red[2 * c + 1] += o2[c].y * o2[c].y;
+    }
+    red[6] += (isfinite(rho0) && isfinite(ux0) && isfinite(uy0)) ? 0.f : 1.f;
+    red[6] += (isfinite(rho1) && isfinite(ux1) && isfinite(uy1)) ? 0.f : 1.f;
+    *reinterpret_cast<float2*>(static_cast<float*>(a.rho_new) + n) = v[0];
+    *reinterpret_cast<float2*>(static_cast<float*>(a.ux_new) + n) = v[1];
+    *reinterpret_cast<float2*>(static_cast<float*>(a.uy_new) + n) = v[2];
+  }
+}
+
 // One pair of the node-pair kernel (row y, nodes x0 and x0 + 1).
 template <class S, int COLL, int FORC, bool RES>
 __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, float red[7]) {
@@ -978,10 +1009,12 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, floa
   const long long n = ni;
   const char* __restrict__ fb = reinterpret_cast<const char*>(static_cast<const S*>(a.fin) + ni);
   char* __restrict__ ob = reinterpret_cast<char*>(static_cast<S*>(a.fout) + ni);
-  float old0[3], old1[3];
+  // the previous residual step's fields of both nodes (n even: 8-byte words)
+  float2 o2[3];
   if (RES) {
-    load_old<float>(a, n, old0);
-    load_old<float>(a, n + 1, old1);
+    o2[0] = *reinterpret_cast<const float2*>(static_cast<const float*>(a.rho_old) + n);
+    o2[1] = *reinterpret_cast<const float2*>(static_cast<const float*>(a.ux_old) + n);
+    o2[2] = *reinterpret_cast<const float2*>(static_cast<const float*>(a.uy_old) + n);
   }
   W w[9];
   w[0] = pair_pull<S, 0>(fb, a.off_pull[0]);
@@ -1001,16 +1034,16 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, floa
   node_update<S, COLL, FORC>(f1, a, n + 1, rho1, ux1, uy1, seg);
 #pragma unroll
   for (int k = 0; k < 9; ++k) *reinterpret_cast<W*>(ob + a.off_plane[k]) = IO::pack(f0[k], f1[k]);
-  node_outputs<float, RES ? RES_ON : RES_OFF>(a, n, -1, rho0, ux0, uy0, red, old0);
-  node_outputs<float, RES ? RES_ON : RES_OFF>(a, n + 1, -1, rho1, ux1, uy1, red, old1);
+  pair_outputs<RES>(a, n, rho0, ux0, uy0, rho1, ux1, uy1, red, o2);
 }
 
 // CAP = 1 asks for 6 resident blocks of 256 threads (at most 40 registers),
-// CAP = 2 for 4 (at most 64).  RES: the residual instantiation.  (Two rows per
+// CAP = 2 for 4 (at most 64), CAP = 3 for 7 (32, with a few spills).  RES: the
+// residual instantiation.  (Two rows per
 // thread, one after the other, ran no faster: 131.8 against 131.5 GLUPS in
 // FP16, 87.6 against 91.0 in FP32.)
 template <class S, int COLL, int FORC, int CAP, bool RES>
-__global__ void __launch_bounds__(256, CAP == 1 ? 6 : (CAP == 2 ? 4 : 1))
+__global__ void __launch_bounds__(256, CAP == 1 ? 6 : (CAP == 2 ? 4 : (CAP == 3 ? 7 : 1)))
     step_pair_kernel(const StepArgs a) {
   const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
   float red[7] = {0, 0, 0, 0, 0, 0, 0};

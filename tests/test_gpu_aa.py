@@ -98,7 +98,12 @@ def test_aa_graph_replay_and_restart():
 
 @pytest.mark.parametrize("storage", ["fp32_shifted", "fp16_shifted"])
 @pytest.mark.parametrize("coll", ["BGK", "MRT"])
-def test_aa_shifted_storage_matches_two_buffers(storage, coll):
+def test_aa_shifted_storage_matches_two_buffers(storage, coll, monkeypatch):
+    """Both layouts on the node-pair kernel (the AA default for shifted
+    storage): kernels that contract the collision's arithmetic differently
+    round FP16 storage differently, and over 501 steps of this unsteady flow
+    such differences grow to the size of FP16's own error (1e-3)."""
+    monkeypatch.setenv("LBM_VARIANT", "3,2,128,1")
     case = Case(workloads.cylinder(nx=512, ny=128, radius=16.0, center=(128, 67), model=coll))
     out = {}
     for layout in ("ab", "aa"):

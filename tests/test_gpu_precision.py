@@ -64,7 +64,7 @@ def test_shifted_storage_error_vs_fp64(name):
 _COMMON = [(2, 0, 256, 4), (2, 0, 512, 3), (2, 0, 256, 2)]
 _SCALAR = [(0, 1, 128, 0), (0, 1, 256, 0), (0, 1, 128, 1), (0, 1, 256, 1), (0, 1, 128, 2),
            (0, 1, 256, 2)]
-_PAIRS = [(3, 2, 128, 0), (3, 2, 256, 0), (3, 2, 128, 1), (3, 2, 256, 2)]
+_PAIRS = [(3, 2, 128, 0), (3, 2, 256, 0), (3, 2, 128, 1), (3, 2, 256, 2), (3, 2, 128, 3)]
 SHIFTED_VARIANTS = {
     "fp32_shifted": _COMMON + [(1, 4, 256, 0), (1, 2, 256, 0)] + _SCALAR + _PAIRS,
     "fp16_shifted": _COMMON + [(1, 8, 256, 0), (1, 4, 256, 0)] + _SCALAR + _PAIRS,

@@ -18,7 +18,12 @@ pytestmark = pytest.mark.gpu
 
 RES_RTOL = 1e-12
 FORCE_RTOL = 1e-12
-AB_TOL = {"fp32_shifted": 1e-6, "fp16_shifted": 1e-4}   # max |u_aa - u_ab| / max |u_ab|
+# max |u_aa - u_ab| / max |u_ab|.  Kernels may contract the collision's FP32
+# arithmetic into FMAs differently; in FP16 storage an occasional flipped
+# rounding of a stored half then follows, and over 501 steps these add up to
+# about FP16's own error against FP64 (8e-4 here), so FP16 is bounded at
+# 2e-3: a layout error would be of order 1.
+AB_TOL = {"fp32_shifted": 1e-6, "fp16_shifted": 2e-3}
 
 
 def _inner_mask(nx, ny, solid_padded):
@@ -100,9 +105,7 @@ def test_aa_graph_replay_and_restart():
 @pytest.mark.parametrize("coll", ["BGK", "MRT"])
 def test_aa_shifted_storage_matches_two_buffers(storage, coll, monkeypatch):
     """Both layouts on the node-pair kernel (the AA default for shifted
-    storage): kernels that contract the collision's arithmetic differently
-    round FP16 storage differently, and over 501 steps of this unsteady flow
-    such differences grow to the size of FP16's own error (1e-3)."""
+    storage), 501 steps."""
     monkeypatch.setenv("LBM_VARIANT", "3,2,128,1")
     case = Case(workloads.cylinder(nx=512, ny=128, radius=16.0, center=(128, 67), model=coll))
     out = {}

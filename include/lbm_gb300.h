@@ -256,16 +256,22 @@ int lbm_forces(LbmHandle* h, double* out);
  * LBM_ERR_STATE and leaves the obstacle where it was. */
 typedef struct {
   double center[2];        /* position, lattice units                        */
-  double radius;
+  double radius;           /* circle radius; for an ellipse its semi-major
+                              axis (the radius of the box it moves in)      */
   double velocity[2];      /* linear velocity                                */
   double omega;            /* angular velocity                               */
-  double angle;            /* inclination                                    */
-  double mass, inertia;    /* pi r^2 rho_s and m r^2 / 2 (obstacle.py)       */
+  double angle;            /* inclination (radians); an ellipse's major axis
+                              lies at this angle to x and turns with it     */
+  double mass, inertia;    /* pi r^2 rho_s and m r^2 / 2 (pi a b rho_s and
+                              m (a^2 + b^2) / 4 for an ellipse, obstacle.py) */
   double density;          /* rho_s: the density reported on its nodes       */
   double force[2], torque; /* momentum exchange of the last step (output)    */
   int32_t id;              /* obstacle id: reference order in obstacle_dict  */
   int32_t calculated;      /* 1: velocities follow the force and torque      */
   int32_t rotation, translation;  /* degrees of freedom                      */
+  double semi_axes[2];     /* ellipse: semi-major a, semi-minor b            */
+  int32_t shape;           /* 0 circle, 1 ellipse                            */
+  int32_t reserved;
 } LbmMovingObstacle;
 
 /* Registers the moving obstacles (at most 32) and the gravity of their

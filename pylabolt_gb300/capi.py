@@ -54,7 +54,9 @@ class LbmMovingObstacle(ctypes.Structure):
                 ("inertia", ctypes.c_double), ("density", ctypes.c_double),
                 ("force", ctypes.c_double * 2), ("torque", ctypes.c_double),
                 ("id", ctypes.c_int32), ("calculated", ctypes.c_int32),
-                ("rotation", ctypes.c_int32), ("translation", ctypes.c_int32)]
+                ("rotation", ctypes.c_int32), ("translation", ctypes.c_int32),
+                ("semi_axes", ctypes.c_double * 2), ("shape", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class LbmPopView(ctypes.Structure):

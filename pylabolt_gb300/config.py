@@ -442,12 +442,8 @@ class Case:
                 obs.translation_allowed = sm["degree_of_freedom"] in ("translation", "both")
             self.obstacles.append(obs)
             moving = (not obs.static) and bool(opts.get("move_obstacles", False))
-            if moving and obs.type != "circle":
-                raise ValueError("move_obstacles: only circles move on the device; obstacle " +
-                                 name + " is an ellipse (make it static, or leave "
-                                 "move_obstacles unset to keep it in place as a moving wall)")
             if obs.type == "ellipse":
-                self._rasterise_ellipse(obs)
+                self._rasterise_ellipse(obs, solid=not moving)
             else:
                 self._rasterise_circle(obs, solid=not moving)
         if any(not o.static for o in self.obstacles) and not self.compute_force_torque:
@@ -518,11 +514,12 @@ class Case:
         self.velocity[inside, 1] = lin[1] + ang * rxm[inside]
         self.density[inside] = obs.density
 
-    def _rasterise_ellipse(self, obs):
+    def _rasterise_ellipse(self, obs, solid=True):
         """(x'/a)^2 + (y'/b)^2 <= 1 in the frame turned by the inclination,
         with the periodic minimum image (is_ellipse / construct_ellipse,
         pylabolt/parallel/cpu/obstacle_kernels.py:151-241, same operation
-        order); solid nodes take the body velocity and density."""
+        order); solid nodes take the body velocity and density.  solid=False
+        (a moving obstacle) sets only the fields: the device places it."""
         a, b = (np.float64(v) for v in obs.semi_axes)
         alpha = np.float64(obs.inclination) * np.pi / 180
         cos_a, sin_a = np.cos(alpha), np.sin(alpha)
@@ -530,7 +527,7 @@ class Case:
         xp = rxm * cos_a + rym * sin_a
         yp = -rxm * sin_a + rym * cos_a
         inside = (xp * xp) / (a * a) + (yp * yp) / (b * b) <= 1
-        self._mark_solid(obs, inside, rxm, rym)
+        self._mark_solid(obs, inside, rxm, rym, solid)
 
     def _rasterise_circle(self, obs, solid=True):
         """dist^2 <= r^2 with the periodic minimum image (obstacle_kernels.py:11-93);

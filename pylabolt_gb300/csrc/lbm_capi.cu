@@ -1630,6 +1630,14 @@ int lbm_set_moving_obstacles(LbmHandle* h, const LbmMovingObstacle* obs, int n,
     lbm::MovObs& m = M.init[j];
     if (!(o.radius > 0.0) || !std::isfinite(o.center[0]) || !std::isfinite(o.center[1]))
       return fail(LBM_ERR_ARG, "lbm_set_moving_obstacles: obstacle " + std::to_string(j) + ": bad radius or centre");
+    if (o.shape != 0 && o.shape != 1)
+      return fail(LBM_ERR_ARG, "lbm_set_moving_obstacles: obstacle " + std::to_string(j) +
+                                   ": shape must be 0 (circle) or 1 (ellipse)");
+    if (o.shape == 1 && !(o.semi_axes[0] > 0.0 && o.semi_axes[1] > 0.0 &&
+                          o.radius >= o.semi_axes[0] && o.radius >= o.semi_axes[1] &&
+                          std::isfinite(o.angle)))
+      return fail(LBM_ERR_ARG, "lbm_set_moving_obstacles: obstacle " + std::to_string(j) +
+                                   ": an ellipse needs semi-axes > 0, radius >= both and a finite angle");
     if (o.calculated && ((o.translation && !(o.mass > 0.0)) || (o.rotation && !(o.inertia > 0.0))))
       return fail(LBM_ERR_ARG, "lbm_set_moving_obstacles: obstacle " + std::to_string(j) + ": mass and inertia must be > 0");
     m.cx = o.center[0];
@@ -1647,6 +1655,9 @@ int lbm_set_moving_obstacles(LbmHandle* h, const LbmMovingObstacle* obs, int n,
     m.calculated = o.calculated;
     m.rotation = o.rotation;
     m.translation = o.translation;
+    m.shape = o.shape;
+    m.sa = o.shape == 1 ? o.semi_axes[0] : 0.0;
+    m.sb = o.shape == 1 ? o.semi_axes[1] : 0.0;
     // the initial box with its border must lie in [1, nx-2] x [1, ny-2] and
     // in static bulk fluid
     const int bx0 = (int)std::floor(m.cx - m.r) - 1, bx1 = (int)std::ceil(m.cx + m.r) + 1;
@@ -1730,6 +1741,10 @@ int lbm_get_moving_obstacles(LbmHandle* h, LbmMovingObstacle* out) {
     o.calculated = m.calculated;
     o.rotation = m.rotation;
     o.translation = m.translation;
+    o.shape = m.shape;
+    o.semi_axes[0] = m.sa;
+    o.semi_axes[1] = m.sb;
+    o.reserved = 0;
   }
   return LBM_OK;
 }
@@ -1827,7 +1842,7 @@ struct StateHeader {
   int32_t tuned, res_tuned;
   int32_t variant[4], res_variant[4];   // kind, vec, block, stages
 };
-constexpr int32_t kStateVersion = 3;
+constexpr int32_t kStateVersion = 4;
 
 // Moving-obstacle part of the state: obstacles, node classes and segment
 // flags (they follow the obstacles), solid / refill flags, solid velocity and

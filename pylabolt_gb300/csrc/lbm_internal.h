@@ -163,7 +163,10 @@ __host__ __device__ inline long long aa_post_index(long long plane, int pitch, i
 // A moving obstacle on the device (FP64 state, see lbm_set_moving_obstacles).
 struct MovObs {
   double cx, cy, r, vx, vy, om, angle, mass, inertia, density, fx, fy, tq;
+  double sa, sb;            // ellipse semi-axes (shape 1)
+  double cth, sth;          // cos, sin of `angle` (ellipse orientation), set by the motion
   int id, calculated, rotation, translation;
+  int shape;                // 0 circle, 1 ellipse
   int bx0, by0, bx1, by1;   // nodes the last move may have changed (inclusive)
 };
 

@@ -9,8 +9,10 @@
 //                        nodes the move may change;
 //   mov_raster_kernel    solid flag, wall velocity v + omega x r and the
 //                        reported density / velocity of covered nodes
-//                        (construct_circle, obstacle_kernels.py:43-93); nodes
-//                        left behind are marked fresh;
+//                        (construct_circle, obstacle_kernels.py:43-93, or
+//                        construct_ellipse :192-241 with the inclination the
+//                        rotation has reached); nodes left behind are marked
+//                        fresh;
 //   mov_classify_kernel  node classes around the obstacle (2 solid, 4 fluid
 //                        next to a moving solid, 0 bulk) and the refill of
 //                        fresh nodes with f_eq(mean density of their fluid
@@ -126,6 +128,10 @@ __global__ void mov_motion_kernel(const MovArgs a) {
   }
   m.cx = ncx;
   m.cy = ncy;
+  if (m.shape == 1) {   // orientation of the ellipse for this step's raster
+    m.cth = cos(m.angle);
+    m.sth = sin(m.angle);
+  }
   m.bx0 = bx0;
   m.bx1 = bx1;
   m.by0 = by0;
@@ -145,7 +151,15 @@ __global__ void mov_raster_kernel(const MovArgs a) {
   const long long n = g.node(x, y);
   const double rx = (double)x - o.cx, ry = (double)y - o.cy;
   const uint8_t me = (uint8_t)(a.j + 1);
-  if (rx * rx + ry * ry <= o.r * o.r) {
+  bool inside;
+  if (o.shape == 1) {   // is_ellipse's test in the turned frame (obstacle_kernels.py:151-189)
+    const double xp = rx * o.cth + ry * o.sth;
+    const double yp = -rx * o.sth + ry * o.cth;
+    inside = (xp * xp) / (o.sa * o.sa) + (yp * yp) / (o.sb * o.sb) <= 1.0;
+  } else {
+    inside = rx * rx + ry * ry <= o.r * o.r;
+  }
+  if (inside) {
     a.dsolid[n] = me;
     const double ux = o.vx - o.om * ry, uy = o.vy + o.om * rx;
     T* us = static_cast<T*>(a.us);

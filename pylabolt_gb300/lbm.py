@@ -78,10 +78,17 @@ class FluidLBM:
             arr = (capi.LbmMovingObstacle * len(case.moving))()
             for a, o in zip(arr, case.moving):
                 a.center[:] = [float(o.center[0]), float(o.center[1])]
-                a.radius = float(o.radius)
+                if o.type == "ellipse":
+                    a.shape = 1
+                    a.semi_axes[:] = [float(o.semi_axes[0]), float(o.semi_axes[1])]
+                    a.radius = max(a.semi_axes[0], a.semi_axes[1])
+                else:
+                    a.radius = float(o.radius)
                 a.velocity[:] = [float(o.linear_velocity[0]), float(o.linear_velocity[1])]
                 a.omega = float(o.angular_velocity)
-                a.angle = 0.0
+                # an ellipse starts at its inclination (degrees in obstacle_dict)
+                a.angle = (float(np.float64(o.inclination) * np.pi / 180)
+                           if o.type == "ellipse" else 0.0)
                 a.mass = float(o.mass)
                 a.inertia = float(o.moment_of_inertia)
                 a.density = float(o.density)

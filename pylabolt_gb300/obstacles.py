@@ -59,15 +59,17 @@ def _min_image(r, n, periodic):
 
 class Geometry:
     """Padded geometry fields of a Case ([nx+2, ny+2] arrays, x-major).
-    `solid`, `solid_id` [nx, ny] and `centers` {obstacle id: (x, y)} replace
-    the case's set-up geometry (moving obstacles: the device's node flags and
-    positions at the time of output)."""
+    `solid`, `solid_id` [nx, ny], `centers` {obstacle id: (x, y)} and
+    `angles` {obstacle id: radians} replace the case's set-up geometry
+    (moving obstacles: the device's node flags, positions and ellipse
+    orientations at the time of output)."""
 
-    def __init__(self, case, solid=None, solid_id=None, centers=None):
+    def __init__(self, case, solid=None, solid_id=None, centers=None, angles=None):
         nx, ny = case.nx, case.ny
         self.nx, self.ny = nx, ny
         self.x_periodic, self.y_periodic = case.x_periodic, case.y_periodic
         centers = centers or {}
+        angles = angles or {}   # {obstacle id: inclination in radians} of moving ellipses
         solid_a = np.zeros((nx + 2, ny + 2), dtype=bool)
         solid_id_a = np.full((nx + 2, ny + 2), -1, dtype=np.int64)
         solid_a[1:-1, 1:-1] = case.solid if solid is None else solid
@@ -103,7 +105,7 @@ class Geometry:
             ry = _min_image(Y - cy, ny, self.y_periodic)
             if obs.type == "ellipse":
                 a, b = (np.float64(v) for v in obs.semi_axes)
-                alpha = np.float64(obs.inclination) * np.pi / 180
+                alpha = angles.get(obs.id, np.float64(obs.inclination) * np.pi / 180)
                 cos_a, sin_a = np.cos(alpha), np.sin(alpha)
                 xp = rx * cos_a + ry * sin_a
                 yp = -rx * sin_a + ry * cos_a

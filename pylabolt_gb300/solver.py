@@ -128,8 +128,10 @@ class Solver:
         solid_id = np.where(flags == 1, c.solid_id, -1)
         for j, o in enumerate(c.moving):
             solid_id[flags == 2 + j] = o.id
-        centers = {st["id"]: st["center"] for st in self.lbm.moving_obstacles()}
-        return Geometry(c, solid=solid, solid_id=solid_id, centers=centers)
+        states = self.lbm.moving_obstacles()
+        centers = {st["id"]: st["center"] for st in states}
+        angles = {st["id"]: st["angle"] for st in states}
+        return Geometry(c, solid=solid, solid_id=solid_id, centers=centers, angles=angles)
 
     def run(self):
         c = self.case

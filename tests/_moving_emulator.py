@@ -39,10 +39,16 @@ class MovingEmulator(FusedEmulator):
         self.cls = self.cls_static.copy()
         self.obs = []
         for o in c.moving:
+            ell = o.type == "ellipse"
             self.obs.append({"cx": float(o.center[0]), "cy": float(o.center[1]),
-                             "r": float(o.radius), "vx": float(o.linear_velocity[0]),
+                             "r": max(o.semi_axes) if ell else float(o.radius),
+                             "shape": 1 if ell else 0,
+                             "sa": float(o.semi_axes[0]) if ell else 0.0,
+                             "sb": float(o.semi_axes[1]) if ell else 0.0,
+                             "vx": float(o.linear_velocity[0]),
                              "vy": float(o.linear_velocity[1]), "om": float(o.angular_velocity),
-                             "angle": 0.0, "mass": float(o.mass),
+                             "angle": float(np.float64(o.inclination) * np.pi / 180) if ell else 0.0,
+                             "mass": float(o.mass),
                              "inertia": float(o.moment_of_inertia), "density": float(o.density),
                              "fx": 0.0, "fy": 0.0, "tq": 0.0, "calculated": o.calculated,
                              "rotation": o.rotation_allowed, "translation": o.translation_allowed})
@@ -79,6 +85,8 @@ class MovingEmulator(FusedEmulator):
         nx, ny = self.case.nx, self.case.ny
         assert box[0] >= 2 and box[2] >= 2 and box[1] <= nx - 3 and box[3] <= ny - 3
         m["cx"], m["cy"], m["box"] = ncx, ncy, box
+        if m["shape"] == 1:
+            m["cth"], m["sth"] = math.cos(m["angle"]), math.sin(m["angle"])
         return m
 
     def _geometry(self, motion):
@@ -90,7 +98,13 @@ class MovingEmulator(FusedEmulator):
                 for y in range(y0, y1 + 1):
                     n = self._node(x, y)
                     rx, ry = float(x) - o["cx"], float(y) - o["cy"]
-                    if rx * rx + ry * ry <= o["r"] * o["r"]:
+                    if o["shape"] == 1:
+                        xp = rx * o["cth"] + ry * o["sth"]
+                        yp = -rx * o["sth"] + ry * o["cth"]
+                        inside = (xp * xp) / (o["sa"] * o["sa"]) + (yp * yp) / (o["sb"] * o["sb"]) <= 1.0
+                    else:
+                        inside = rx * rx + ry * ry <= o["r"] * o["r"]
+                    if inside:
                         self.dsolid[n] = me
                         ux, uy = o["vx"] - o["om"] * ry, o["vy"] + o["om"] * rx
                         self.us[n] = (ux, uy)

@@ -20,7 +20,7 @@ int main(void) {
   CHECK(sizeof(LbmConfig) == 120);
   CHECK(sizeof(LbmNodeLinks) == 240);
   CHECK(sizeof(LbmForceLink) == 32);
-  CHECK(sizeof(LbmMovingObstacle) == 120);
+  CHECK(sizeof(LbmMovingObstacle) == 144);
   CHECK(sizeof(LbmPopView) == 56);
 
   LbmConfig cfg;

@@ -10,7 +10,7 @@ from pylabolt_gb300 import capi
 from pylabolt_gb300.config import Case
 from pylabolt_gb300.lbm import FluidLBM
 from _moving_emulator import MovingEmulator
-from test_moving_cpu import disk_case
+from test_moving_cpu import disk_case, wing_case
 
 pytestmark = pytest.mark.gpu
 
@@ -46,6 +46,27 @@ def test_moving_disk_fp64_matches_restatement(kw):
     o, eo = obs[0], e.obs[0]
     assert o["center"][0] == eo["cx"] and o["center"][1] == eo["cy"]
     assert o["velocity"][0] == eo["vx"] and o["velocity"][1] == eo["vy"]
+    assert o["omega"] == eo["om"] and o["angle"] == eo["angle"]
+    assert o["force"][0] == eo["fx"] and o["force"][1] == eo["fy"] and o["torque"] == eo["tq"]
+    assert np.array_equal(flags.ravel() >= 2, e.dsolid > 0)
+    assert np.array_equal(rho.ravel(), e.rho)
+    assert np.array_equal(u.reshape(-1, 2), e.u)
+
+
+@pytest.mark.parametrize("kw", [
+    {"v": (0.04, -0.02), "om": 0.015},                     # prescribed translation + rotation
+    {"v": (0.0, 0.0), "om": 0.0, "kind": "calculated", "density": 1.2},   # force-driven
+])
+def test_moving_ellipse_fp64_matches_restatement(kw):
+    """An inclined ellipse that translates and turns: the device raster in the
+    frame of the angle the motion has reached, FP64 bit for bit against the
+    restatement (positions, angle, forces, node flags, fields)."""
+    case = Case(wing_case(True, **kw))
+    steps = 120
+    rho, u, obs, flags = _gpu(case, steps)
+    e = _emu(case, steps)
+    o, eo = obs[0], e.obs[0]
+    assert o["center"][0] == eo["cx"] and o["center"][1] == eo["cy"]
     assert o["omega"] == eo["om"] and o["angle"] == eo["angle"]
     assert o["force"][0] == eo["fx"] and o["force"][1] == eo["fy"] and o["torque"] == eo["tq"]
     assert np.array_equal(flags.ravel() >= 2, e.dsolid > 0)

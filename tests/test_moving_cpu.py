@@ -28,6 +28,50 @@ def disk_case(moving, v=(0.0, 0.0), om=0.0, kind="fixed_velocity", dof="both", n
     return c
 
 
+def wing_case(moving, v=(0.0, 0.0), om=0.0, kind="fixed_velocity", dof="both", axes=(6.0, 2.5),
+              incl=30.0, density=1.0, nx=48, ny=40, center=(18, 20)):
+    """The disk case with an inclined ellipse in place of the disk."""
+    c = disk_case(moving, v=v, om=om, kind=kind, dof=dof, nx=nx, ny=ny, center=center,
+                  density=density)
+    d = c["obstacle_dict"].pop("disk")
+    del d["radius"]
+    d.update({"type": "ellipse", "semi_major_axis": axes[0], "semi_minor_axis": axes[1],
+              "inclination_angle": incl})
+    c["obstacle_dict"]["wing"] = d
+    return c
+
+
+def test_resting_moving_ellipse_equals_static_ellipse():
+    """An ellipse that does not move: the device-placed raster and its run-time
+    links reproduce the static rasteriser and link records bit for bit."""
+    st = FusedEmulator(Case(wing_case(False)))
+    mv = MovingEmulator(Case(wing_case(True)))
+    st.initialize()
+    mv.initialize()
+    assert np.array_equal(mv.dsolid > 0, st.solid)
+    for _ in range(40):
+        st.step()
+        mv.step()
+    fl = ~st.solid
+    assert np.array_equal(st.fstar[fl], mv.fstar[fl])
+    assert np.array_equal(st.rho[fl], mv.rho[fl])
+
+
+def test_rotating_ellipse_geometry():
+    """A spinning ellipse: after t steps at omega its solid set is the static
+    raster at inclination alpha + omega t."""
+    om = 0.02
+    mv = MovingEmulator(Case(wing_case(True, om=om, dof="rotation")))
+    mv.initialize()
+    for _ in range(25):
+        mv.step()
+    o = mv.obs[0]
+    assert o["angle"] == pytest.approx(np.pi / 6 + 25 * om)
+    turned = Case(wing_case(False, incl=float(np.degrees(o["angle"]))))
+    assert abs(int((mv.dsolid > 0).sum()) - int(turned.solid.sum())) <= 4
+    assert (mv.dsolid.reshape(turned.solid.shape) > 0)[turned.solid].mean() > 0.95
+
+
 def test_resting_moving_disk_equals_static_disk():
     """A moving obstacle that does not move: the run-time links reproduce the
     static link records bit for bit."""
@@ -79,6 +123,15 @@ def test_motion_dict_validation_messages():
     c["obstacle_dict"]["options"]["move_obstacles"] = "yes"
     with pytest.raises(ValueError, match="move_obstacles must be bool"):
         Case(c)
+
+
+def test_moving_ellipse_parameters():
+    case = Case(wing_case(True, kind="calculated", dof="both", density=2.0))
+    o = case.moving[0]
+    assert o.type == "ellipse" and o.semi_axes == (6.0, 2.5)
+    assert o.mass == pytest.approx(np.pi * 6.0 * 2.5 * 2.0)
+    assert o.moment_of_inertia == pytest.approx(o.mass * (36.0 + 6.25) / 4)
+    assert not case.solid.any()
 
 
 def test_moving_obstacle_parameters():

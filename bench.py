@@ -282,12 +282,16 @@ def run_gb300(args, world, rank, local):
 
     # ---- end to end through the Python API, pinned host buffers -----------
     e2e_steps = args.steps                          # the same K steps as the device-timed leg
-    rho_h = torch.empty(case.density.shape, dtype=torch.float64, pin_memory=True).numpy()
-    u_h = torch.empty(case.velocity.shape, dtype=torch.float64, pin_memory=True).numpy()
+    # host fields as the reference's case holds them: float64 for precision
+    # "double" (FP64 storage), float32 for precision "single" (the FP32 and
+    # FP16 storage cases; pylabolt/base/fields.py:64-77)
+    host_dt = torch.float64 if args.storage == "fp64" else torch.float32
+    rho_h = torch.empty(case.density.shape, dtype=host_dt, pin_memory=True).numpy()
+    u_h = torch.empty(case.velocity.shape, dtype=host_dt, pin_memory=True).numpy()
     rho_h[...] = case.density
     u_h[...] = case.velocity
-    rho_out = torch.empty(case.density.shape, dtype=torch.float64, pin_memory=True).numpy()
-    u_out = torch.empty(case.velocity.shape, dtype=torch.float64, pin_memory=True).numpy()
+    rho_out = torch.empty(case.density.shape, dtype=host_dt, pin_memory=True).numpy()
+    u_out = torch.empty(case.velocity.shape, dtype=host_dt, pin_memory=True).numpy()
     def end_to_end(nsteps):
         barrier()
         t0 = time.perf_counter()
@@ -307,8 +311,10 @@ def run_gb300(args, world, rank, local):
            "steps": e2e_steps, "ms": t_e2e * 1e3,
            "host_link_gbs": link,
            "transfer_floor_ms": io_bytes / link["h2d"] / 1e6 + io_bytes / link["d2h"] / 1e6,
+           "host_fields": str(rho_h.dtype),
            "what": "FluidLBM.initialize(host rho,u) + per step lbm_step_ex(RESIDUAL) + "
-                   "lbm_residual readback + final lbm_get_moments readback"}
+                   "lbm_residual readback + final moments readback "
+                   f"({'lbm_init_fields/lbm_get_moments' if args.storage == 'fp64' else 'lbm_init_fields_f32/lbm_get_moments_f32'})"}
     if e2e_steps != 200 and not args.no_extra:
         t200 = end_to_end(200)
         e2e["at_200_steps"] = {"value": whole_job_mlups(world, nodes, 200, t200), "ms": t200 * 1e3}

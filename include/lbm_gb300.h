@@ -136,6 +136,13 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
  * inner-layout arrays the same way.  The values are the same either way. */
 int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout);
 
+/* As lbm_init_fields with FP32 fields: a case with "precision": "single"
+ * holds state.fields.density/velocity as float32 (pylabolt/base/control.py:36-40,
+ * pylabolt/base/fields.py:64-77).  The values are widened exactly, so the
+ * state equals lbm_init_fields on the same values as doubles; half the bytes
+ * cross the host link. */
+int lbm_init_fields_f32(LbmHandle* h, const float* rho, const float* u, int layout);
+
 /* Sets a per-node body force field F[n][2] (inner layout) used instead of
  * rho*g when cfg.body_force_field == 1 (extension: no reference key). */
 int lbm_set_body_force(LbmHandle* h, const double* force);
@@ -164,6 +171,11 @@ int lbm_step_ex(LbmHandle* h, int64_t nsteps, int flags);
  * with InputOutputOperator.write_fields (pylabolt/utils/io_operator.py:158-190).
  * rho: [n], u: [n][2] in `layout`. */
 int lbm_get_moments(LbmHandle* h, double* rho, double* u, int layout);
+
+/* As lbm_get_moments into FP32 fields (single-precision cases), each value
+ * the FP64 result rounded to nearest; exact for FP32 and FP16 storage, whose
+ * moments are FP32 values. */
+int lbm_get_moments_f32(LbmHandle* h, float* rho, float* u, int layout);
 
 /* Residuals {res_rho, res_ux, res_uy} of the last LBM_STEP_RESIDUAL step:
  * sqrt(sum (phi-phi_old)^2 / (sum phi_old^2 + eps)) over fluid nodes, phi_old

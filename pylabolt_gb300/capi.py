@@ -82,8 +82,8 @@ assert FORCE_LINK_DTYPE.itemsize == 32
 _LIB = None
 
 # every symbol include/lbm_gb300.h declares
-EXPORTS = ["lbm_create", "lbm_init_fields", "lbm_set_body_force", "lbm_step",
-           "lbm_step_ex", "lbm_get_moments", "lbm_residual", "lbm_conservation",
+EXPORTS = ["lbm_create", "lbm_init_fields", "lbm_init_fields_f32", "lbm_set_body_force", "lbm_step",
+           "lbm_step_ex", "lbm_get_moments", "lbm_get_moments_f32", "lbm_residual", "lbm_conservation",
            "lbm_get_populations", "lbm_set_populations", "lbm_time",
            "lbm_kernel_launches", "lbm_kernel_variant", "lbm_tuning", "lbm_device_bytes", "lbm_time_steps",
            "lbm_synchronize", "lbm_last_error", "lbm_destroy", "lbm_conservation_noalloc",
@@ -112,10 +112,12 @@ def load(build=True):
     sig = {
         "lbm_create": [ctypes.POINTER(LbmConfig), P, P, i64, ctypes.POINTER(P)],
         "lbm_init_fields": [P, P, P, ctypes.c_int],
+        "lbm_init_fields_f32": [P, P, P, ctypes.c_int],
         "lbm_set_body_force": [P, P],
         "lbm_step": [P, i64],
         "lbm_step_ex": [P, i64, ctypes.c_int],
         "lbm_get_moments": [P, P, P, ctypes.c_int],
+        "lbm_get_moments_f32": [P, P, P, ctypes.c_int],
         "lbm_residual": [P, dbl],
         "lbm_conservation": [P, dbl],
         "lbm_get_populations": [P, P],

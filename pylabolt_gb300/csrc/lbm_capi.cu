@@ -1016,29 +1016,32 @@ int lbm_destroy(LbmHandle* h) {
   return LBM_OK;
 }
 
-int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout) {
-  if (!h || !rho || !u) return fail(LBM_ERR_ARG, "lbm_init_fields: null argument");
-  if (layout != LBM_LAYOUT_INNER && layout != LBM_LAYOUT_PADDED)
-    return fail(LBM_ERR_ARG, "lbm_init_fields: unknown layout");
-  LBM_CUDA(cudaSetDevice(h->cfg.device));
+extern "C++" {
+// Caller fields in host order (HT = double, or float for single-precision
+// cases) to the FP64 device-order stage *ds: rho [plane], u [2][plane].
+template <class HT>
+static int fields_to_stage(LbmHandle* h, const HT* rho, const HT* u, int layout, double** ds_out) {
   const long long nh = h->host_nodes(layout), plane = h->g.plane;
-  const double* rd = h->host_direct(rho);
-  const double* ud = h->host_direct(u);
+  const HT* rd = h->host_direct(rho);
+  const HT* ud = h->host_direct(u);
   const bool direct = rd && ud;
-  int rc = h->ensure_stage(direct ? 3 * plane : 3 * nh + 3 * plane);
+  // host-order part of the stage, in doubles (none when read in place)
+  const long long hn = direct ? 0 : (3 * nh * (long long)sizeof(HT) + 7) / 8;
+  int rc = h->ensure_stage(hn + 3 * plane);
   if (rc) return rc;
   h->initialized = false;   // until the new state is complete
-  double* ds = h->stage + (direct ? 0 : 3 * nh);   // device order: rho [plane], u [2][plane]
+  double* ds = h->stage + hn;   // device order: rho [plane], u [2][plane]
+  HT* hs = reinterpret_cast<HT*>(h->stage);   // host order: rho [nh], u [nh][2]
+  const int nx = h->cfg.nx;
   LBM_CUDA(cudaMemsetAsync(ds, 0, 3 * plane * sizeof(double), h->stream));
   if (direct) {   // transposed straight from the caller's pinned buffers
-    LBM_CUDA(lbm::reorder(h->g, rd, ds, 1, layout, 1, h->stream));
-    LBM_CUDA(lbm::reorder(h->g, ud, ds + plane, 2, layout, 1, h->stream));
+    LBM_CUDA(lbm::reorder_cols(h->g, rd, ds, 1, layout, 1, 0, nx, h->stream));
+    LBM_CUDA(lbm::reorder_cols(h->g, ud, ds + plane, 2, layout, 1, 0, nx, h->stream));
   } else if (layout == LBM_LAYOUT_INNER) {
     // column chunks: chunk c is copied on the transfer stream while the
     // handle's stream transposes chunk c - 1 (host order is x-major, so the
     // columns x0 <= x < x1 are one contiguous run of each array)
     if ((rc = h->ensure_xfer())) return rc;
-    double* hs = h->stage;   // host order: rho [nh], u [nh][2]
     const long long ny = h->cfg.ny;
     constexpr int NC = LbmHandle::kXferChunks;
     LBM_CUDA(cudaEventRecord(h->xev[NC], h->stream));
@@ -1046,9 +1049,9 @@ int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout
     for (int c = 0; c < NC; ++c) {
       const int x0 = h->xfer_col(c), x1 = h->xfer_col(c + 1);
       if (x0 >= x1) continue;
-      LBM_CUDA(cudaMemcpyAsync(hs + x0 * ny, rho + x0 * ny, (x1 - x0) * ny * sizeof(double),
+      LBM_CUDA(cudaMemcpyAsync(hs + x0 * ny, rho + x0 * ny, (x1 - x0) * ny * sizeof(HT),
                                cudaMemcpyDefault, h->xfer));
-      LBM_CUDA(cudaMemcpyAsync(hs + nh + 2 * x0 * ny, u + 2 * x0 * ny, 2 * (x1 - x0) * ny * sizeof(double),
+      LBM_CUDA(cudaMemcpyAsync(hs + nh + 2 * x0 * ny, u + 2 * x0 * ny, 2 * (x1 - x0) * ny * sizeof(HT),
                                cudaMemcpyDefault, h->xfer));
       LBM_CUDA(cudaEventRecord(h->xev[c], h->xfer));
       LBM_CUDA(cudaStreamWaitEvent(h->stream, h->xev[c], 0));
@@ -1056,12 +1059,45 @@ int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout
       LBM_CUDA(lbm::reorder_cols(h->g, hs + nh, ds + plane, 2, layout, 1, x0, x1, h->stream));
     }
   } else {
-    double* hs = h->stage;   // host order: rho [nh], u [nh][2]
-    LBM_CUDA(cudaMemcpyAsync(hs, rho, nh * sizeof(double), cudaMemcpyDefault, h->stream));
-    LBM_CUDA(cudaMemcpyAsync(hs + nh, u, 2 * nh * sizeof(double), cudaMemcpyDefault, h->stream));
-    LBM_CUDA(lbm::reorder(h->g, hs, ds, 1, layout, 1, h->stream));
-    LBM_CUDA(lbm::reorder(h->g, hs + nh, ds + plane, 2, layout, 1, h->stream));
+    LBM_CUDA(cudaMemcpyAsync(hs, rho, nh * sizeof(HT), cudaMemcpyDefault, h->stream));
+    LBM_CUDA(cudaMemcpyAsync(hs + nh, u, 2 * nh * sizeof(HT), cudaMemcpyDefault, h->stream));
+    LBM_CUDA(lbm::reorder_cols(h->g, hs, ds, 1, layout, 1, 0, nx, h->stream));
+    LBM_CUDA(lbm::reorder_cols(h->g, hs + nh, ds + plane, 2, layout, 1, 0, nx, h->stream));
   }
+  *ds_out = ds;
+  return LBM_OK;
+}
+
+}  // extern "C++"
+
+static int init_from_stage(LbmHandle* h, double* ds);
+
+extern "C++" {
+template <class HT>
+static int init_fields(LbmHandle* h, const HT* rho, const HT* u, int layout, const char* name) {
+  if (!h || !rho || !u) return fail(LBM_ERR_ARG, std::string(name) + ": null argument");
+  if (layout != LBM_LAYOUT_INNER && layout != LBM_LAYOUT_PADDED)
+    return fail(LBM_ERR_ARG, std::string(name) + ": unknown layout");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  double* ds = nullptr;
+  int rc = fields_to_stage(h, rho, u, layout, &ds);
+  return rc ? rc : init_from_stage(h, ds);
+}
+
+}  // extern "C++"
+
+int lbm_init_fields(LbmHandle* h, const double* rho, const double* u, int layout) {
+  return init_fields(h, rho, u, layout, "lbm_init_fields");
+}
+
+int lbm_init_fields_f32(LbmHandle* h, const float* rho, const float* u, int layout) {
+  return init_fields(h, rho, u, layout, "lbm_init_fields_f32");
+}
+
+// Equilibrium populations from the staged fields, then the step state reset.
+static int init_from_stage(LbmHandle* h, double* ds) {
+  const long long plane = h->g.plane;
+  int rc;
   if (h->mov.n) {   // static classes back before f_eq is written (a run may have moved obstacles)
     LBM_CUDA(cudaMemcpyAsync(const_cast<uint8_t*>(h->g.cls), h->mov.cls_static, plane,
                              cudaMemcpyDeviceToDevice, h->stream));
@@ -1404,28 +1440,35 @@ int lbm_adjoint_backward(LbmHandle* h, const double* grad_u, double* grad_force,
   return LBM_OK;
 }
 
-int lbm_get_moments(LbmHandle* h, double* rho, double* u, int layout) {
-  if (!h || !rho || !u) return fail(LBM_ERR_ARG, "lbm_get_moments: null argument");
+extern "C++" {
+// Moments of the last recorded step into caller fields in host order
+// (HT = double, or float for single-precision cases, rounded to nearest).
+template <class HT>
+static int get_moments(LbmHandle* h, HT* rho, HT* u, int layout, const char* name) {
+  if (!h || !rho || !u) return fail(LBM_ERR_ARG, std::string(name) + ": null argument");
   if (layout != LBM_LAYOUT_INNER && layout != LBM_LAYOUT_PADDED)
-    return fail(LBM_ERR_ARG, "lbm_get_moments: unknown layout");
-  if (!h->has_moments) return fail(LBM_ERR_STATE, "lbm_get_moments: no moments recorded (use LBM_STEP_MOMENTS)");
+    return fail(LBM_ERR_ARG, std::string(name) + ": unknown layout");
+  if (!h->has_moments)
+    return fail(LBM_ERR_STATE, std::string(name) + ": no moments recorded (use LBM_STEP_MOMENTS)");
   LBM_CUDA(cudaSetDevice(h->cfg.device));
   const long long nh = h->host_nodes(layout), plane = h->g.plane;
-  double* rd = layout == LBM_LAYOUT_INNER ? h->host_direct(rho) : nullptr;
-  double* ud = layout == LBM_LAYOUT_INNER ? h->host_direct(u) : nullptr;
+  const int nx = h->cfg.nx;
+  HT* rd = layout == LBM_LAYOUT_INNER ? h->host_direct(rho) : nullptr;
+  HT* ud = layout == LBM_LAYOUT_INNER ? h->host_direct(u) : nullptr;
   if (rd && ud) {   // transposed straight into the caller's pinned buffers
     int rc = h->ensure_stage(3 * plane);
     if (rc) return rc;
     double* ds = h->stage;
     LBM_CUDA(h->ks->moments_to_f64(h->g, h->mom[0], h->mom[1], h->mom[2], ds, h->stream));
-    LBM_CUDA(lbm::reorder(h->g, ds, rd, 1, layout, 0, h->stream));
-    LBM_CUDA(lbm::reorder(h->g, ds + plane, ud, 2, layout, 0, h->stream));
+    LBM_CUDA(lbm::reorder_cols(h->g, ds, rd, 1, layout, 0, 0, nx, h->stream));
+    LBM_CUDA(lbm::reorder_cols(h->g, ds + plane, ud, 2, layout, 0, 0, nx, h->stream));
     return h->wait();
   }
-  int rc = h->ensure_stage(3 * nh + 3 * plane);
+  const long long hn = (3 * nh * (long long)sizeof(HT) + 7) / 8;   // host-order part, in doubles
+  int rc = h->ensure_stage(hn + 3 * plane);
   if (rc) return rc;
-  double* hs = h->stage;
-  double* ds = h->stage + 3 * nh;
+  HT* hs = reinterpret_cast<HT*>(h->stage);
+  double* ds = h->stage + hn;
   LBM_CUDA(h->ks->moments_to_f64(h->g, h->mom[0], h->mom[1], h->mom[2], ds, h->stream));
   if (layout == LBM_LAYOUT_INNER) {
     // column chunks: chunk c goes to the host on the transfer stream while
@@ -1440,21 +1483,31 @@ int lbm_get_moments(LbmHandle* h, double* rho, double* u, int layout) {
       LBM_CUDA(lbm::reorder_cols(h->g, ds + plane, hs + nh, 2, layout, 0, x0, x1, h->stream));
       LBM_CUDA(cudaEventRecord(h->xev[c], h->stream));
       LBM_CUDA(cudaStreamWaitEvent(h->xfer, h->xev[c], 0));
-      LBM_CUDA(cudaMemcpyAsync(rho + x0 * ny, hs + x0 * ny, (x1 - x0) * ny * sizeof(double),
+      LBM_CUDA(cudaMemcpyAsync(rho + x0 * ny, hs + x0 * ny, (x1 - x0) * ny * sizeof(HT),
                                cudaMemcpyDefault, h->xfer));
-      LBM_CUDA(cudaMemcpyAsync(u + 2 * x0 * ny, hs + nh + 2 * x0 * ny, 2 * (x1 - x0) * ny * sizeof(double),
+      LBM_CUDA(cudaMemcpyAsync(u + 2 * x0 * ny, hs + nh + 2 * x0 * ny, 2 * (x1 - x0) * ny * sizeof(HT),
                                cudaMemcpyDefault, h->xfer));
     }
     LBM_CUDA(cudaEventRecord(h->xev[NC], h->xfer));
     LBM_CUDA(cudaStreamWaitEvent(h->stream, h->xev[NC], 0));
     return h->wait();
   }
-  LBM_CUDA(cudaMemsetAsync(hs, 0, 3 * nh * sizeof(double), h->stream));   // ghosts of the padded layout
-  LBM_CUDA(lbm::reorder(h->g, ds, hs, 1, layout, 0, h->stream));
-  LBM_CUDA(lbm::reorder(h->g, ds + plane, hs + nh, 2, layout, 0, h->stream));
-  LBM_CUDA(cudaMemcpyAsync(rho, hs, nh * sizeof(double), cudaMemcpyDefault, h->stream));
-  LBM_CUDA(cudaMemcpyAsync(u, hs + nh, 2 * nh * sizeof(double), cudaMemcpyDefault, h->stream));
+  LBM_CUDA(cudaMemsetAsync(hs, 0, 3 * nh * sizeof(HT), h->stream));   // ghosts of the padded layout
+  LBM_CUDA(lbm::reorder_cols(h->g, ds, hs, 1, layout, 0, 0, nx, h->stream));
+  LBM_CUDA(lbm::reorder_cols(h->g, ds + plane, hs + nh, 2, layout, 0, 0, nx, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(rho, hs, nh * sizeof(HT), cudaMemcpyDefault, h->stream));
+  LBM_CUDA(cudaMemcpyAsync(u, hs + nh, 2 * nh * sizeof(HT), cudaMemcpyDefault, h->stream));
   return h->wait();
+}
+
+}  // extern "C++"
+
+int lbm_get_moments(LbmHandle* h, double* rho, double* u, int layout) {
+  return get_moments(h, rho, u, layout, "lbm_get_moments");
+}
+
+int lbm_get_moments_f32(LbmHandle* h, float* rho, float* u, int layout) {
+  return get_moments(h, rho, u, layout, "lbm_get_moments_f32");
 }
 
 int lbm_residual(LbmHandle* h, double out[3]) {

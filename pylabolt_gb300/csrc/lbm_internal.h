@@ -283,13 +283,19 @@ inline dim3 step_grid(const Geom& g, Variant v, int sms, int elem_bytes) {
   const long long per_block = (long long)v.block * v.vec;
   return dim3((unsigned)((g.pitch + per_block - 1) / per_block), (unsigned)g.ny);
 }
-// Host-order <-> device-order copies of FP64 node data with `ncomp`
+// Host-order <-> device-order copies of node data with `ncomp`
 // components: host AoS [node][ncomp] in inner (ind = x*ny+y) or padded
 // (ind = (x+1)*(ny+2)+(y+1)) order; device SoA [ncomp][plane].
 cudaError_t reorder(const Geom& g, const double* in, double* out, int ncomp,
                     int layout, int to_device, cudaStream_t s);
-// The same for the columns x_lo <= x < x_hi only.
+// The same for the columns x_lo <= x < x_hi only; the FP32 forms take FP32
+// host-order data (widened exactly on the way in, rounded to nearest on the
+// way out) for the single-precision field entry points.
 cudaError_t reorder_cols(const Geom& g, const double* in, double* out, int ncomp,
+                         int layout, int to_device, int x_lo, int x_hi, cudaStream_t s);
+cudaError_t reorder_cols(const Geom& g, const float* in, double* out, int ncomp,
+                         int layout, int to_device, int x_lo, int x_hi, cudaStream_t s);
+cudaError_t reorder_cols(const Geom& g, const double* in, float* out, int ncomp,
                          int layout, int to_device, int x_lo, int x_hi, cudaStream_t s);
 
 // Launches the bounded-wait self-test kernel (one mbarrier nobody arrives

@@ -45,8 +45,9 @@ cudaError_t finish_reduce(const double* partials, long long nrows, double* scrat
 // layout 0: inner ind = x*ny + y ; 1: padded ind = (x+1)*(ny+2) + (y+1)
 constexpr int kTile = 32, kTileRows = 8;
 
+template <class TI, class TO>
 __global__ void __launch_bounds__(kTile * kTileRows)
-    reorder_kernel(const Geom g, const double* __restrict__ in, double* __restrict__ out,
+    reorder_kernel(const Geom g, const TI* __restrict__ in, TO* __restrict__ out,
                    int ncomp, int layout, int to_device, int x_lo, int x_hi) {
   __shared__ double t[kTile][kTile + 1];
   const int tx = threadIdx.x, ty = threadIdx.y;
@@ -57,22 +58,22 @@ __global__ void __launch_bounds__(kTile * kTileRows)
     if (to_device) {
       for (int r = ty; r < kTile; r += kTileRows) {   // host rows: x = x0 + r, lanes along y
         const int x = x0 + r, y = y0 + tx;
-        if (x < x_hi && y < g.ny) t[r][tx] = in[((x + off) * hy + y + off) * ncomp + c];
+        if (x < x_hi && y < g.ny) t[r][tx] = double(in[((x + off) * hy + y + off) * ncomp + c]);
       }
       __syncthreads();
       for (int r = ty; r < kTile; r += kTileRows) {   // device rows: y = y0 + r, lanes along x
         const int x = x0 + tx, y = y0 + r;
-        if (x < x_hi && y < g.ny) out[c * g.plane + g.node(x, y)] = t[tx][r];
+        if (x < x_hi && y < g.ny) out[c * g.plane + g.node(x, y)] = TO(t[tx][r]);
       }
     } else {
       for (int r = ty; r < kTile; r += kTileRows) {
         const int x = x0 + tx, y = y0 + r;
-        if (x < x_hi && y < g.ny) t[r][tx] = in[c * g.plane + g.node(x, y)];
+        if (x < x_hi && y < g.ny) t[r][tx] = double(in[c * g.plane + g.node(x, y)]);
       }
       __syncthreads();
       for (int r = ty; r < kTile; r += kTileRows) {
         const int x = x0 + r, y = y0 + tx;
-        if (x < x_hi && y < g.ny) out[((x + off) * hy + y + off) * ncomp + c] = t[tx][r];
+        if (x < x_hi && y < g.ny) out[((x + off) * hy + y + off) * ncomp + c] = TO(t[tx][r]);
       }
     }
     __syncthreads();
@@ -103,18 +104,34 @@ cudaError_t bounded_wait_selftest(int* err, double limit_s, unsigned long long* 
   return cudaGetLastError();
 }
 
+template <class TI, class TO>
+static cudaError_t reorder_launch(const Geom& g, const TI* in, TO* out, int ncomp, int layout,
+                                  int to_device, int x_lo, int x_hi, cudaStream_t s) {
+  if (x_lo < 0 || x_hi > g.nx || x_lo >= x_hi) return cudaErrorInvalidValue;
+  dim3 grid((x_hi - x_lo + kTile - 1) / kTile, (g.ny + kTile - 1) / kTile);
+  reorder_kernel<TI, TO><<<grid, dim3(kTile, kTileRows), 0, s>>>(g, in, out, ncomp, layout,
+                                                                 to_device, x_lo, x_hi);
+  return cudaGetLastError();
+}
+
 cudaError_t reorder(const Geom& g, const double* in, double* out, int ncomp,
                     int layout, int to_device, cudaStream_t s) {
-  return reorder_cols(g, in, out, ncomp, layout, to_device, 0, g.nx, s);
+  return reorder_launch(g, in, out, ncomp, layout, to_device, 0, g.nx, s);
 }
 
 cudaError_t reorder_cols(const Geom& g, const double* in, double* out, int ncomp,
                          int layout, int to_device, int x_lo, int x_hi, cudaStream_t s) {
-  if (x_lo < 0 || x_hi > g.nx || x_lo >= x_hi) return cudaErrorInvalidValue;
-  dim3 grid((x_hi - x_lo + kTile - 1) / kTile, (g.ny + kTile - 1) / kTile);
-  reorder_kernel<<<grid, dim3(kTile, kTileRows), 0, s>>>(g, in, out, ncomp, layout, to_device,
-                                                         x_lo, x_hi);
-  return cudaGetLastError();
+  return reorder_launch(g, in, out, ncomp, layout, to_device, x_lo, x_hi, s);
+}
+
+cudaError_t reorder_cols(const Geom& g, const float* in, double* out, int ncomp,
+                         int layout, int to_device, int x_lo, int x_hi, cudaStream_t s) {
+  return reorder_launch(g, in, out, ncomp, layout, to_device, x_lo, x_hi, s);
+}
+
+cudaError_t reorder_cols(const Geom& g, const double* in, float* out, int ncomp,
+                         int layout, int to_device, int x_lo, int x_hi, cudaStream_t s) {
+  return reorder_launch(g, in, out, ncomp, layout, to_device, x_lo, x_hi, s);
 }
 
 }  // namespace lbm

@@ -53,6 +53,23 @@ def _dptr(a):
     return ptr(a)
 
 
+def _is_f32(a):
+    """True for a float32 numpy array or torch tensor (the field type of a
+    case with "precision": "single", pylabolt/base/fields.py:64-77)."""
+    return str(a.dtype) in ("float32", "torch.float32")
+
+
+def _fptr(a):
+    """ctypes pointer of a C-contiguous float32 or float64 field, host or CUDA."""
+    if _is_tensor(a):
+        if not a.is_contiguous() or str(a.dtype) not in ("torch.float64", "torch.float32"):
+            raise ValueError("tensor fields must be contiguous float64 or float32")
+        return ctypes.c_void_p(a.data_ptr())
+    if not a.flags.c_contiguous or a.dtype not in (np.float64, np.float32):
+        raise ValueError("fields must be C-contiguous float64 or float32 arrays")
+    return ptr(a)
+
+
 class FluidLBM:
     """One fluidLB case resident on the GPU."""
 
@@ -119,12 +136,32 @@ class FluidLBM:
 
     # -- set-up
     def initialize(self, density=None, velocity=None):
-        """f = f_eq(rho, u) on fluid nodes (equilibrium_kernels.py:38-78)."""
-        rho = np.ascontiguousarray(self.case.density if density is None else density,
-                                   dtype=np.float64)
-        u = np.ascontiguousarray(self.case.velocity if velocity is None else velocity,
-                                 dtype=np.float64)
-        check(self.lib.lbm_init_fields(self.h, ptr(rho), ptr(u), capi.LAYOUT_INNER))
+        """f = f_eq(rho, u) on fluid nodes (equilibrium_kernels.py:38-78).
+        Float32 density and velocity (both; the fields of a single-precision
+        case) cross the host link as float32 and are widened exactly on the
+        device; anything else is taken as float64.  Contiguous CUDA tensors
+        of either type are read on the device."""
+        rho = self.case.density if density is None else density
+        u = self.case.velocity if velocity is None else velocity
+        n = self.case.nx * self.case.ny
+        if _is_tensor(rho) and _is_tensor(u):
+            if rho.dtype != u.dtype:
+                raise ValueError("initialize: density and velocity of one dtype")
+            if rho.is_cuda or u.is_cuda:
+                import torch
+                torch.cuda.current_stream(rho.device).synchronize()
+            size = (rho.numel(), u.numel())
+        else:
+            if not (_is_f32(rho) and _is_f32(u)):
+                rho = np.asarray(rho, dtype=np.float64)
+                u = np.asarray(u, dtype=np.float64)
+            rho = np.ascontiguousarray(rho)
+            u = np.ascontiguousarray(u)
+            size = (rho.size, u.size)
+        if size != (n, 2 * n):
+            raise ValueError("initialize: fields of the grid size")
+        fn = self.lib.lbm_init_fields_f32 if _is_f32(rho) else self.lib.lbm_init_fields
+        check(fn(self.h, _fptr(rho), _fptr(u), capi.LAYOUT_INNER))
 
     def set_body_force(self, force):
         """[Nx, Ny, 2] body-force field: a numpy array or a float64 torch
@@ -152,30 +189,35 @@ class FluidLBM:
         check(self.lib.lbm_synchronize(self.h, float(timeout_s)))
 
     # -- results
-    def moments(self, layout=capi.LAYOUT_INNER, out=None):
+    def moments(self, layout=capi.LAYOUT_INNER, out=None, dtype=np.float64):
         """(rho, u) recorded at the last moments step: inner layout gives
         ``[Nx, Ny]`` / ``[Nx, Ny, 2]``; padded gives the reference's
-        ``[(Nx+2)*(Ny+2)]`` / ``[..., 2]`` arrays (ghosts 0).  `out` = (rho,
-        u): C-contiguous FP64 arrays of that size to fill instead (e.g. pinned
-        host memory for a faster copy)."""
+        ``[(Nx+2)*(Ny+2)]`` / ``[..., 2]`` arrays (ghosts 0).  `dtype`
+        float32 returns the fields of a single-precision case (each value
+        rounded to nearest, exact for FP32/FP16 storage).  `out` = (rho, u):
+        C-contiguous float64 or float32 arrays or tensors of that size to
+        fill instead (e.g. pinned host memory for a faster copy)."""
         nx, ny = self.case.nx, self.case.ny
         n = nx * ny if layout == capi.LAYOUT_INNER else (nx + 2) * (ny + 2)
         if out is None:
-            rho = np.empty(n)
-            u = np.empty((n, 2))
+            rho = np.empty(n, dtype=dtype)
+            u = np.empty((n, 2), dtype=dtype)
         else:
             rho, u = out
             if _is_tensor(rho) and _is_tensor(u):   # e.g. CUDA tensors: filled on the device
-                if rho.numel() != n or u.numel() != 2 * n:
-                    raise ValueError("moments(out=...): tensors of the grid size")
-                check(self.lib.lbm_get_moments(self.h, _dptr(rho), _dptr(u), layout))
+                if rho.numel() != n or u.numel() != 2 * n or rho.dtype != u.dtype:
+                    raise ValueError("moments(out=...): tensors of the grid size and one dtype")
+                fn = self.lib.lbm_get_moments_f32 if _is_f32(rho) else self.lib.lbm_get_moments
+                check(fn(self.h, _fptr(rho), _fptr(u), layout))
                 if layout == capi.LAYOUT_INNER:
                     return rho.view(nx, ny), u.view(nx, ny, 2)
                 return rho, u
-            if (rho.dtype != np.float64 or u.dtype != np.float64 or rho.size != n
+            if (rho.dtype != u.dtype or rho.dtype not in (np.float64, np.float32) or rho.size != n
                     or u.size != 2 * n or not rho.flags.c_contiguous or not u.flags.c_contiguous):
-                raise ValueError("moments(out=...): C-contiguous float64 arrays of the grid size")
-        check(self.lib.lbm_get_moments(self.h, ptr(rho), ptr(u), layout))
+                raise ValueError("moments(out=...): C-contiguous float64 or float32 arrays "
+                                 "of the grid size")
+        fn = self.lib.lbm_get_moments_f32 if _is_f32(rho) else self.lib.lbm_get_moments
+        check(fn(self.h, _fptr(rho), _fptr(u), layout))
         if layout == capi.LAYOUT_INNER:
             return rho.reshape(nx, ny), u.reshape(nx, ny, 2)
         return rho, u

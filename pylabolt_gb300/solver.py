@@ -152,7 +152,7 @@ class Solver:
         if not resumed:
             self._update_forces(self.out.obstacle_due(0), self.out.boundary_due(0))
             if self.out.save_due(c.start_time):
-                rho, u = self.lbm.moments()
+                rho, u = self.lbm.moments(dtype=self.out.dtype)
                 if c.moving:
                     self.out.set_geometry(self._moving_geometry())
                 self.out.write_fields(c.start_time, rho, u)
@@ -174,7 +174,7 @@ class Solver:
                 self.residues = r
                 self.log(log_line(t, res_density=r[:1], res_velocity=r[1:]))
             if save:
-                rho, u = self.lbm.moments()
+                rho, u = self.lbm.moments(dtype=self.out.dtype)
                 if c.moving:
                     self.out.set_geometry(self._moving_geometry())
                 self.out.write_fields(t, rho, u)

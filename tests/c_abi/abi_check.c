@@ -48,6 +48,11 @@ int main(void) {
 
   CHECK(lbm_step(NULL, 1) == LBM_ERR_ARG);
   CHECK(lbm_destroy(NULL) == LBM_ERR_ARG);
+  float fr[48], fu[96];
+  CHECK(lbm_init_fields_f32(NULL, fr, fu, LBM_LAYOUT_INNER) == LBM_ERR_ARG);
+  CHECK(strstr(lbm_last_error(), "lbm_init_fields_f32") != NULL);
+  CHECK(lbm_get_moments_f32(NULL, fr, fu, LBM_LAYOUT_INNER) == LBM_ERR_ARG);
+  CHECK(strstr(lbm_last_error(), "lbm_get_moments_f32") != NULL);
   double out[3];
   CHECK(lbm_residual(NULL, out) == LBM_ERR_ARG);
   CHECK(lbm_conservation_noalloc(NULL, NULL, NULL) == LBM_ERR_ARG);

@@ -47,10 +47,12 @@ class GoldenLBM:
         nx, ny = self.case.nx, self.case.ny
         return a.reshape(nx + 2, ny + 2, *a.shape[1:])[1:-1, 1:-1]
 
-    def moments(self):
+    def moments(self, dtype=np.float64):
         if self.t == 0:
-            return self._inner(self.g["rho0"]), self._inner(self.g["u0"])
-        return self._inner(self.g[f"density_t{self.t}"]), self._inner(self.g[f"velocity_t{self.t}"])
+            r, u = self._inner(self.g["rho0"]), self._inner(self.g["u0"])
+        else:
+            r, u = self._inner(self.g[f"density_t{self.t}"]), self._inner(self.g[f"velocity_t{self.t}"])
+        return r.astype(dtype), u.astype(dtype)
 
     def forces(self):
         return {"obstacles": self.g[f"force_obstacles_t{self.t}"],

@@ -351,7 +351,7 @@ def run_gb300(args, world, rank, local):
                        "l2": "inputs larger than L2 (two population buffers of "
                              f"{9 * nodes * B_LU[args.storage] / 18 / 1e6:.0f} MB)",
                        "parallelism": f"replicas x{world}",
-                       "kernel": {"kind": ["scalar", "vector", "tma_pipeline", "node_pairs"][variant[0]],
+                       "kernel": {"kind": ["scalar", "-", "node_pair_tiles", "node_pairs"][variant[0]],
                                   "nodes_per_thread": variant[1], "block": variant[2],
                                   "stages": variant[3],
                                   "autotune_ms": [round(t, 4) for t in tuning]}},

@@ -151,6 +151,29 @@ struct Kernels {
     return cudaErrorInvalidValue;
   }
 
+  template <int COLL, int FORC, bool RES>
+  static cudaError_t tile(const StepArgs& a, Variant v, dim3 grid, cudaStream_t s) {
+    if constexpr (Store<S>::shifted) {
+      const int smem = v.stages * tile_stage_bytes();
+      constexpr int TP = kTileBytes / (2 * sizeof(S));   // pairs of a tile
+      static int configured[3] = {0, 0, 0};   // bytes the attribute was last raised to
+      if (v.block == TP || v.block == TP / 2 || v.block == TP / 4) {
+        const int i = v.block == TP ? 0 : (v.block == TP / 2 ? 1 : 2);
+        const auto kern = i == 0   ? step_tile_pair_kernel<S, COLL, FORC, RES, 1>
+                          : i == 1 ? step_tile_pair_kernel<S, COLL, FORC, RES, 2>
+                                   : step_tile_pair_kernel<S, COLL, FORC, RES, 4>;
+        if (smem > configured[i]) {
+          cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+          if (e != cudaSuccess) return e;
+          configured[i] = smem;
+        }
+        kern<<<grid, v.block, smem, s>>>(a, v.stages);
+        return cudaGetLastError();
+      }
+    }
+    return cudaErrorInvalidValue;
+  }
+
   template <int COLL, int FORC>
   static cudaError_t step_t(const StepArgs& a, Variant v, int sms, cudaStream_t s) {
     const dim3 grid = step_grid(a.g, v, sms, sizeof(S));
@@ -171,28 +194,14 @@ struct Kernels {
         if (a.flags & F_RESIDUAL) return pair<COLL, FORC, true>(a, v, grid, s);
         return pair<COLL, FORC, false>(a, v, grid, s);
       }
-      if (v.kind == 2) {
-        if (v.stages < 1 || v.stages > 8) return cudaErrorInvalidValue;
-        const int smem = v.stages * tma_stage_bytes(sizeof(S));
-        static int configured = 0;   // bytes the attribute was last raised to
-        if (smem > configured) {
-          cudaError_t e = cudaFuncSetAttribute(step_tma_kernel<S, COLL, FORC>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-          if (e != cudaSuccess) return e;
-          configured = smem;
-        }
-        step_tma_kernel<S, COLL, FORC><<<grid, v.block, smem, s>>>(a, v.stages);
-        return cudaGetLastError();
-      }
-      constexpr int V1 = sizeof(S) == 4 ? 4 : 8;
-      constexpr int V2 = sizeof(S) == 4 ? 2 : 4;
-      if (v.kind == 1 && v.vec == V1) {
-        step_vec_kernel<S, V1, COLL, FORC><<<grid, v.block, 0, s>>>(a);
-        return cudaGetLastError();
-      }
-      if (v.kind == 1 && v.vec == V2) {
-        step_vec_kernel<S, V2, COLL, FORC><<<grid, v.block, 0, s>>>(a);
-        return cudaGetLastError();
+      if (v.kind == 2) {   // node pairs from shared-memory tiles (no moving obstacles)
+        if (v.vec != 2 || (v.block != kTileBytes / (2 * (int)sizeof(S)) &&
+                           v.block != kTileBytes / (4 * (int)sizeof(S)) &&
+                           v.block != kTileBytes / (8 * (int)sizeof(S))) ||
+            v.stages < 1 || v.stages > kMaxTileStages || a.rho_dyn_out)
+          return cudaErrorInvalidValue;
+        if (a.flags & F_RESIDUAL) return tile<COLL, FORC, true>(a, v, grid, s);
+        return tile<COLL, FORC, false>(a, v, grid, s);
       }
     }
     if (v.kind != 0) return cudaErrorInvalidValue;
@@ -283,18 +292,18 @@ struct Kernels {
     k.compute_bytes = sizeof(T);
     k.step = &step;
     if constexpr (Store<S>::shifted) {
-      constexpr int V1 = sizeof(S) == 4 ? 4 : 8;
-      constexpr int V2 = sizeof(S) == 4 ? 2 : 4;
-      // kind 2: {threads, stages}; kind 1: {nodes per thread, threads};
+      // kind 2: node pairs from shared-memory tiles {2, threads, stages}
+      // (TP threads: one pair of a tile each, TP / 2: two, TP / 4: four);
       // kind 0: {threads, register cap: 0 none, 1 32, 2 40};
       // kind 3: node pairs {2 nodes per thread, threads, register cap: 0 none,
       // 1 40, 2 64, 3 32}
-      const Variant vs[] = {{2, 0, 256, 4}, {2, 0, 512, 3}, {2, 0, 256, 2}, {1, V1, 256, 0},
-                            {1, V2, 256, 0}, {0, 1, 128, 0}, {0, 1, 256, 0}, {0, 1, 128, 1},
+      constexpr int TP = kTileBytes / (2 * sizeof(S));
+      const Variant vs[] = {{2, 2, TP / 2, 2}, {2, 2, TP / 2, 3}, {2, 2, TP, 2},
+                            {2, 2, TP / 4, 2}, {0, 1, 128, 0}, {0, 1, 256, 0}, {0, 1, 128, 1},
                             {0, 1, 256, 1}, {0, 1, 128, 2}, {0, 1, 256, 2}, {3, 2, 128, 0},
                             {3, 2, 256, 0}, {3, 2, 128, 1}, {3, 2, 256, 2}, {3, 2, 128, 3}};
-      k.nvariants = 16;
-      for (int i = 0; i < 16; ++i) k.variants[i] = vs[i];
+      k.nvariants = 15;
+      for (int i = 0; i < 15; ++i) k.variants[i] = vs[i];
     } else {
       const Variant vs[] = {{0, 1, 128, 0}, {0, 1, 256, 0}, {0, 1, 512, 0}};
       k.nvariants = 3;

@@ -323,8 +323,9 @@ struct LbmHandle {
     for (int pass = 0; pass < 2 && rc == LBM_OK; ++pass)
       for (int i = 0; i < ks->nvariants && rc == LBM_OK; ++i) {
         const lbm::Variant v = ks->variants[i];
-        // the scalar and node-pair kernels have residual instantiations
-        if (v.kind != 0 && (v.kind != 3 || mov.n)) continue;
+        // every kernel has a residual instantiation; moving obstacles take
+        // the scalar one
+        if (v.kind != 0 && mov.n) continue;
         if ((rc = launch_v(lbm::F_RESIDUAL, v, false))) break;
         cudaEventRecord(e0, stream);
         for (int r = 0; r < 4 && rc == LBM_OK; ++r) rc = launch_v(lbm::F_RESIDUAL, v, false);
@@ -830,6 +831,9 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   for (int y = 0; y < ny; ++y)
     for (int x = 0; x < nx; ++x)
       if (cls[dnode(x, y)]) segflag[(size_t)y * nseg + x / 32] = 1;
+  std::vector<int> seglist;
+  for (size_t i = 0; i < segflag.size(); ++i)
+    if (segflag[i]) seglist.push_back((int)i);
 
   // ---- device --------------------------------------------------------------
   LbmHandle* h = new LbmHandle();
@@ -874,12 +878,13 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   g.nrec = (int)nlinks;
   const size_t eb = ks->elem_bytes, cb = ks->compute_bytes;
   const size_t nrec1 = std::max<int64_t>(nlinks, 1);
-  void *d_cls, *d_seg, *d_recmap, *d_rtype, *d_rsrc, *d_rparam, *d_raux, *d_rpf;
+  void *d_cls, *d_seg, *d_seglist, *d_recmap, *d_rtype, *d_rsrc, *d_rparam, *d_raux, *d_rpf;
   std::vector<float2> rpf(rparam.size());
   for (size_t i = 0; i < rparam.size(); ++i)
     rpf[i] = make_float2((float)rparam[i], (float)(rparam[i] - 1.0));
   int rc;
   if ((rc = h->alloc(&d_cls, plane)) || (rc = h->alloc(&d_seg, segflag.size())) ||
+      (rc = h->alloc(&d_seglist, std::max<size_t>(seglist.size(), 1) * sizeof(int))) ||
       (rc = h->alloc(&d_recmap, plane * sizeof(int))) || (rc = h->alloc(&d_rtype, 9 * nrec1)) ||
       (rc = h->alloc(&d_rsrc, 9 * nrec1 * sizeof(int))) ||
       (rc = h->alloc(&d_rparam, 9 * nrec1 * sizeof(double))) ||
@@ -931,6 +936,8 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   if (e != cudaSuccess) return bail(fail(LBM_ERR_ALLOC, std::string("cudaMallocHost: ") + cudaGetErrorString(e)));
   g.cls = (const uint8_t*)d_cls;
   g.segflag = (const uint8_t*)d_seg;
+  g.seglist = (const int*)d_seglist;
+  g.nflag = (int)seglist.size();
   g.recmap = (const int*)d_recmap;
   g.rtype = (const int8_t*)d_rtype;
   g.rsrc = (const int*)d_rsrc;
@@ -942,6 +949,7 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   };
   if ((e = up(d_cls, cls.data(), plane)) != cudaSuccess ||
       (e = up(d_seg, segflag.data(), segflag.size())) != cudaSuccess ||
+      (!seglist.empty() && (e = up(d_seglist, seglist.data(), seglist.size() * sizeof(int))) != cudaSuccess) ||
       (e = up(d_recmap, recmap.data(), plane * sizeof(int))) != cudaSuccess ||
       (e = up(d_rtype, rtype.data(), rtype.size())) != cudaSuccess ||
       (e = up(d_rsrc, rsrc.data(), rsrc.size() * sizeof(int))) != cudaSuccess ||

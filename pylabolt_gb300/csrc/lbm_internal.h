@@ -20,6 +20,8 @@ struct Geom {
   const uint8_t* cls;        // [plane] node class: 0 bulk, 1 special, 2 solid
                              // (3 on padding rows and columns)
   const uint8_t* segflag;    // [ny*nseg] 0: all 32 nodes of the segment bulk
+  const int* seglist;        // [nflag] y*nseg + x/32 of every segment flagged at
+  int nflag;                 // creation, in order (the kind-2 kernel's boundary work)
   const int* recmap;         // [plane] record index of special nodes
   int nrec;
   const int8_t* rtype;       // [nrec*9] link kind
@@ -193,9 +195,9 @@ struct MovArgs {
 
 // Launch shape of the fused step.
 //   kind 0: scalar kernel, one node per thread
-//   kind 1: vector kernel, `vec` consecutive nodes per thread
-//   kind 2: persistent TMA-pipelined kernel: tiles of one row segment of
-//           kTmaRowBytes, `stages` shared-memory stages, `block` threads
+//   kind 2: persistent node-pair kernel fed by bulk copies: tiles of one row
+//           segment of kTileBytes per plane, `stages` shared-memory stages,
+//           `block` threads (vec = 2)
 //   kind 3: node-pair kernel, two nodes per thread along x (vec = 2),
 //           `stages` its register cap
 struct Variant {
@@ -206,8 +208,11 @@ struct Variant {
 };
 
 constexpr int kMaxVariants = 16;     // autotuner candidates per storage at most
-constexpr int kTmaRowBytes = 4096;   // tile width in bytes of one plane row
-constexpr int kTmaHaloBytes = 16;    // TMA granule: halo on each side
+constexpr int kTmaRowBytes = 4096;   // row pitch alignment of shifted storage, bytes
+constexpr int kTileBytes = 2048;     // tile width of the kind-2 kernel, bytes of one plane row
+constexpr int kTmaHaloBytes = 16;    // bulk-copy granule: halo on each side
+constexpr int kMaxTileStages = 8;    // shared-memory stages of the kind-2 kernel at most
+constexpr int kSmemPerSM = 228 * 1024;   // shared memory of one SM, bytes
 constexpr int kErrWaitTimeout = 1;   // err code: an mbarrier wait timed out
 constexpr int kErrMovBounds = 2;     // a moving obstacle would leave the allowed region
 constexpr int kErrMovSpeed = 3;      // a moving obstacle would move a node or more in a step
@@ -263,18 +268,21 @@ const KernelSet& kernels_fp16();
 constexpr int kFinishBlocks = 128;
 cudaError_t finish_reduce(const double* partials, long long nrows, double* scratch,
                           double* out8, cudaStream_t s);
-// Shared memory of one TMA stage (nine halo-padded row windows).
-inline int tma_stage_bytes(int elem_bytes) {
-  return 9 * (kTmaRowBytes + 2 * kTmaHaloBytes);
-}
+// Shared memory of one stage of the kind-2 kernel (nine halo-padded row windows).
+inline int tile_stage_bytes() { return 9 * (kTileBytes + 2 * kTmaHaloBytes); }
 // Number of SMs of the current device (cached by the caller's handle).
-// grid of the fused step for variant v (`sms` multiprocessors)
+// grid of the fused step for variant v (`sms` multiprocessors).  Kind 2 is
+// persistent: as many blocks as are sure to be resident at once -- shared
+// memory per block (stages, the static barriers and residual rows, and the
+// 1 KB the runtime reserves) and the 1024 threads per SM its launch bounds
+// guarantee registers for.
 inline dim3 step_grid(const Geom& g, Variant v, int sms, int elem_bytes) {
   if (v.kind == 2) {
-    const long long tiles = (long long)g.ny * (g.pitch / (kTmaRowBytes / elem_bytes));
-    const int smem = v.stages * tma_stage_bytes(elem_bytes) + 1024;
-    int per_sm = (227 * 1024) / smem;
-    if (per_sm * v.block > 2048) per_sm = 2048 / v.block;
+    const int tw = kTileBytes / elem_bytes;
+    const long long tiles = (long long)g.ny * ((g.nx + tw - 1) / tw);
+    const int smem = v.stages * tile_stage_bytes() + 8 * kMaxTileStages + 32 * 8 * 8 + 1024;
+    int per_sm = kSmemPerSM / smem;
+    if (per_sm * v.block > 1024) per_sm = 1024 / v.block;   // 64 registers a thread
     if (per_sm < 1) per_sm = 1;
     long long blocks = (long long)sms * per_sm;
     if (blocks > tiles) blocks = tiles;

@@ -992,6 +992,26 @@ __device__ __forceinline__ void pair_outputs(const StepArgs& a, long long n, flo
   }
 }
 
+// Collision, stores and outputs of a bulk pair (nodes n, n + 1) from its
+// nine incoming words; ob: the byte address of node n in plane 0 of fout.
+template <class S, int COLL, int FORC, bool RES>
+__device__ __forceinline__ void pair_finish(const StepArgs& a, long long n, int seg,
+                                            char* __restrict__ ob,
+                                            const typename PairIO<S>::W w[9],
+                                            const float2 o2[3], float red[7]) {
+  using IO = PairIO<S>;
+  using W = typename IO::W;
+  float f0[9], f1[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) IO::unpack(w[k], f0[k], f1[k]);
+  float rho0, ux0, uy0, rho1, ux1, uy1;
+  node_update<S, COLL, FORC>(f0, a, n, rho0, ux0, uy0, seg);
+  node_update<S, COLL, FORC>(f1, a, n + 1, rho1, ux1, uy1, seg);
+#pragma unroll
+  for (int k = 0; k < 9; ++k) *reinterpret_cast<W*>(ob + a.off_plane[k]) = IO::pack(f0[k], f1[k]);
+  pair_outputs<RES>(a, n, rho0, ux0, uy0, rho1, ux1, uy1, red, o2);
+}
+
 // One pair of the node-pair kernel (row y, nodes x0 and x0 + 1).
 template <class S, int COLL, int FORC, bool RES>
 __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, float red[7]) {
@@ -1026,15 +1046,7 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, floa
   w[6] = pair_pull<S, 6>(fb, a.off_pull[6]);
   w[7] = pair_pull<S, 7>(fb, a.off_pull[7]);
   w[8] = pair_pull<S, 8>(fb, a.off_pull[8]);
-  float f0[9], f1[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) IO::unpack(w[k], f0[k], f1[k]);
-  float rho0, ux0, uy0, rho1, ux1, uy1;
-  node_update<S, COLL, FORC>(f0, a, n, rho0, ux0, uy0, seg);
-  node_update<S, COLL, FORC>(f1, a, n + 1, rho1, ux1, uy1, seg);
-#pragma unroll
-  for (int k = 0; k < 9; ++k) *reinterpret_cast<W*>(ob + a.off_plane[k]) = IO::pack(f0[k], f1[k]);
-  pair_outputs<RES>(a, n, rho0, ux0, uy0, rho1, ux1, uy1, red, o2);
+  pair_finish<S, COLL, FORC, RES>(a, n, seg, ob, w, o2, red);
 }
 
 // CAP = 1 asks for 6 resident blocks of 256 threads (at most 40 registers),
@@ -1125,181 +1137,15 @@ __global__ void __launch_bounds__(256, CAP == 1 ? 6 : (CAP == 2 ? 4 : 1))
 }
 
 // ---------------------------------------------------------------------------
-// Vector I/O of V consecutive nodes (16- or 8-byte aligned accesses).
-template <class S, int V> struct VecIO;
-template <int V> struct VecIO<float, V> {
-  static_assert(V == 2 || V == 4, "float vectors of 2 or 4");
-  __device__ static __forceinline__ void load(const float* __restrict__ p, float (&out)[V], const Params&) {
-    if constexpr (V == 4) {
-      const float4 v = __ldg(reinterpret_cast<const float4*>(p));
-      out[0] = v.x; out[1] = v.y; out[2] = v.z; out[3] = v.w;
-    } else {
-      const float2 v = __ldg(reinterpret_cast<const float2*>(p));
-      out[0] = v.x; out[1] = v.y;
-    }
-  }
-  __device__ static __forceinline__ float ld1(const float* __restrict__ p, const Params&) { return __ldg(p); }
-  __device__ static __forceinline__ void store(float* __restrict__ p, const float (&in)[V], const Params&) {
-    if constexpr (V == 4)
-      *reinterpret_cast<float4*>(p) = make_float4(in[0], in[1], in[2], in[3]);
-    else
-      *reinterpret_cast<float2*>(p) = make_float2(in[0], in[1]);
-  }
-};
-template <int V> struct VecIO<__half, V> {
-  static_assert(V == 4 || V == 8, "half vectors of 4 or 8");
-  __device__ static __forceinline__ void load(const __half* __restrict__ p, float (&out)[V], const Params&) {
-    uint32_t w[V / 2];
-    if constexpr (V == 8) {
-      const uint4 raw = __ldg(reinterpret_cast<const uint4*>(p));
-      w[0] = raw.x; w[1] = raw.y; w[2] = raw.z; w[3] = raw.w;
-    } else {
-      const uint2 raw = __ldg(reinterpret_cast<const uint2*>(p));
-      w[0] = raw.x; w[1] = raw.y;
-    }
-#pragma unroll
-    for (int i = 0; i < V / 2; ++i) {
-      __half2 h;
-      memcpy(&h, &w[i], 4);
-      const float2 t = __half22float2(h);
-      out[2 * i] = t.x;
-      out[2 * i + 1] = t.y;
-    }
-  }
-  __device__ static __forceinline__ float ld1(const __half* __restrict__ p, const Params&) {
-    return __half2float(p[0]);
-  }
-  __device__ static __forceinline__ void store(__half* __restrict__ p, const float (&in)[V], const Params&) {
-    uint32_t w[V / 2];
-#pragma unroll
-    for (int i = 0; i < V / 2; ++i) {
-      const __half2 h = __floats2half2_rn(in[2 * i], in[2 * i + 1]);
-      memcpy(&w[i], &h, 4);
-    }
-    if constexpr (V == 8)
-      *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
-    else
-      *reinterpret_cast<uint2*>(p) = make_uint2(w[0], w[1]);
-  }
-};
-
-// Pulls direction K for the V nodes of this lane: one aligned vector load of
-// the source row plus a warp shuffle for the x shift (lane 0 / lane 31 load
-// the one element that crosses the warp's segment).
-template <class S, int V, int K>
-__device__ __forceinline__ void pull_dir(const S* __restrict__ fin, const Geom& g,
-                                         const Params& p, long long n0, int lane,
-                                         bool nopull, float (&f)[9][V]) {
-  constexpr int cx = CXk(K), cy = CYk(K);
-  const S* row = fin + K * g.plane + n0 - (nopull ? 0 : cy * g.pitch);
-  float a[V];
-  VecIO<S, V>::load(row, a, p);
-  if (cx == 0 || nopull) {  // nopull is the same for the whole grid
-#pragma unroll
-    for (int v = 0; v < V; ++v) f[K][v] = a[v];
-    return;
-  }
-  if constexpr (cx == 1) {
-    float prev = __shfl_up_sync(0xffffffffu, a[V - 1], 1);
-    if (lane == 0) prev = VecIO<S, V>::ld1(row - 1, p);
-    f[K][0] = prev;
-#pragma unroll
-    for (int v = 1; v < V; ++v) f[K][v] = a[v - 1];
-  } else {
-    float next = __shfl_down_sync(0xffffffffu, a[0], 1);
-    if (lane == 31) next = VecIO<S, V>::ld1(row + V, p);
-#pragma unroll
-    for (int v = 0; v < V - 1; ++v) f[K][v] = a[v + 1];
-    f[K][V - 1] = next;
-  }
-}
-
-// Vector kernel: each thread updates V consecutive nodes of one row; a warp
-// covers 32*V nodes (512 bytes of every population plane).  All lanes take
-// part in the loads and shuffles; boundary / solid / padding nodes are then
-// handled per node.
-template <class S, int V, int COLL, int FORC>
-__global__ void __launch_bounds__(256) step_vec_kernel(const StepArgs a) {
-  static_assert(Store<S>::shifted, "vector kernel is for shifted storage");
-  const Geom& g = a.g;
-  const Params& p = a.p;
-  const int lane = threadIdx.x & 31;
-  const int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * V;
-  const int warp_x0 = x0 - lane * V;
-  const int y = blockIdx.y;
-  float red[7] = {0, 0, 0, 0, 0, 0, 0};
-
-  if (warp_x0 < g.pitch) {
-    const long long n0 = g.node(x0, y);
-    const S* __restrict__ fin = static_cast<const S*>(a.fin);
-    S* __restrict__ fout = static_cast<S*>(a.fout);
-    const bool nopull = (a.flags & F_NOPULL) != 0;
-    float f[9][V];
-    pull_dir<S, V, 0>(fin, g, p, n0, lane, nopull, f);
-    pull_dir<S, V, 1>(fin, g, p, n0, lane, nopull, f);
-    pull_dir<S, V, 2>(fin, g, p, n0, lane, nopull, f);
-    pull_dir<S, V, 3>(fin, g, p, n0, lane, nopull, f);
-    pull_dir<S, V, 4>(fin, g, p, n0, lane, nopull, f);
-    pull_dir<S, V, 5>(fin, g, p, n0, lane, nopull, f);
-    pull_dir<S, V, 6>(fin, g, p, n0, lane, nopull, f);
-    pull_dir<S, V, 7>(fin, g, p, n0, lane, nopull, f);
-    pull_dir<S, V, 8>(fin, g, p, n0, lane, nopull, f);
-
-    if (x0 < g.nx) {
-      uint8_t cls[V];
-#pragma unroll
-      for (int v = 0; v < V; ++v) cls[v] = 0;
-      if (g.segflag[y * g.nseg + (x0 >> 5)]) {
-#pragma unroll
-        for (int v = 0; v < V; ++v) cls[v] = g.cls[n0 + v];
-      } else if (x0 + V > g.nx) {
-#pragma unroll
-        for (int v = 0; v < V; ++v) cls[v] = (x0 + v < g.nx) ? 0 : 3;
-      }
-#pragma unroll
-      for (int v = 0; v < V; ++v) {
-        if (cls[v] >= 2) continue;  // solid or padding: keep as loaded
-        float fn[9];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) fn[k] = f[k][v];
-        int r = -1;
-        if (cls[v] == 1) {
-          r = g.recmap[n0 + v];
-          if (!nopull) special_links<S>(fn, a, fin, n0 + v, r);
-        }
-        float rho, ux, uy;
-        node_update<S, COLL, FORC>(fn, a, n0 + v, rho, ux, uy, y * g.nseg + ((x0 + v) >> 5));
-#pragma unroll
-        for (int k = 0; k < 9; ++k) f[k][v] = fn[k];
-        node_outputs<float>(a, n0 + v, r, rho, ux, uy, red);
-      }
-#pragma unroll
-      for (int k = 0; k < 9; ++k) VecIO<S, V>::store(fout + k * g.plane + n0, f[k], p);
-    }
-  }
-  if (a.flags & F_RESIDUAL) block_residual<decltype(red[0] + 0)>(a, red);
-}
-
-// ---------------------------------------------------------------------------
-// Persistent TMA-pipelined kernel (shifted storage).
-//
-// Work is split into tiles: one row y and a segment of W = kTmaRowBytes bytes
-// of every population plane.  For a tile, thread 0 issues nine bulk copies
-// (cp.async.bulk, one per direction k) of the source row y - c_ky over
-// [x0 - H, x0 + W + H) into one shared-memory stage and arms the stage's
-// mbarrier with the byte count; the block then reads each node's nine
-// incoming populations from shared memory at offset x - x0 + H - c_kx.  The
-// ring of `stages` stages keeps stages-1 tiles of loads in flight while the
-// block computes, without holding them in registers.  Stores go straight to
-// global memory (each warp writes 32 consecutive nodes per direction).
-// Every mbarrier wait is bounded in wall-clock time; on expiry the kernel
-// records kErrWaitTimeout, waits (bounded) for its own copies and returns.
-
+// Shared-memory and bulk-copy helpers (bounded mbarrier waits).
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
@@ -1342,125 +1188,204 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity,
   return true;
 }
 
-template <class S>
-__device__ __forceinline__ float smem_ld(const S* p, const Params& q);
-template <>
-__device__ __forceinline__ float smem_ld<float>(const float* p, const Params&) { return *p; }
-template <>
-__device__ __forceinline__ float smem_ld<__half>(const __half* p, const Params&) {
-  return __half2float(*p);
+// Persistent node-pair kernel fed by bulk copies (shifted storage).
+//
+// Work is split into tiles: one row y and TW = kTileBytes / sizeof(S) nodes of
+// every population plane.  For a tile, thread 0 copies per direction k the
+// source row y - c_ky over [x0 - H, x0 + TW + H) (H: one 16-byte granule of
+// halo on each side) into one shared-memory stage with cp.async.bulk, and arms
+// the stage's mbarrier with the byte count.  The ring of `stages` stages keeps
+// the next tiles' loads in flight while the block works on the current one,
+// with no registers holding them.  A thread takes node pairs of the tile: it
+// reads the nine incoming words from shared memory (the x shift as in
+// pair_pull), and the arithmetic and the stores are those of the node-pair
+// kernel.  Flagged segments (boundary, solid and padding nodes) are left out
+// of the tiles: their per-node path (link records, dependent global loads)
+// would hold up the warp that refills the ring and, through it, the block.
+// After its tiles each block works through its share of the list of flagged
+// segments, one node per lane through step_node; a no-pull step runs every
+// node through step_node.  Every mbarrier wait is bounded in
+// wall-clock time; on expiry the kernel records kErrWaitTimeout, waits
+// (bounded) for its own copies and returns.
+template <class S, int K>
+__device__ __forceinline__ typename PairIO<S>::W tile_pull(const typename PairIO<S>::W* row) {
+  using IO = PairIO<S>;
+  constexpr int cx = CXk(K);
+  if (cx == 0) return row[0];
+  if (cx == 1) return IO::mid(row[-1], row[0]);
+  return IO::mid(row[0], row[1]);
 }
 
-template <class S, int COLL, int FORC>
-__global__ void __launch_bounds__(1024) step_tma_kernel(const StepArgs a, int stages) {
-  static_assert(Store<S>::shifted, "TMA kernel is for shifted storage");
-  constexpr int W = kTmaRowBytes / sizeof(S);       // nodes per tile
-  constexpr int H = kTmaHaloBytes / sizeof(S);      // halo elements
-  constexpr int RW = W + 2 * H;                     // row window elements
-  constexpr uint32_t kCopyBytes = RW * sizeof(S);
+// The flagged segments of the kind-2 kernel: block b takes its share of the
+// segment list, one segment per warp, one node per lane (step_node).
+template <class S, int COLL, int FORC, bool RES>
+__device__ __forceinline__ void tile_flagged_segments(const StepArgs& a, float red[7]) {
+  const Geom& g = a.g;
+  const int f0 = (int)((long long)g.nflag * blockIdx.x / gridDim.x);
+  const int f1 = (int)((long long)g.nflag * (blockIdx.x + 1) / gridDim.x);
+  for (int i = f0 + (int)(threadIdx.x >> 5); i < f1; i += (int)(blockDim.x >> 5)) {
+    const int sg = g.seglist[i];
+    const int y = sg / g.nseg;
+    const int x = (sg - y * g.nseg) * 32 + (int)(threadIdx.x & 31);
+    if (x < g.nx) step_node<S, COLL, FORC, false, RES>(a, x, y, red);
+  }
+}
+
+// PPT: pairs of a tile per thread (blocks of TW / (2 PPT) threads); up to 64
+// registers a thread.
+template <class S, int COLL, int FORC, bool RES, int PPT>
+__global__ void __launch_bounds__(kTileBytes / (2 * PPT * sizeof(S)), 2048 * PPT * sizeof(S) / kTileBytes)
+    step_tile_pair_kernel(const StepArgs a, int stages) {
+  static_assert(Store<S>::shifted, "the tile kernel is for shifted storage");
+  using IO = PairIO<S>;
+  using W = typename IO::W;
+  constexpr int TW = kTileBytes / sizeof(S);         // nodes per tile
+  constexpr int H = kTmaHaloBytes / sizeof(S);       // halo nodes on each side
+  constexpr int RWW = (TW + 2 * H) / 2;              // words of one stage row
+  constexpr uint32_t kCopyBytes = (TW + 2 * H) * sizeof(S);
   constexpr uint32_t kStageBytes = 9 * kCopyBytes;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  __shared__ __align__(8) unsigned long long bars[8];
+  __shared__ __align__(8) unsigned long long full[kMaxTileStages], empty[kMaxTileStages];
   const Geom& g = a.g;
-  const Params& p = a.p;
-  const int tiles_per_row = g.pitch / W;
-  const long long ntiles = (long long)g.ny * tiles_per_row;
-  const bool nopull = (a.flags & F_NOPULL) != 0;
-  const S* __restrict__ fin = static_cast<const S*>(a.fin);
-  S* __restrict__ fout = static_cast<S*>(a.fout);
   float red[7] = {0, 0, 0, 0, 0, 0, 0};
 
+  if (a.flags & F_NOPULL) {   // first step after initialisation: per node
+    const int npr = (g.nx + 1) / 2;
+    const long long total = (long long)g.ny * npr;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (long long)gridDim.x * blockDim.x) {
+      const int y = (int)(q / npr), x0 = 2 * (int)(q % npr);
+      if (g.segflag[y * g.nseg + (x0 >> 5)] != 0) continue;   // in the segment list
+      step_node<S, COLL, FORC, false, RES>(a, x0, y, red);
+      step_node<S, COLL, FORC, false, RES>(a, x0 + 1, y, red);
+    }
+    tile_flagged_segments<S, COLL, FORC, RES>(a, red);
+    if constexpr (RES) block_residual<float>(a, red);
+    return;
+  }
+
+  // block b takes the contiguous tiles [t0, t1) in row-major order; the
+  // consumer cursor (cy, cx) and thread 0's copy cursor (py, px) walk them
+  const int tpr = (g.nx + TW - 1) / TW;
+  const int ntiles = g.ny * tpr;
+  const int t0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
+  const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
+  const char* fin = static_cast<const char*>(a.fin);
+  const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < stages; ++s) mbar_init(smem_u32(&bars[s]), 1);
+    for (int s = 0; s < stages; ++s) {
+      mbar_init(smem_u32(&full[s]), 1);
+      mbar_init(smem_u32(&empty[s]), blockDim.x / 32);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
 
-  auto issue = [&](long long tile, int s) {
-    const int y = (int)(tile / tiles_per_row);
-    const int x0 = (int)(tile % tiles_per_row) * W;
-    const uint32_t bar = smem_u32(&bars[s]);
+  auto issue = [&](int y, int x0, int s) {
+    const uint32_t bar = smem_u32(&full[s]);
     mbar_expect_tx(bar, kStageBytes);
     const uint32_t dst0 = smem_u32(smem_raw + (size_t)s * kStageBytes);
+    const char* src0 = fin + (g.node(x0, y) - H) * (long long)sizeof(S);
 #pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      const int dy = nopull ? 0 : CYk(k);
-      const S* src = fin + k * g.plane + g.node(x0, y) - (long long)dy * g.pitch - H;
-      bulk_g2s(dst0 + k * kCopyBytes, src, kCopyBytes, bar);
-    }
+    for (int k = 0; k < 9; ++k) bulk_g2s(dst0 + k * kCopyBytes, src0 + a.off_pull[k], kCopyBytes, bar);
   };
-
-  // prologue: fill the ring (thread 0 counts the tiles it has issued)
-  long long issued = 0;
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < stages; ++s) {
-      const long long t = blockIdx.x + (long long)s * gridDim.x;
-      if (t < ntiles) {
-        issue(t, s);
-        ++issued;
-      }
+  int cy = t0 / tpr, cx = (t0 - cy * tpr) * TW;
+  int py = cy, px = cx, pt = t0;
+  if (threadIdx.x == 0) {   // prologue: fill the ring
+    for (int s = 0; s < stages && pt < t1; ++s, ++pt) {
+      issue(py, px, s);
+      px += TW;
+      if (px >= g.nx) px = 0, ++py;
     }
   }
 
+  // Each warp walks the tiles on its own: it waits for a stage's copies
+  // (full), works on its pairs and releases the stage (empty, one arrival
+  // per warp).  Thread 0 refills a stage once every warp has released it, so
+  // a warp slowed by boundary pairs holds up no other warp until the ring's
+  // other stages are used up.  Waits are bounded and their outcome is made
+  // warp-uniform, so a warp leaves the loop as a whole.
   bool ok = true;
-  long long it = 0;
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
-    const int s = (int)(it % stages);
-    const uint32_t parity = (uint32_t)((it / stages) & 1);
-    const bool got = mbar_wait_bounded(smem_u32(&bars[s]), parity, a.err);
-    if (__syncthreads_or(!got)) {  // the whole block leaves together
+  int t = t0, s = 0;
+  uint32_t parity = 0;
+  for (; t < t1; ++t) {
+    // the thread's pairs of this tile: segment flags (and the previous
+    // residual step's fields) are loaded before the wait for the stage
+    int x0[PPT];
+    bool bulk[PPT];
+    float2 o2[PPT][3];
+#pragma unroll
+    for (int p = 0; p < PPT; ++p) {
+      x0[p] = cx + 2 * (int)(threadIdx.x + p * blockDim.x);
+      bulk[p] = x0[p] < g.nx && g.segflag[cy * g.nseg + (x0[p] >> 5)] == 0;
+      if (RES && bulk[p]) {
+        const long long n = g.node(x0[p], cy);
+        o2[p][0] = *reinterpret_cast<const float2*>(static_cast<const float*>(a.rho_old) + n);
+        o2[p][1] = *reinterpret_cast<const float2*>(static_cast<const float*>(a.ux_old) + n);
+        o2[p][2] = *reinterpret_cast<const float2*>(static_cast<const float*>(a.uy_old) + n);
+      }
+    }
+    if (!__all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&full[s]), parity, a.err))) {
       ok = false;
       break;
     }
-    const S* stage = reinterpret_cast<const S*>(smem_raw + (size_t)s * kStageBytes);
-    const int y = (int)(tile / tiles_per_row);
-    const int x0 = (int)(tile % tiles_per_row) * W;
-    for (int xl = threadIdx.x; xl < W; xl += blockDim.x) {
-      const int x = x0 + xl;
-      if (x >= g.nx) continue;
-      const long long n = g.node(x, y);
-      int cls = 0;
-      if (g.segflag[y * g.nseg + (x >> 5)]) cls = g.cls[n];
-      if (cls == 2) continue;
-      float f[9];
+    const W* stage = reinterpret_cast<const W*>(smem_raw + (size_t)s * kStageBytes);
 #pragma unroll
-      for (int k = 0; k < 9; ++k) {
-        const int dx = nopull ? 0 : CXk(k);
-        f[k] = smem_ld<S>(stage + k * RW + xl + H - dx, p);
-      }
-      int r = -1;
-      if (cls == 1) {
-        r = g.recmap[n];
-        if (!nopull) special_links<S>(f, a, fin, n, r);
-      }
-      float rho, ux, uy;
-      node_update<S, COLL, FORC>(f, a, n, rho, ux, uy, y * g.nseg + (x >> 5));
-#pragma unroll
-      for (int k = 0; k < 9; ++k) Store<S>::str(fout, k * g.plane + n, f[k]);
-      node_outputs<float>(a, n, r, rho, ux, uy, red);
+    for (int p = 0; p < PPT; ++p) {
+      if (!bulk[p]) continue;   // flagged: in the segment list, after the tiles
+      const int j = (int)(threadIdx.x + p * blockDim.x);
+      const long long n = g.node(x0[p], cy);
+      const W* row = stage + H / 2 + j;   // the pair's word in direction 0's row
+      W w[9];
+      w[0] = tile_pull<S, 0>(row);
+      w[1] = tile_pull<S, 1>(row + 1 * RWW);
+      w[2] = tile_pull<S, 2>(row + 2 * RWW);
+      w[3] = tile_pull<S, 3>(row + 3 * RWW);
+      w[4] = tile_pull<S, 4>(row + 4 * RWW);
+      w[5] = tile_pull<S, 5>(row + 5 * RWW);
+      w[6] = tile_pull<S, 6>(row + 6 * RWW);
+      w[7] = tile_pull<S, 7>(row + 7 * RWW);
+      w[8] = tile_pull<S, 8>(row + 8 * RWW);
+      char* ob = reinterpret_cast<char*>(static_cast<S*>(a.fout) + n);
+      pair_finish<S, COLL, FORC, RES>(a, n, cy * g.nseg + (x0[p] >> 5), ob, w, o2[p], red);
     }
-    __syncthreads();  // every thread is done reading stage s
-    if (threadIdx.x == 0) {
-      const long long next = tile + (long long)stages * gridDim.x;
-      if (next < ntiles) {
-        issue(next, s);
-        ++issued;
+    __syncwarp();   // every lane is done reading stage s
+    if (lane == 0) mbar_arrive(smem_u32(&empty[s]));
+    if (threadIdx.x < 32) {   // warp 0: thread 0 refills stage s with tile pt
+      bool got = true;
+      if (threadIdx.x == 0 && pt < t1) {
+        got = mbar_wait_bounded(smem_u32(&empty[s]), parity, a.err);
+        if (got) {
+          issue(py, px, s);
+          px += TW;
+          if (px >= g.nx) px = 0, ++py;
+          ++pt;
+        }
+      }
+      if (!__shfl_sync(0xffffffffu, got, 0)) {
+        ok = false;
+        ++t;   // tile t was consumed
+        break;
       }
     }
+    cx += TW;
+    if (cx >= g.nx) cx = 0, ++cy;
+    if (++s == stages) s = 0, parity ^= 1u;
   }
   if (!ok && threadIdx.x == 0) {
-    // drain the copies still in flight (iterations it .. issued-1), bounded,
-    // so no bulk copy lands in shared memory after the block has left
-    for (long long j = it; j < issued; ++j) {
-      const uint32_t bar = smem_u32(&bars[j % stages]);
+    // drain the copies still in flight (tiles t .. pt-1), bounded, so no
+    // bulk copy lands in shared memory after the block has left
+    for (int j = t - t0; j < pt - t0; ++j) {
+      const uint32_t bar = smem_u32(&full[j % stages]);
       const uint32_t par = (uint32_t)((j / stages) & 1);
-      const unsigned long long t0 = global_ns();
-      while (!mbar_try_wait(bar, par) && global_ns() - t0 < 1000000000ull) {
+      const unsigned long long tw0 = global_ns();
+      while (!mbar_try_wait(bar, par) && global_ns() - tw0 < 1000000000ull) {
       }
     }
   }
+  if (ok) tile_flagged_segments<S, COLL, FORC, RES>(a, red);
   __syncthreads();
-  if (a.flags & F_RESIDUAL) block_residual<decltype(red[0] + 0)>(a, red);
+  if constexpr (RES) block_residual<float>(a, red);
 }
 
 // ---------------------------------------------------------------------------

@@ -61,13 +61,15 @@ def test_shifted_storage_error_vs_fp64(name):
 
 
 # (kind, nodes per thread, threads per block, stages): every autotuner candidate
-_COMMON = [(2, 0, 256, 4), (2, 0, 512, 3), (2, 0, 256, 2)]
+# kind 2: node pairs from shared-memory tiles of 2048 bytes per plane row
+_TILES = {"fp32_shifted": [(2, 2, 128, 2), (2, 2, 128, 3), (2, 2, 256, 2), (2, 2, 64, 2)],
+          "fp16_shifted": [(2, 2, 256, 2), (2, 2, 256, 3), (2, 2, 512, 2), (2, 2, 128, 2)]}
 _SCALAR = [(0, 1, 128, 0), (0, 1, 256, 0), (0, 1, 128, 1), (0, 1, 256, 1), (0, 1, 128, 2),
            (0, 1, 256, 2)]
 _PAIRS = [(3, 2, 128, 0), (3, 2, 256, 0), (3, 2, 128, 1), (3, 2, 256, 2), (3, 2, 128, 3)]
 SHIFTED_VARIANTS = {
-    "fp32_shifted": _COMMON + [(1, 4, 256, 0), (1, 2, 256, 0)] + _SCALAR + _PAIRS,
-    "fp16_shifted": _COMMON + [(1, 8, 256, 0), (1, 4, 256, 0)] + _SCALAR + _PAIRS,
+    "fp32_shifted": _TILES["fp32_shifted"] + _SCALAR + _PAIRS,
+    "fp16_shifted": _TILES["fp16_shifted"] + _SCALAR + _PAIRS,
 }
 
 
@@ -231,7 +233,7 @@ def test_node_pairs_match_the_scalar_kernel(storage, coll):
     case = Case(workloads.cylinder(nx=512, ny=128, radius=16.0, center=(128, 67), model=coll))
     fluid = ~case.solid
     outs = []
-    for v in ((0, 1, 128, 0), (3, 2, 128, 0), (3, 2, 256, 2), (3, 2, 128, 1)):
+    for v in ((0, 1, 128, 0), (3, 2, 128, 0), (3, 2, 256, 2), (3, 2, 128, 1)) + tuple(_TILES[storage]):
         os.environ["LBM_VARIANT"] = ",".join(str(i) for i in v)
         try:
             with FluidLBM(case, storage=storage) as sim:
@@ -249,3 +251,51 @@ def test_node_pairs_match_the_scalar_kernel(storage, coll):
         assert _rel(u, u0, fluid) <= 1e-6
         np.testing.assert_allclose(a, a0, rtol=1e-6)
         np.testing.assert_allclose(b, b0, rtol=1e-6)
+
+
+@pytest.mark.parametrize("storage", ["fp32_shifted", "fp16_shifted"])
+@pytest.mark.parametrize("coll,forcing", [("BGK", None), ("MRT", None), ("BGK", "guo_second_order")])
+@pytest.mark.parametrize("shape", [(2048 + 96, 70), (1000, 33)])
+def test_tile_kernel_matches_node_pairs(storage, coll, forcing, shape):
+    """The node-pair kernel fed by shared-memory tiles runs the node-pair
+    arithmetic on the same incoming words: in FP32 the same populations and
+    moments bit for bit, on grids that end inside a tile and rows whose tiles
+    straddle the cylinder.  The residual sums are FP32 sums in another order
+    (other blocks), so they agree to a few FP32 roundings."""
+    nx, ny = shape
+    cd = workloads.cylinder(nx=nx, ny=ny, radius=9.0, center=(nx // 3, ny // 2 + 1), model=coll)
+    if forcing:
+        cd["collision_dict"]["fluid"]["forcing_model"] = forcing
+        cd["forcing_dict"] = {"gravity": [2e-6, 0.0]}
+    case = Case(cd)
+    outs = []
+    for v in [(3, 2, 128, 1)] + _TILES[storage]:
+        os.environ["LBM_VARIANT"] = ",".join(str(i) for i in v)
+        try:
+            with FluidLBM(case, storage=storage) as sim:
+                sim.initialize()
+                sim.step(31, residual=True)
+                r1 = sim.residual()
+                sim.step(20, moments=True, residual=True)
+                r2 = sim.residual()
+                assert sim.kernel_variant == v
+                outs.append((sim.moments(), sim.populations(), r1, r2))
+        finally:
+            del os.environ["LBM_VARIANT"]
+    (rho0, u0), p0, a0, b0 = outs[0]
+    fluid = ~case.solid
+    for (rho, u), p, a, b in outs[1:]:
+        if storage == "fp32_shifted":
+            assert np.array_equal(p, p0)
+            assert np.array_equal(rho, rho0) and np.array_equal(u, u0)
+            np.testing.assert_allclose(a, a0, rtol=1e-6)
+            np.testing.assert_allclose(b, b0, rtol=1e-6)
+        else:
+            # FP16: the two kernels may contract the FP32 arithmetic into
+            # FMAs differently, and a last-bit FP32 difference sometimes
+            # rounds a stored half the other way; at the small velocities of
+            # these 51 steps such flips reach FP16's own accuracy, so the
+            # bound is FP16's (a pull or tile error would be of order 1)
+            assert _rel(u, u0, fluid) <= 2e-3
+            np.testing.assert_allclose(a, a0, rtol=1e-2)
+            np.testing.assert_allclose(b, b0, rtol=1e-2)

@@ -2,10 +2,12 @@
 
 Restates, on the CPU, the index arithmetic of the layout (planes of (ny+2)
 rows of `pitch` elements, one guard row before and after the nine planes) and
-of the TMA kernel's bulk-copy windows [x0 - H, x0 + W + H) of rows y - c_y,
-for grids that exercise padding, narrow rows and FP32 / FP16 storage."""
+of the node-pair tile kernel's bulk-copy windows [x0 - H, x0 + TW + H) of rows
+y - c_y and shared-memory words, for grids that exercise padding, narrow rows
+and FP32 / FP16 storage."""
 import pytest
 
+CX = [0, 1, 0, -1, 0, 1, -1, -1, 1]
 CY = [0, 0, 1, 0, -1, 1, 1, -1, -1]
 TMA_ROW_BYTES, HALO_BYTES = 4096, 16
 
@@ -16,37 +18,73 @@ def layout(nx, ny, eb, fp64=False):
     return pitch, (ny + 2) * pitch
 
 
-@pytest.mark.parametrize("nx,ny", [(8192, 2048), (4096, 1024), (24, 16), (1000, 7), (12, 10), (3, 3)])
+TILE_BYTES, SMEM_PER_SM = 2048, 228 * 1024
+
+
+@pytest.mark.parametrize("nx,ny", [(8192, 2048), (4096, 1024), (2144, 70), (24, 16), (1000, 7),
+                                   (12, 10), (3, 3)])
 @pytest.mark.parametrize("eb", [4, 2])
-def test_tma_windows_inside_allocation(nx, ny, eb):
+def test_tile_windows_inside_allocation(nx, ny, eb):
+    """The node-pair tile kernel (kind 2) copies, for tile (y, x0), the rows
+    y - c_ky of every plane over [x0 - H, x0 + TW + H): TW = 2048 bytes of
+    nodes, x0 a multiple of TW below nx, H one 16-byte granule."""
     pitch, plane = layout(nx, ny, eb)
-    W, H = TMA_ROW_BYTES // eb, HALO_BYTES // eb
+    TW, H = TILE_BYTES // eb, HALO_BYTES // eb
     lo, hi = -pitch, 9 * plane + pitch          # allocation, relative to plane 0
-    assert pitch % W == 0
-    for nopull in (False, True):
-        for y in (0, ny - 1):
-            for x0 in range(0, pitch, W):
-                for k in range(9):
-                    dy = 0 if nopull else CY[k]
-                    src = k * plane + (y + 1) * pitch + x0 - dy * pitch - H
-                    assert lo <= src and src + W + 2 * H <= hi
-                    assert (src * eb) % 16 == 0 and ((W + 2 * H) * eb) % 16 == 0
+    assert pitch % TW == 0
+    tpr = (nx + TW - 1) // TW
+    for y in (0, ny - 1):
+        for x0 in range(0, tpr * TW, TW):
+            for k in range(9):
+                src = k * plane + (y + 1) * pitch + x0 - CY[k] * pitch - H
+                assert lo <= src and src + TW + 2 * H <= hi
+                assert (src * eb) % 16 == 0 and ((TW + 2 * H) * eb) % 16 == 0
+
+
+@pytest.mark.parametrize("eb", [4, 2])
+@pytest.mark.parametrize("ppt", [1, 2, 4])
+def test_tile_shared_words_and_blocks(eb, ppt):
+    """Shared-memory words a pair reads stay inside its stage row, and they
+    hold the pulled nodes x - c_kx; the blocks the grid formula asks for fit
+    one SM's shared memory, and the contiguous tile ranges cover every tile
+    once."""
+    TW, H = TILE_BYTES // eb, HALO_BYTES // eb
+    RWW = (TW + 2 * H) // 2
+    block = TW // (2 * ppt)
+    for j in range(TW // 2):
+        wi = H // 2 + j
+        for k in range(9):
+            words = [wi] if CX[k] == 0 else ([wi - 1, wi] if CX[k] == 1 else [wi, wi + 1])
+            assert all(0 <= w < RWW for w in words)
+            # elements (low, high) the pair takes: mid() = high half of the
+            # first word, low half of the second
+            got = [2 * wi, 2 * wi + 1] if CX[k] == 0 else [2 * words[0] + 1, 2 * words[1]]
+            assert got == [2 * j + d - CX[k] + H for d in (0, 1)]
+    for stages in (1, 2, 3, 4):
+        stage = 9 * (TW + 2 * H) * eb
+        smem = stages * stage + 8 * 8 + 32 * 8 * 8 + 1024
+        per_sm = max(min(SMEM_PER_SM // smem, 1024 // block), 1)
+        assert stages * stage <= 227 * 1024
+        assert per_sm * smem <= SMEM_PER_SM or per_sm == 1
+        for ntiles in (1, 7, 16384):
+            grid = min(152 * per_sm, ntiles)
+            cover = []
+            for b in range(grid):
+                cover += range(ntiles * b // grid, ntiles * (b + 1) // grid)
+            assert cover == list(range(ntiles))
 
 
 @pytest.mark.parametrize("nx,ny", [(8192, 2048), (24, 16), (5, 4)])
 @pytest.mark.parametrize("eb,fp64", [(8, True), (4, False), (2, False)])
 def test_shifted_pulls_inside_allocation(nx, ny, eb, fp64):
-    """Vector / scalar pulls of rows y-1..y+1 and columns x-1..x+V (lane 0 /
-    lane 31 extra elements) of every node of every row."""
+    """Scalar pulls of rows y-1..y+1 and columns x-1..x+1 of every node of
+    every row."""
     pitch, plane = layout(nx, ny, eb, fp64)
     lo, hi = -pitch, 9 * plane + pitch
     for k in range(9):
         for y in (0, ny - 1):
             row = k * plane + (y + 1 - CY[k]) * pitch
             assert lo <= row - 1 and row + pitch + 1 <= hi
-
-
-CX = [0, 1, 0, -1, 0, 1, -1, -1, 1]
 
 
 @pytest.mark.parametrize("nx,ny", [(8192, 2048), (4096, 1024), (100, 40), (64, 8), (33, 5)])

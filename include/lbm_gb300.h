@@ -321,8 +321,9 @@ int lbm_time(LbmHandle* h, int64_t* t);
 int lbm_kernel_launches(LbmHandle* h, int64_t* n);
 
 /* Launch shape of the fused step picked by the autotuner on the first step:
- * out = {kind (0 scalar, 1 vector, 2 TMA pipeline, 3 node pairs), nodes per thread,
- * threads per block, shared-memory stages}.  LBM_VARIANT="kind,vec,block,stages"
+ * out = {kind (0 scalar, 2 node pairs from shared-memory tiles, 3 node pairs),
+ * nodes per thread, threads per block, stages (kind 2: shared-memory stages;
+ * kinds 0 and 3: register cap)}.  LBM_VARIANT="kind,vec,block,stages"
  * forces one candidate, LBM_TUNE=0 keeps the first.  (Extension: the
  * reference launches every kernel with 256 threads, backend.py:59-75.) */
 int lbm_kernel_variant(LbmHandle* h, int out[4]);

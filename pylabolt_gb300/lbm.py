@@ -358,7 +358,7 @@ class FluidLBM:
     @property
     def kernel_variant(self):
         """(kind, nodes per thread, threads per block, stages) of the fused
-        step; kind 0 scalar, 1 vector, 2 TMA pipeline, 3 node pairs."""
+        step; kind 0 scalar, 2 node pairs from shared-memory tiles, 3 node pairs."""
         out = (ctypes.c_int * 4)()
         check(self.lib.lbm_kernel_variant(self.h, out))
         return tuple(out[:])

@@ -1,7 +1,8 @@
 """Build recipe for liblbm_gb300.so (in-tree, sm_103a only).
 
 Each translation unit is compiled by nvcc in parallel (one per storage type,
-the shared helpers, the C-ABI and the allocation-free entry); the FP64 unit gets
+the FP32 / FP16 fused step split by collision model, the shared helpers, the
+C-ABI and the allocation-free entry); the FP64 unit gets
 ``--fmad=false`` so that it keeps the reference's rounding.  The result is
 ``pylabolt_gb300/_build/liblbm_gb300.so`` (git-ignored).
 """
@@ -23,7 +24,11 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
 UNITS = {
     "lbm_fp64.cu": ["--fmad=false"],
     "lbm_fp32.cu": [],
+    "lbm_fp32_bgk.cu": [],
+    "lbm_fp32_mrt.cu": [],
     "lbm_fp16.cu": [],
+    "lbm_fp16_bgk.cu": [],
+    "lbm_fp16_mrt.cu": [],
     "lbm_lowp.cu": [],
     "lbm_capi.cu": [],
     "lbm_noalloc.cu": [],

@@ -83,6 +83,9 @@ __global__ void conservation_kernel(const Geom g, const Params p, const S* f,
 }
 
 // ---------------------------------------------------------------------------
+template <class S, int COLL>
+cudaError_t step_coll(int forc, const StepArgs& a, Variant v, int sms, cudaStream_t s);
+
 template <class S>
 struct Kernels {
   using T = typename Store<S>::T;
@@ -151,17 +154,20 @@ struct Kernels {
     return cudaErrorInvalidValue;
   }
 
-  template <int COLL, int FORC, bool RES>
+  // MODE 0: two buffers; 1 / 2: the AA layout's even / odd phase (two pairs
+  // of a tile per thread only)
+  template <int COLL, int FORC, bool RES, int MODE>
   static cudaError_t tile(const StepArgs& a, Variant v, dim3 grid, cudaStream_t s) {
     if constexpr (Store<S>::shifted) {
       const int smem = v.stages * tile_stage_bytes();
       constexpr int TP = kTileBytes / (2 * sizeof(S));   // pairs of a tile
       static int configured[3] = {0, 0, 0};   // bytes the attribute was last raised to
-      if (v.block == TP || v.block == TP / 2 || v.block == TP / 4) {
+      if (v.block == TP / 2 || (MODE == 0 && (v.block == TP || v.block == TP / 4))) {
         const int i = v.block == TP ? 0 : (v.block == TP / 2 ? 1 : 2);
-        const auto kern = i == 0   ? step_tile_pair_kernel<S, COLL, FORC, RES, 1>
-                          : i == 1 ? step_tile_pair_kernel<S, COLL, FORC, RES, 2>
-                                   : step_tile_pair_kernel<S, COLL, FORC, RES, 4>;
+        const auto kern = MODE != 0 ? step_tile_pair_kernel<S, COLL, FORC, RES, 2, MODE>
+                          : i == 0  ? step_tile_pair_kernel<S, COLL, FORC, RES, 1, MODE>
+                          : i == 1  ? step_tile_pair_kernel<S, COLL, FORC, RES, 2, MODE>
+                                    : step_tile_pair_kernel<S, COLL, FORC, RES, 4, MODE>;
         if (smem > configured[i]) {
           cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
           if (e != cudaSuccess) return e;
@@ -179,6 +185,17 @@ struct Kernels {
     const dim3 grid = step_grid(a.g, v, sms, sizeof(S));
     if (a.aa) {   // AA layout: the scalar kernel (capped for shifted storage), one phase
       constexpr int AC = Store<S>::shifted ? (COLL == 0 ? 1 : 2) : 0;
+      if constexpr (Store<S>::shifted) {
+        if (v.kind == 2) {   // node pairs from shared-memory tiles, in place
+          if (v.vec != 2 || v.block != kTileBytes / (4 * (int)sizeof(S)) || v.stages < 1 ||
+              v.stages > kMaxTileStages || a.rho_dyn_out)
+            return cudaErrorInvalidValue;
+          const bool res = (a.flags & F_RESIDUAL) != 0;
+          if (a.aa == 1)
+            return res ? tile<COLL, FORC, true, 1>(a, v, grid, s) : tile<COLL, FORC, false, 1>(a, v, grid, s);
+          return res ? tile<COLL, FORC, true, 2>(a, v, grid, s) : tile<COLL, FORC, false, 2>(a, v, grid, s);
+        }
+      }
       if (v.block > 256) return cudaErrorInvalidValue;
       if (v.kind == 3) return aa_pair<COLL, FORC>(a, v, grid, s);
       if (v.kind != 0) return cudaErrorInvalidValue;
@@ -200,8 +217,8 @@ struct Kernels {
                            v.block != kTileBytes / (8 * (int)sizeof(S))) ||
             v.stages < 1 || v.stages > kMaxTileStages || a.rho_dyn_out)
           return cudaErrorInvalidValue;
-        if (a.flags & F_RESIDUAL) return tile<COLL, FORC, true>(a, v, grid, s);
-        return tile<COLL, FORC, false>(a, v, grid, s);
+        if (a.flags & F_RESIDUAL) return tile<COLL, FORC, true, 0>(a, v, grid, s);
+        return tile<COLL, FORC, false, 0>(a, v, grid, s);
       }
     }
     if (v.kind != 0) return cudaErrorInvalidValue;
@@ -210,14 +227,7 @@ struct Kernels {
   }
   static cudaError_t step(int coll, int forc, const StepArgs& a, Variant v, int sms,
                           cudaStream_t s) {
-    if (coll == 0) {
-      if (forc == 0) return step_t<0, 0>(a, v, sms, s);
-      if (forc == 1) return step_t<0, 1>(a, v, sms, s);
-      return step_t<0, 2>(a, v, sms, s);
-    }
-    if (forc == 0) return step_t<1, 0>(a, v, sms, s);
-    if (forc == 1) return step_t<1, 1>(a, v, sms, s);
-    return step_t<1, 2>(a, v, sms, s);
+    return coll == 0 ? step_coll<S, 0>(forc, a, v, sms, s) : step_coll<S, 1>(forc, a, v, sms, s);
   }
   static cudaError_t init(const Geom& g, const Params& p, const double* rho,
                           const double* u, void* f, void* mr, void* mx, void* my,
@@ -326,5 +336,17 @@ struct Kernels {
     return k;
   }
 };
+
+// One collision model's fused steps for storage S, defined (LBM_STEP_DEFINITIONS)
+// and instantiated only in the units that compile them: lbm_fp64.cu for FP64,
+// lbm_<storage>_{bgk,mrt}.cu for shifted storage, compiled in parallel.
+#ifdef LBM_STEP_DEFINITIONS
+template <class S, int COLL>
+cudaError_t step_coll(int forc, const StepArgs& a, Variant v, int sms, cudaStream_t s) {
+  if (forc == 0) return Kernels<S>::template step_t<COLL, 0>(a, v, sms, s);
+  if (forc == 1) return Kernels<S>::template step_t<COLL, 1>(a, v, sms, s);
+  return Kernels<S>::template step_t<COLL, 2>(a, v, sms, s);
+}
+#endif
 
 }  // namespace lbm

@@ -512,6 +512,14 @@ struct LbmHandle {
     return LBM_OK;
   }
 
+  // The node-pair tile kernel in the AA layout: shifted storage, two pairs
+  // of a tile per thread, 1 to kMaxTileStages stages, no moving obstacles.
+  bool aa_tile_ok(lbm::Variant v) const {
+    return cfg.precision != LBM_FP64 && !mov.n && v.kind == 2 && v.vec == 2 &&
+           v.block == lbm::kTileBytes / (4 * ks->elem_bytes) && v.stages >= 1 &&
+           v.stages <= lbm::kMaxTileStages;
+  }
+
   // Register cap of the scalar AA kernel (0 none for FP64; shifted storage:
   // 1 (32 registers) for BGK, 2 (40) for MRT).
   int aa_scalar_cap() const {
@@ -530,12 +538,17 @@ struct LbmHandle {
     if (const char* f = std::getenv("LBM_VARIANT")) {
       int kind = -1, vec = 0, blk = 0, st = 0;
       if (aa && std::sscanf(f, "%d,%d,%d,%d", &kind, &vec, &blk, &st) == 4) {
+        if (aa_tile_ok(lbm::Variant{kind, vec, blk, st})) {
+          variant = lbm::Variant{kind, vec, blk, st};
+          return LBM_OK;
+        }
         const bool scalar = kind == 0 && vec == 1;
         const bool pairs = kind == 3 && vec == 2 && cfg.precision != LBM_FP64 && st >= 0 && st <= 2;
         if (!(scalar || pairs) || blk < 32 || blk > 256 || blk % 32)
           return fail(LBM_ERR_ARG, std::string("LBM_VARIANT: the AA layout runs the scalar kernel "
                                                "(0,1,block,cap) or, for shifted storage, the node-pair "
-                                               "kernel (3,2,block,cap), 32 <= block <= 256: ") + f);
+                                               "kernel (3,2,block,cap), 32 <= block <= 256, or the tile "
+                                               "kernel (2,2,tile/4 bytes,stages): ") + f);
         if (scalar)
           variant = lbm::Variant{0, 1, blk, aa_scalar_cap()};   // the storage's register cap
         else
@@ -920,14 +933,21 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   h->variant = ks->variants[0];
   if (aa) {
     // no autotuner (a trial launch would advance the state in place): FP64
-    // runs the scalar kernel, shifted storage the node-pair kernel, 128
-    // threads under a 40-register cap, the fastest in a sweep at 8192x2048
-    // (FP32 86.2 GLUPS against 82.8 scalar, FP16 123.5 against 109.7)
-    h->variant = c.precision == LBM_FP64 ? lbm::Variant{0, 1, 128, 0} : lbm::Variant{3, 2, 128, 1};
+    // runs the scalar kernel; FP32 the node-pair kernel, 128 threads under a
+    // 40-register cap (86.2 GLUPS at 8192x2048 against 82.8 scalar and 76.3
+    // from shared-memory tiles); FP16 the node-pair tile kernel, two pairs of
+    // a tile per thread, two stages (139.9 against 125.8 node pairs)
+    h->variant = c.precision == LBM_FP64            ? lbm::Variant{0, 1, 128, 0}
+                 : c.precision == LBM_FP32_SHIFTED ? lbm::Variant{3, 2, 128, 1}
+                                                   : lbm::Variant{2, 2, lbm::kTileBytes / 8, 2};
   }
   long long maxparts = ny;
   for (int i = 0; i < ks->nvariants; ++i) maxparts = std::max(maxparts, h->nparts_of(ks->variants[i]));
-  if (aa) maxparts = std::max(maxparts, h->nparts_of(lbm::Variant{0, 1, 32, 0}));   // smallest AA block
+  if (aa) {
+    maxparts = std::max(maxparts, h->nparts_of(lbm::Variant{0, 1, 32, 0}));   // smallest AA block
+    if (c.precision != LBM_FP64)   // the AA tile kernel's largest grid (one stage)
+      maxparts = std::max(maxparts, h->nparts_of(lbm::Variant{2, 2, lbm::kTileBytes / (4 * (int)eb), 1}));
+  }
   if ((rc = h->alloc(reinterpret_cast<void**>(&h->partials), maxparts * 8 * sizeof(double))) ||
       (rc = h->alloc(reinterpret_cast<void**>(&h->red), 16 * sizeof(double))) ||
       (rc = h->alloc(reinterpret_cast<void**>(&h->scratch), lbm::kFinishBlocks * 8 * sizeof(double))))
@@ -1969,6 +1989,10 @@ StateHeader state_header(const LbmHandle* h) {
 bool valid_variant(const LbmHandle* h, const int32_t v[4], lbm::Variant* out) {
   const lbm::Variant w{v[0], v[1], v[2], v[3]};
   if (h->aa) {
+    if (h->aa_tile_ok(w)) {
+      *out = w;
+      return true;
+    }
     const bool scalar = w.kind == 0 && w.vec == 1;
     const bool pairs = w.kind == 3 && w.vec == 2 && h->cfg.precision != LBM_FP64 && w.stages >= 0 &&
                        w.stages <= 2;

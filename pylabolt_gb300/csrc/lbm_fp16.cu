@@ -1,4 +1,5 @@
-// FP16 shifted-storage instantiation of the fused step and its helpers.
+// FP16 shifted-storage instantiation of the kernel set; the fused step's
+// BGK and MRT instantiations are in lbm_fp16_bgk.cu and lbm_fp16_mrt.cu.
 #include "lbm_aux.cuh"
 
 namespace lbm {

@@ -1207,18 +1207,11 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity,
 // node through step_node.  Every mbarrier wait is bounded in
 // wall-clock time; on expiry the kernel records kErrWaitTimeout, waits
 // (bounded) for its own copies and returns.
-template <class S, int K>
-__device__ __forceinline__ typename PairIO<S>::W tile_pull(const typename PairIO<S>::W* row) {
-  using IO = PairIO<S>;
-  constexpr int cx = CXk(K);
-  if (cx == 0) return row[0];
-  if (cx == 1) return IO::mid(row[-1], row[0]);
-  return IO::mid(row[0], row[1]);
-}
 
 // The flagged segments of the kind-2 kernel: block b takes its share of the
-// segment list, one segment per warp, one node per lane (step_node).
-template <class S, int COLL, int FORC, bool RES>
+// segment list, one segment per warp, one node per lane (step_node, or
+// aa_node in the AA layout's phases: MODE 1 even, 2 odd).
+template <class S, int COLL, int FORC, bool RES, int MODE>
 __device__ __forceinline__ void tile_flagged_segments(const StepArgs& a, float red[7]) {
   const Geom& g = a.g;
   const int f0 = (int)((long long)g.nflag * blockIdx.x / gridDim.x);
@@ -1227,13 +1220,38 @@ __device__ __forceinline__ void tile_flagged_segments(const StepArgs& a, float r
     const int sg = g.seglist[i];
     const int y = sg / g.nseg;
     const int x = (sg - y * g.nseg) * 32 + (int)(threadIdx.x & 31);
-    if (x < g.nx) step_node<S, COLL, FORC, false, RES>(a, x, y, red);
+    if (x >= g.nx) continue;
+    if constexpr (MODE == 0)
+      step_node<S, COLL, FORC, false, RES>(a, x, y, red);
+    else
+      aa_node<S, COLL, FORC, MODE == 2>(a, x, y, red);
   }
 }
 
+// Incoming word of direction K of the pair whose word in direction 0's stage
+// row is `row`: aligned (AA even phase: the nodes' own slots), or pulled
+// from x - c_kx as in pair_pull.
+template <class S, int K, int MODE>
+__device__ __forceinline__ typename PairIO<S>::W tile_pull(const typename PairIO<S>::W* row) {
+  using IO = PairIO<S>;
+  constexpr int cx = MODE == 1 ? 0 : CXk(K);
+  if (cx == 0) return row[0];
+  if (cx == 1) return IO::mid(row[-1], row[0]);
+  return IO::mid(row[0], row[1]);
+}
+
+// The node-pair kernel fed by shared-memory tiles, in three modes: MODE 0
+// two buffers (fin -> fout), MODE 1 / 2 the AA layout's even / odd phase in
+// place (the same slots as step_aa_pair_kernel: the even phase reads a
+// node's own slots of plane k and writes plane kbar; the odd phase pulls
+// plane kbar from x - c_k and pushes plane k to x + c_k).  In the AA phases
+// every slot is read and written by one node only; a tile's copy also brings
+// in slots of neighbouring tiles' nodes, which may be rewritten meanwhile,
+// but those values are never used.
+//
 // PPT: pairs of a tile per thread (blocks of TW / (2 PPT) threads); up to 64
 // registers a thread.
-template <class S, int COLL, int FORC, bool RES, int PPT>
+template <class S, int COLL, int FORC, bool RES, int PPT, int MODE>
 __global__ void __launch_bounds__(kTileBytes / (2 * PPT * sizeof(S)), 2048 * PPT * sizeof(S) / kTileBytes)
     step_tile_pair_kernel(const StepArgs a, int stages) {
   static_assert(Store<S>::shifted, "the tile kernel is for shifted storage");
@@ -1242,35 +1260,44 @@ __global__ void __launch_bounds__(kTileBytes / (2 * PPT * sizeof(S)), 2048 * PPT
   constexpr int TW = kTileBytes / sizeof(S);         // nodes per tile
   constexpr int H = kTmaHaloBytes / sizeof(S);       // halo nodes on each side
   constexpr int RWW = (TW + 2 * H) / 2;              // words of one stage row
-  constexpr uint32_t kCopyBytes = (TW + 2 * H) * sizeof(S);
-  constexpr uint32_t kStageBytes = 9 * kCopyBytes;
+  constexpr uint32_t kStageBytes = 9 * (TW + 2 * H) * sizeof(S);
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long full[kMaxTileStages], empty[kMaxTileStages];
   const Geom& g = a.g;
   float red[7] = {0, 0, 0, 0, 0, 0, 0};
 
-  if (a.flags & F_NOPULL) {   // first step after initialisation: per node
+  if (MODE != 1 && (a.flags & F_NOPULL)) {   // first pulling step after initialisation: per node
     const int npr = (g.nx + 1) / 2;
     const long long total = (long long)g.ny * npr;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
          q += (long long)gridDim.x * blockDim.x) {
       const int y = (int)(q / npr), x0 = 2 * (int)(q % npr);
       if (g.segflag[y * g.nseg + (x0 >> 5)] != 0) continue;   // in the segment list
-      step_node<S, COLL, FORC, false, RES>(a, x0, y, red);
-      step_node<S, COLL, FORC, false, RES>(a, x0 + 1, y, red);
+      if constexpr (MODE == 0) {
+        step_node<S, COLL, FORC, false, RES>(a, x0, y, red);
+        step_node<S, COLL, FORC, false, RES>(a, x0 + 1, y, red);
+      } else {
+        aa_node<S, COLL, FORC, true>(a, x0, y, red);
+        aa_node<S, COLL, FORC, true>(a, x0 + 1, y, red);
+      }
     }
-    tile_flagged_segments<S, COLL, FORC, RES>(a, red);
+    tile_flagged_segments<S, COLL, FORC, RES, MODE>(a, red);
     if constexpr (RES) block_residual<float>(a, red);
     return;
   }
 
   // block b takes the contiguous tiles [t0, t1) in row-major order; the
-  // consumer cursor (cy, cx) and thread 0's copy cursor (py, px) walk them
+  // consumer cursor (cy, cx) and thread 0's copy cursor (py, px) walk them.
+  // A tile's copies span its nodes up to nx rounded up to the copy granule,
+  // plus the halo on both sides (at most one halo past a row's end, inside
+  // the next row or the guard row).
   const int tpr = (g.nx + TW - 1) / TW;
   const int ntiles = g.ny * tpr;
+  const int nxr = (g.nx + H - 1) / H * H;
   const int t0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
   const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
-  const char* fin = static_cast<const char*>(a.fin);
+  const char* src = static_cast<const char*>(MODE == 0 ? a.fin : a.fout);
+  const long long* off = MODE == 0 ? a.off_pull : (MODE == 1 ? a.off_plane : a.off_aa_pull);
   const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     for (int s = 0; s < stages; ++s) {
@@ -1282,12 +1309,14 @@ __global__ void __launch_bounds__(kTileBytes / (2 * PPT * sizeof(S)), 2048 * PPT
   __syncthreads();
 
   auto issue = [&](int y, int x0, int s) {
+    const uint32_t copy = (uint32_t)((min(TW, nxr - x0) + 2 * H) * (int)sizeof(S));
     const uint32_t bar = smem_u32(&full[s]);
-    mbar_expect_tx(bar, kStageBytes);
+    mbar_expect_tx(bar, 9 * copy);
     const uint32_t dst0 = smem_u32(smem_raw + (size_t)s * kStageBytes);
-    const char* src0 = fin + (g.node(x0, y) - H) * (long long)sizeof(S);
+    const char* src0 = src + (g.node(x0, y) - H) * (long long)sizeof(S);
 #pragma unroll
-    for (int k = 0; k < 9; ++k) bulk_g2s(dst0 + k * kCopyBytes, src0 + a.off_pull[k], kCopyBytes, bar);
+    for (int k = 0; k < 9; ++k)
+      bulk_g2s(dst0 + k * (uint32_t)(RWW * sizeof(W)), src0 + off[k], copy, bar);
   };
   int cy = t0 / tpr, cx = (t0 - cy * tpr) * TW;
   int py = cy, px = cx, pt = t0;
@@ -1302,9 +1331,9 @@ __global__ void __launch_bounds__(kTileBytes / (2 * PPT * sizeof(S)), 2048 * PPT
   // Each warp walks the tiles on its own: it waits for a stage's copies
   // (full), works on its pairs and releases the stage (empty, one arrival
   // per warp).  Thread 0 refills a stage once every warp has released it, so
-  // a warp slowed by boundary pairs holds up no other warp until the ring's
-  // other stages are used up.  Waits are bounded and their outcome is made
-  // warp-uniform, so a warp leaves the loop as a whole.
+  // a warp slowed down holds up no other warp until the ring's other stages
+  // are used up.  Waits are bounded and their outcome is made warp-uniform,
+  // so a warp leaves the loop as a whole.
   bool ok = true;
   int t = t0, s = 0;
   uint32_t parity = 0;
@@ -1337,17 +1366,43 @@ __global__ void __launch_bounds__(kTileBytes / (2 * PPT * sizeof(S)), 2048 * PPT
       const long long n = g.node(x0[p], cy);
       const W* row = stage + H / 2 + j;   // the pair's word in direction 0's row
       W w[9];
-      w[0] = tile_pull<S, 0>(row);
-      w[1] = tile_pull<S, 1>(row + 1 * RWW);
-      w[2] = tile_pull<S, 2>(row + 2 * RWW);
-      w[3] = tile_pull<S, 3>(row + 3 * RWW);
-      w[4] = tile_pull<S, 4>(row + 4 * RWW);
-      w[5] = tile_pull<S, 5>(row + 5 * RWW);
-      w[6] = tile_pull<S, 6>(row + 6 * RWW);
-      w[7] = tile_pull<S, 7>(row + 7 * RWW);
-      w[8] = tile_pull<S, 8>(row + 8 * RWW);
+      w[0] = tile_pull<S, 0, MODE>(row);
+      w[1] = tile_pull<S, 1, MODE>(row + 1 * RWW);
+      w[2] = tile_pull<S, 2, MODE>(row + 2 * RWW);
+      w[3] = tile_pull<S, 3, MODE>(row + 3 * RWW);
+      w[4] = tile_pull<S, 4, MODE>(row + 4 * RWW);
+      w[5] = tile_pull<S, 5, MODE>(row + 5 * RWW);
+      w[6] = tile_pull<S, 6, MODE>(row + 6 * RWW);
+      w[7] = tile_pull<S, 7, MODE>(row + 7 * RWW);
+      w[8] = tile_pull<S, 8, MODE>(row + 8 * RWW);
+      const int seg = cy * g.nseg + (x0[p] >> 5);
       char* ob = reinterpret_cast<char*>(static_cast<S*>(a.fout) + n);
-      pair_finish<S, COLL, FORC, RES>(a, n, cy * g.nseg + (x0[p] >> 5), ob, w, o2[p], red);
+      if constexpr (MODE == 0) {
+        pair_finish<S, COLL, FORC, RES>(a, n, seg, ob, w, o2[p], red);
+      } else {
+        float f0[9], f1[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) IO::unpack(w[k], f0[k], f1[k]);
+        float rho0, ux0, uy0, rho1, ux1, uy1;
+        node_update<S, COLL, FORC>(f0, a, n, rho0, ux0, uy0, seg);
+        node_update<S, COLL, FORC>(f1, a, n + 1, rho1, ux1, uy1, seg);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          if (MODE == 1) {   // own slots, plane kbar
+            *reinterpret_cast<W*>(ob + a.off_plane[INVk(k)]) = IO::pack(f0[k], f1[k]);
+          } else {           // pushes to x + c_k of plane k
+            char* tg = ob + a.off_aa_push[k];
+            if (CXk(k) == 0) {
+              *reinterpret_cast<W*>(tg) = IO::pack(f0[k], f1[k]);
+            } else {
+              S* ts = reinterpret_cast<S*>(tg);
+              Store<S>::str(ts, 0, f0[k]);
+              Store<S>::str(ts, 1, f1[k]);
+            }
+          }
+        }
+        pair_outputs<RES>(a, n, rho0, ux0, uy0, rho1, ux1, uy1, red, o2[p]);
+      }
     }
     __syncwarp();   // every lane is done reading stage s
     if (lane == 0) mbar_arrive(smem_u32(&empty[s]));
@@ -1383,7 +1438,7 @@ __global__ void __launch_bounds__(kTileBytes / (2 * PPT * sizeof(S)), 2048 * PPT
       }
     }
   }
-  if (ok) tile_flagged_segments<S, COLL, FORC, RES>(a, red);
+  if (ok) tile_flagged_segments<S, COLL, FORC, RES, MODE>(a, red);
   __syncthreads();
   if constexpr (RES) block_residual<float>(a, red);
 }

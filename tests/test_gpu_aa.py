@@ -214,13 +214,56 @@ def test_aa_node_pairs_match_scalar_aa(storage, coll, monkeypatch):
 
 
 def test_aa_default_launch_shape():
-    """Without LBM_VARIANT the AA layout runs the node-pair kernel for shifted
-    storage and the scalar kernel for FP64."""
+    """Without LBM_VARIANT the AA layout runs the scalar kernel for FP64, the
+    node-pair kernel for FP32 storage and the node-pair tile kernel (two
+    pairs of a 1024-node tile per thread, two stages) for FP16."""
     import os
     assert "LBM_VARIANT" not in os.environ
     case = Case(load_golden("channel_cylinder_abb")[0])
-    for storage, shape in (("fp64", (0, 1, 128, 0)), ("fp32_shifted", (3, 2, 128, 1))):
+    for storage, shape in (("fp64", (0, 1, 128, 0)), ("fp32_shifted", (3, 2, 128, 1)),
+                           ("fp16_shifted", (2, 2, 256, 2))):
         with FluidLBM(case, storage=storage, layout="aa") as sim:
             sim.initialize()
             sim.step(3)
             assert sim.kernel_variant == shape
+
+
+@pytest.mark.parametrize("storage", ["fp32_shifted", "fp16_shifted"])
+@pytest.mark.parametrize("coll,forcing", [("BGK", None), ("MRT", None), ("BGK", "guo_second_order")])
+@pytest.mark.parametrize("shape", [(2144, 70), (1000, 33)])
+def test_aa_tile_kernel_matches_aa_node_pairs(storage, coll, forcing, shape, monkeypatch):
+    """The node-pair tile kernel in the AA layout (the even phase staging a
+    tile's own slots, the odd phase the pulled rows, pushes to global memory)
+    against the AA node-pair kernel, after even and odd step counts with
+    moment and residual steps: FP32 the same populations and moments bit for
+    bit, residuals within FP32 summation order; FP16 within AB_TOL.  The grids
+    end inside a tile, and their rows are not whole tiles (AA rows are
+    padded to 128 bytes)."""
+    nx, ny = shape
+    cd = workloads.cylinder(nx=nx, ny=ny, radius=9.0, center=(nx // 3, ny // 2 + 1), model=coll)
+    if forcing:
+        cd["collision_dict"]["fluid"]["forcing_model"] = forcing
+        cd["forcing_dict"] = {"gravity": [2e-6, 0.0]}
+    case = Case(cd)
+    fluid = ~case.solid
+    tp = 2048 // (2 if storage == "fp16_shifted" else 4) // 2   # pairs of a tile
+    outs = []
+    for v in ("3,2,128,1", f"2,2,{tp // 2},2", f"2,2,{tp // 2},3"):
+        monkeypatch.setenv("LBM_VARIANT", v)
+        with FluidLBM(case, storage=storage, layout="aa") as sim:
+            sim.initialize()
+            res = []
+            for n in (1, 20, 36):
+                sim.step(n, moments=True, residual=True)
+                res.append(sim.residual())
+            assert sim.kernel_variant == tuple(int(i) for i in v.split(","))
+            rho, u = sim.moments()
+            outs.append((rho, u, sim.populations(), np.array(res)))
+    rho0, u0, p0, r0 = outs[0]
+    for rho, u, p, r in outs[1:]:
+        if storage == "fp32_shifted":
+            assert np.array_equal(p, p0)
+            assert np.array_equal(rho, rho0) and np.array_equal(u, u0)
+            np.testing.assert_allclose(r, r0, rtol=1e-6)
+        else:
+            assert np.abs(u - u0)[fluid].max() <= AB_TOL[storage] * np.abs(u0[fluid]).max()

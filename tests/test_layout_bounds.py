@@ -41,6 +41,35 @@ def test_tile_windows_inside_allocation(nx, ny, eb):
                 assert (src * eb) % 16 == 0 and ((TW + 2 * H) * eb) % 16 == 0
 
 
+INV = [0, 3, 4, 1, 2, 7, 8, 5, 6]
+
+
+@pytest.mark.parametrize("nx,ny", [(8192, 2048), (2144, 70), (1000, 33), (100, 7), (24, 16),
+                                   (3, 3)])
+@pytest.mark.parametrize("eb", [4, 2])
+def test_aa_tile_windows_inside_allocation(nx, ny, eb):
+    """The tile kernel in the AA layout: rows padded to 128 bytes with at
+    least one padding column (not whole tiles), copies of [x0 - H,
+    x0 + w + H) with w = min(TW, nx rounded up to the granule - x0): plane k
+    of row y in the even phase, plane kbar of row y - c_ky in the odd one."""
+    align = 128 // eb
+    pitch = (nx + 1 + align - 1) // align * align
+    plane = (ny + 2) * pitch
+    TW, H = TILE_BYTES // eb, HALO_BYTES // eb
+    nxr = (nx + H - 1) // H * H
+    lo, hi = -pitch, 9 * plane + pitch
+    tpr = (nx + TW - 1) // TW
+    for y in (0, ny - 1):
+        for x0 in range(0, tpr * TW, TW):
+            w = min(TW, nxr - x0)
+            assert w >= min(TW, nx - x0) and (w + 2 * H) * eb % 16 == 0
+            for k in range(9):
+                for src in ((k * plane + (y + 1) * pitch + x0 - H),
+                            (INV[k] * plane + (y + 1 - CY[k]) * pitch + x0 - H)):
+                    assert lo <= src and src + w + 2 * H <= hi
+                    assert (src * eb) % 16 == 0
+
+
 @pytest.mark.parametrize("eb", [4, 2])
 @pytest.mark.parametrize("ppt", [1, 2, 4])
 def test_tile_shared_words_and_blocks(eb, ppt):

@@ -914,8 +914,9 @@ __global__ void __launch_bounds__(CAP ? 256 : 512, CAP == 1 ? 8 : (CAP == 2 ? 6 
 // issues as many instructions per node as the FP32 one for half the bytes).
 //
 // A pair whose 32-node row segment holds any boundary, solid or padding node
-// (segflag), and every pair of a no-pull step, takes the per-node scalar path
-// for both nodes, so link records are handled exactly as by step_kernel.
+// (segflag) takes the per-node scalar path for both nodes, so link records
+// are handled exactly as by step_kernel.  On a no-pull step a bulk pair reads
+// its own slots as aligned words.
 template <class S> struct PairIO;
 template <> struct PairIO<__half> {
   using W = uint32_t;
@@ -1019,7 +1020,7 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, floa
   using W = typename IO::W;
   const Geom& g = a.g;
   const int seg = y * g.nseg + (x0 >> 5);
-  if (g.segflag[seg] != 0 || (a.flags & F_NOPULL)) {
+  if (g.segflag[seg] != 0) {
     step_node<S, COLL, FORC, false, RES>(a, x0, y, red);
     if (x0 + 1 < g.nx) step_node<S, COLL, FORC, false, RES>(a, x0 + 1, y, red);
     return;
@@ -1037,15 +1038,20 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, floa
     o2[2] = *reinterpret_cast<const float2*>(static_cast<const float*>(a.uy_old) + n);
   }
   W w[9];
-  w[0] = pair_pull<S, 0>(fb, a.off_pull[0]);
-  w[1] = pair_pull<S, 1>(fb, a.off_pull[1]);
-  w[2] = pair_pull<S, 2>(fb, a.off_pull[2]);
-  w[3] = pair_pull<S, 3>(fb, a.off_pull[3]);
-  w[4] = pair_pull<S, 4>(fb, a.off_pull[4]);
-  w[5] = pair_pull<S, 5>(fb, a.off_pull[5]);
-  w[6] = pair_pull<S, 6>(fb, a.off_pull[6]);
-  w[7] = pair_pull<S, 7>(fb, a.off_pull[7]);
-  w[8] = pair_pull<S, 8>(fb, a.off_pull[8]);
+  if (a.flags & F_NOPULL) {   // the stored populations are the incoming ones: own slots
+#pragma unroll
+    for (int k = 0; k < 9; ++k) w[k] = *reinterpret_cast<const W*>(fb + a.off_plane[k]);
+  } else {
+    w[0] = pair_pull<S, 0>(fb, a.off_pull[0]);
+    w[1] = pair_pull<S, 1>(fb, a.off_pull[1]);
+    w[2] = pair_pull<S, 2>(fb, a.off_pull[2]);
+    w[3] = pair_pull<S, 3>(fb, a.off_pull[3]);
+    w[4] = pair_pull<S, 4>(fb, a.off_pull[4]);
+    w[5] = pair_pull<S, 5>(fb, a.off_pull[5]);
+    w[6] = pair_pull<S, 6>(fb, a.off_pull[6]);
+    w[7] = pair_pull<S, 7>(fb, a.off_pull[7]);
+    w[8] = pair_pull<S, 8>(fb, a.off_pull[8]);
+  }
   pair_finish<S, COLL, FORC, RES>(a, n, seg, ob, w, o2, red);
 }
 
@@ -1198,13 +1204,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity,
 // the next tiles' loads in flight while the block works on the current one,
 // with no registers holding them.  A thread takes node pairs of the tile: it
 // reads the nine incoming words from shared memory (the x shift as in
-// pair_pull), and the arithmetic and the stores are those of the node-pair
-// kernel.  Flagged segments (boundary, solid and padding nodes) are left out
+// pair_pull; aligned own slots on a no-pull step), and the arithmetic and the
+// stores are those of the node-pair kernel.  Flagged segments (boundary,
+// solid and padding nodes) are left out
 // of the tiles: their per-node path (link records, dependent global loads)
 // would hold up the warp that refills the ring and, through it, the block.
 // After its tiles each block works through its share of the list of flagged
-// segments, one node per lane through step_node; a no-pull step runs every
-// node through step_node.  Every mbarrier wait is bounded in
+// segments, one node per lane through step_node.  Every mbarrier wait is bounded in
 // wall-clock time; on expiry the kernel records kErrWaitTimeout, waits
 // (bounded) for its own copies and returns.
 
@@ -1266,20 +1272,19 @@ __global__ void __launch_bounds__(kTileBytes / (2 * PPT * sizeof(S)), 2048 * PPT
   const Geom& g = a.g;
   float red[7] = {0, 0, 0, 0, 0, 0, 0};
 
-  if (MODE != 1 && (a.flags & F_NOPULL)) {   // first pulling step after initialisation: per node
+  // a no-pull step (the first after initialisation) reads every node's own
+  // slots: two buffers run it through the tiles with aligned reads, the AA
+  // odd phase per node
+  const bool nopull = (a.flags & F_NOPULL) != 0;
+  if (MODE == 2 && nopull) {
     const int npr = (g.nx + 1) / 2;
     const long long total = (long long)g.ny * npr;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
          q += (long long)gridDim.x * blockDim.x) {
       const int y = (int)(q / npr), x0 = 2 * (int)(q % npr);
       if (g.segflag[y * g.nseg + (x0 >> 5)] != 0) continue;   // in the segment list
-      if constexpr (MODE == 0) {
-        step_node<S, COLL, FORC, false, RES>(a, x0, y, red);
-        step_node<S, COLL, FORC, false, RES>(a, x0 + 1, y, red);
-      } else {
-        aa_node<S, COLL, FORC, true>(a, x0, y, red);
-        aa_node<S, COLL, FORC, true>(a, x0 + 1, y, red);
-      }
+      aa_node<S, COLL, FORC, true>(a, x0, y, red);
+      aa_node<S, COLL, FORC, true>(a, x0 + 1, y, red);
     }
     tile_flagged_segments<S, COLL, FORC, RES, MODE>(a, red);
     if constexpr (RES) block_residual<float>(a, red);
@@ -1297,7 +1302,8 @@ __global__ void __launch_bounds__(kTileBytes / (2 * PPT * sizeof(S)), 2048 * PPT
   const int t0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
   const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
   const char* src = static_cast<const char*>(MODE == 0 ? a.fin : a.fout);
-  const long long* off = MODE == 0 ? a.off_pull : (MODE == 1 ? a.off_plane : a.off_aa_pull);
+  const long long* off = MODE == 0 ? (nopull ? a.off_plane : a.off_pull)
+                                    : (MODE == 1 ? a.off_plane : a.off_aa_pull);
   const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     for (int s = 0; s < stages; ++s) {
@@ -1366,15 +1372,20 @@ __global__ void __launch_bounds__(kTileBytes / (2 * PPT * sizeof(S)), 2048 * PPT
       const long long n = g.node(x0[p], cy);
       const W* row = stage + H / 2 + j;   // the pair's word in direction 0's row
       W w[9];
-      w[0] = tile_pull<S, 0, MODE>(row);
-      w[1] = tile_pull<S, 1, MODE>(row + 1 * RWW);
-      w[2] = tile_pull<S, 2, MODE>(row + 2 * RWW);
-      w[3] = tile_pull<S, 3, MODE>(row + 3 * RWW);
-      w[4] = tile_pull<S, 4, MODE>(row + 4 * RWW);
-      w[5] = tile_pull<S, 5, MODE>(row + 5 * RWW);
-      w[6] = tile_pull<S, 6, MODE>(row + 6 * RWW);
-      w[7] = tile_pull<S, 7, MODE>(row + 7 * RWW);
-      w[8] = tile_pull<S, 8, MODE>(row + 8 * RWW);
+      if (MODE == 0 && nopull) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) w[k] = row[k * RWW];
+      } else {
+        w[0] = tile_pull<S, 0, MODE>(row);
+        w[1] = tile_pull<S, 1, MODE>(row + 1 * RWW);
+        w[2] = tile_pull<S, 2, MODE>(row + 2 * RWW);
+        w[3] = tile_pull<S, 3, MODE>(row + 3 * RWW);
+        w[4] = tile_pull<S, 4, MODE>(row + 4 * RWW);
+        w[5] = tile_pull<S, 5, MODE>(row + 5 * RWW);
+        w[6] = tile_pull<S, 6, MODE>(row + 6 * RWW);
+        w[7] = tile_pull<S, 7, MODE>(row + 7 * RWW);
+        w[8] = tile_pull<S, 8, MODE>(row + 8 * RWW);
+      }
       const int seg = cy * g.nseg + (x0[p] >> 5);
       char* ob = reinterpret_cast<char*>(static_cast<S*>(a.fout) + n);
       if constexpr (MODE == 0) {

@@ -5,6 +5,8 @@ here from its stated shape and parameters, with seeded random perturbations.
 
 * ``cavity``     lid-driven cavity, BGK, bounce-back walls + moving lid
 * ``poiseuille`` gravity-driven channel, MRT + Guo forcing, periodic in x
+* ``cylinder_shedding`` velocity-inlet channel with a cylinder at Re 100
+  (vortex shedding: Strouhal number and drag coefficient)
 * ``cylinder``   channel with a cylinder, anti-bounce-back pressure inlet /
                  outlet, bounce-back walls and cylinder, seeded +-1e-4 velocity
                  perturbation (numpy default_rng(seed))
@@ -158,6 +160,34 @@ def outlet_channel(nx, ny, outlet_last=True, seed=0):
     else:
         b["outlet"] = outlet
         b["walls"] = walls
+    return c
+
+
+def cylinder_shedding(nx=800, ny=200, diameter=20, u_in=0.1, re=100.0, model="MRT",
+                      storage=None, seed=0, amp=1e-3):
+    """Vortex shedding behind a cylinder: velocity inlet (moving-wall
+    bounce-back at u_in), anti-bounce-back outlet (rho 1), bounce-back walls
+    (blockage diameter / ny), cylinder of the given diameter at (nx/5,
+    ny/2 + 1), Re = u_in * diameter / nu.  Starts from u = (u_in, 0) plus a
+    U(-amp, amp) perturbation per component (default_rng(seed)), rho = 1."""
+    kin_visc = u_in * diameter / re
+    c = _base(nx, ny, kin_visc, model=model, storage=storage,
+              mrt_rates={"s_e": 1.4, "s_eps": 1.4, "s_q": 1.2} if model == "MRT" else None)
+    b = c["boundary_dict"]
+    b["inlet"] = {"wall": False, "segments": [[[0, 0], [0, ny - 1]]],
+                  "fluid": {"type": "fixed_velocity", "value": [float(u_in), 0.0]}}
+    b["outlet"] = {"wall": False, "segments": [[[nx - 1, 0], [nx - 1, ny - 1]]],
+                   "fluid": {"type": "fixed_pressure", "value": 1.0}}
+    b["walls"] = {"wall": True, "segments": [[[0, 0], [nx - 1, 0]],
+                                              [[0, ny - 1], [nx - 1, ny - 1]]],
+                  "fluid": {"type": "bounce_back"}}
+    c["obstacle_dict"]["cylinder"] = {"type": "circle", "radius": diameter / 2.0,
+                                      "center": [nx // 5, ny // 2 + 1],
+                                      "density": 1.0, "static": True}
+    rng = np.random.default_rng(seed)
+    u0 = rng.uniform(-amp, amp, size=(nx, ny, 2))
+    u0[..., 0] += u_in
+    c["initial_fields_dict"]["default"]["fluid"]["velocity"] = {"type": "array", "value": u0}
     return c
 
 

@@ -948,15 +948,16 @@ template <> struct PairIO<float> {
   __device__ static __forceinline__ W pack(float lo, float hi) { return make_float2(lo, hi); }
 };
 
-// Incoming word of direction K for the pair whose plane-0 element is at byte
-// address `fb`: the word `off` bytes away (a plane and c_ky rows), combined
-// with its neighbour for c_kx != 0 (both nodes).
+// Incoming word of direction K for the pair at byte offset `nb` of plane 0:
+// the word at nb from `base` (the buffer plus the direction's plane and c_ky
+// rows, the same for the whole grid), combined with its neighbour for
+// c_kx != 0 (both nodes).
 template <class S, int K>
-__device__ __forceinline__ typename PairIO<S>::W pair_pull(const char* __restrict__ fb, long long off) {
+__device__ __forceinline__ typename PairIO<S>::W pair_pull(const char* __restrict__ base, uint32_t nb) {
   using IO = PairIO<S>;
   using W = typename IO::W;
   constexpr int cx = CXk(K);
-  const W* p = reinterpret_cast<const W*>(fb + off);
+  const W* p = reinterpret_cast<const W*>(base + nb);
   if (cx == 0) return IO::ld(p, 0);
   if (cx == 1) return IO::mid(IO::ld(p, -1), IO::ld(p, 0));
   return IO::mid(IO::ld(p, 0), IO::ld(p, 1));
@@ -1008,8 +1009,11 @@ __device__ __forceinline__ void pair_finish(const StepArgs& a, long long n, int 
   float rho0, ux0, uy0, rho1, ux1, uy1;
   node_update<S, COLL, FORC>(f0, a, n, rho0, ux0, uy0, seg);
   node_update<S, COLL, FORC>(f1, a, n + 1, rho1, ux1, uy1, seg);
+  // plane base (the same for the whole grid) + the node's 32-bit byte offset
+  char* const fo = static_cast<char*>(a.fout);
+  const uint32_t nb = (uint32_t)(n * (long long)sizeof(S));
 #pragma unroll
-  for (int k = 0; k < 9; ++k) *reinterpret_cast<W*>(ob + a.off_plane[k]) = IO::pack(f0[k], f1[k]);
+  for (int k = 0; k < 9; ++k) *reinterpret_cast<W*>(fo + a.off_plane[k] + nb) = IO::pack(f0[k], f1[k]);
   pair_outputs<RES>(a, n, rho0, ux0, uy0, rho1, ux1, uy1, red, o2);
 }
 
@@ -1028,7 +1032,8 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, floa
   // both nodes are bulk nodes: every source is inside the grid
   const int ni = (y + 1) * g.pitch + x0;   // even: pitch and x0 are even
   const long long n = ni;
-  const char* __restrict__ fb = reinterpret_cast<const char*>(static_cast<const S*>(a.fin) + ni);
+  const char* const fi = static_cast<const char*>(a.fin);
+  const uint32_t nb = (uint32_t)ni * (uint32_t)sizeof(S);   // byte offset in a plane
   char* __restrict__ ob = reinterpret_cast<char*>(static_cast<S*>(a.fout) + ni);
   // the previous residual step's fields of both nodes (n even: 8-byte words)
   float2 o2[3];
@@ -1040,17 +1045,17 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, floa
   W w[9];
   if (a.flags & F_NOPULL) {   // the stored populations are the incoming ones: own slots
 #pragma unroll
-    for (int k = 0; k < 9; ++k) w[k] = *reinterpret_cast<const W*>(fb + a.off_plane[k]);
+    for (int k = 0; k < 9; ++k) w[k] = *reinterpret_cast<const W*>(fi + a.off_plane[k] + nb);
   } else {
-    w[0] = pair_pull<S, 0>(fb, a.off_pull[0]);
-    w[1] = pair_pull<S, 1>(fb, a.off_pull[1]);
-    w[2] = pair_pull<S, 2>(fb, a.off_pull[2]);
-    w[3] = pair_pull<S, 3>(fb, a.off_pull[3]);
-    w[4] = pair_pull<S, 4>(fb, a.off_pull[4]);
-    w[5] = pair_pull<S, 5>(fb, a.off_pull[5]);
-    w[6] = pair_pull<S, 6>(fb, a.off_pull[6]);
-    w[7] = pair_pull<S, 7>(fb, a.off_pull[7]);
-    w[8] = pair_pull<S, 8>(fb, a.off_pull[8]);
+    w[0] = pair_pull<S, 0>(fi + a.off_pull[0], nb);
+    w[1] = pair_pull<S, 1>(fi + a.off_pull[1], nb);
+    w[2] = pair_pull<S, 2>(fi + a.off_pull[2], nb);
+    w[3] = pair_pull<S, 3>(fi + a.off_pull[3], nb);
+    w[4] = pair_pull<S, 4>(fi + a.off_pull[4], nb);
+    w[5] = pair_pull<S, 5>(fi + a.off_pull[5], nb);
+    w[6] = pair_pull<S, 6>(fi + a.off_pull[6], nb);
+    w[7] = pair_pull<S, 7>(fi + a.off_pull[7], nb);
+    w[8] = pair_pull<S, 8>(fi + a.off_pull[8], nb);
   }
   pair_finish<S, COLL, FORC, RES>(a, n, seg, ob, w, o2, red);
 }
@@ -1096,21 +1101,22 @@ __global__ void __launch_bounds__(256, CAP == 1 ? 6 : (CAP == 2 ? 4 : 1))
     } else {
       const int ni = (y + 1) * g.pitch + x0;
       const long long n = ni;
-      char* __restrict__ Ab = reinterpret_cast<char*>(static_cast<S*>(a.fout) + ni);   // plane 0 element
+      char* const A = static_cast<char*>(a.fout);
+      const uint32_t nb = (uint32_t)ni * (uint32_t)sizeof(S);   // byte offset in a plane
       W w[9];
       if (!ODD) {
 #pragma unroll
-        for (int k = 0; k < 9; ++k) w[k] = *reinterpret_cast<const W*>(Ab + a.off_plane[k]);
+        for (int k = 0; k < 9; ++k) w[k] = *reinterpret_cast<const W*>(A + a.off_plane[k] + nb);
       } else {
-        w[0] = pair_pull<S, 0>(Ab, a.off_aa_pull[0]);
-        w[1] = pair_pull<S, 1>(Ab, a.off_aa_pull[1]);
-        w[2] = pair_pull<S, 2>(Ab, a.off_aa_pull[2]);
-        w[3] = pair_pull<S, 3>(Ab, a.off_aa_pull[3]);
-        w[4] = pair_pull<S, 4>(Ab, a.off_aa_pull[4]);
-        w[5] = pair_pull<S, 5>(Ab, a.off_aa_pull[5]);
-        w[6] = pair_pull<S, 6>(Ab, a.off_aa_pull[6]);
-        w[7] = pair_pull<S, 7>(Ab, a.off_aa_pull[7]);
-        w[8] = pair_pull<S, 8>(Ab, a.off_aa_pull[8]);
+        w[0] = pair_pull<S, 0>(A + a.off_aa_pull[0], nb);
+        w[1] = pair_pull<S, 1>(A + a.off_aa_pull[1], nb);
+        w[2] = pair_pull<S, 2>(A + a.off_aa_pull[2], nb);
+        w[3] = pair_pull<S, 3>(A + a.off_aa_pull[3], nb);
+        w[4] = pair_pull<S, 4>(A + a.off_aa_pull[4], nb);
+        w[5] = pair_pull<S, 5>(A + a.off_aa_pull[5], nb);
+        w[6] = pair_pull<S, 6>(A + a.off_aa_pull[6], nb);
+        w[7] = pair_pull<S, 7>(A + a.off_aa_pull[7], nb);
+        w[8] = pair_pull<S, 8>(A + a.off_aa_pull[8], nb);
       }
       float f0[9], f1[9];
 #pragma unroll
@@ -1121,11 +1127,11 @@ __global__ void __launch_bounds__(256, CAP == 1 ? 6 : (CAP == 2 ? 4 : 1))
       if (!ODD) {
 #pragma unroll
         for (int k = 0; k < 9; ++k)
-          *reinterpret_cast<W*>(Ab + a.off_plane[INVk(k)]) = IO::pack(f0[k], f1[k]);
+          *reinterpret_cast<W*>(A + a.off_plane[INVk(k)] + nb) = IO::pack(f0[k], f1[k]);
       } else {
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
-          char* t = Ab + a.off_aa_push[k];
+          char* t = A + a.off_aa_push[k] + nb;
           if (CXk(k) == 0) {   // both targets in one word, c_ky rows away
             *reinterpret_cast<W*>(t) = IO::pack(f0[k], f1[k]);
           } else {
@@ -1387,7 +1393,9 @@ __global__ void __launch_bounds__(kTileBytes / (2 * PPT * sizeof(S)), 2048 * PPT
         w[8] = tile_pull<S, 8, MODE>(row + 8 * RWW);
       }
       const int seg = cy * g.nseg + (x0[p] >> 5);
-      char* ob = reinterpret_cast<char*>(static_cast<S*>(a.fout) + n);
+      char* const fo = static_cast<char*>(a.fout);
+      const uint32_t nb = (uint32_t)n * (uint32_t)sizeof(S);   // byte offset in a plane
+      char* ob = fo + nb;
       if constexpr (MODE == 0) {
         pair_finish<S, COLL, FORC, RES>(a, n, seg, ob, w, o2[p], red);
       } else {
@@ -1400,9 +1408,9 @@ __global__ void __launch_bounds__(kTileBytes / (2 * PPT * sizeof(S)), 2048 * PPT
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
           if (MODE == 1) {   // own slots, plane kbar
-            *reinterpret_cast<W*>(ob + a.off_plane[INVk(k)]) = IO::pack(f0[k], f1[k]);
+            *reinterpret_cast<W*>(fo + a.off_plane[INVk(k)] + nb) = IO::pack(f0[k], f1[k]);
           } else {           // pushes to x + c_k of plane k
-            char* tg = ob + a.off_aa_push[k];
+            char* tg = fo + a.off_aa_push[k] + nb;
             if (CXk(k) == 0) {
               *reinterpret_cast<W*>(tg) = IO::pack(f0[k], f1[k]);
             } else {

@@ -995,10 +995,9 @@ __device__ __forceinline__ void pair_outputs(const StepArgs& a, long long n, flo
 }
 
 // Collision, stores and outputs of a bulk pair (nodes n, n + 1) from its
-// nine incoming words; ob: the byte address of node n in plane 0 of fout.
+// nine incoming words.
 template <class S, int COLL, int FORC, bool RES>
 __device__ __forceinline__ void pair_finish(const StepArgs& a, long long n, int seg,
-                                            char* __restrict__ ob,
                                             const typename PairIO<S>::W w[9],
                                             const float2 o2[3], float red[7]) {
   using IO = PairIO<S>;
@@ -1034,7 +1033,6 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, floa
   const long long n = ni;
   const char* const fi = static_cast<const char*>(a.fin);
   const uint32_t nb = (uint32_t)ni * (uint32_t)sizeof(S);   // byte offset in a plane
-  char* __restrict__ ob = reinterpret_cast<char*>(static_cast<S*>(a.fout) + ni);
   // the previous residual step's fields of both nodes (n even: 8-byte words)
   float2 o2[3];
   if (RES) {
@@ -1057,7 +1055,7 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, floa
     w[7] = pair_pull<S, 7>(fi + a.off_pull[7], nb);
     w[8] = pair_pull<S, 8>(fi + a.off_pull[8], nb);
   }
-  pair_finish<S, COLL, FORC, RES>(a, n, seg, ob, w, o2, red);
+  pair_finish<S, COLL, FORC, RES>(a, n, seg, w, o2, red);
 }
 
 // CAP = 1 asks for 6 resident blocks of 256 threads (at most 40 registers),
@@ -1395,9 +1393,8 @@ __global__ void __launch_bounds__(kTileBytes / (2 * PPT * sizeof(S)), 2048 * PPT
       const int seg = cy * g.nseg + (x0[p] >> 5);
       char* const fo = static_cast<char*>(a.fout);
       const uint32_t nb = (uint32_t)n * (uint32_t)sizeof(S);   // byte offset in a plane
-      char* ob = fo + nb;
       if constexpr (MODE == 0) {
-        pair_finish<S, COLL, FORC, RES>(a, n, seg, ob, w, o2[p], red);
+        pair_finish<S, COLL, FORC, RES>(a, n, seg, w, o2[p], red);
       } else {
         float f0[9], f1[9];
 #pragma unroll

@@ -141,12 +141,20 @@ def whole_job_mlups(world, nodes, steps, seconds):
     return world * nodes * steps / seconds / 1e6
 
 
-def cpu_measure(case_dict, steps_budget_s=20.0, max_steps=None, warmup=1):
-    """Times the C restatement of the reference CPU kernels on `case_dict`."""
+def reference_real(storage):
+    """Field type of the reference's own case for a storage: FP64 storage is a
+    "precision": "double" case; FP32 and FP16 storage stand for "precision":
+    "single", whose fields are float32 (pylabolt/base/control.py:36-40)."""
+    return "double" if storage == "fp64" else "float"
+
+
+def cpu_measure(case_dict, steps_budget_s=20.0, max_steps=None, warmup=1, real="double"):
+    """Times the C restatement of the reference CPU kernels on `case_dict`
+    (real: "double", or "float" for a single-precision case)."""
     from oracle.setup import build_state
     from oracle.clib import COracle
     st = build_state(case_dict)
-    co = COracle(st)
+    co = COracle(st, real=real)
     co.initialize()
     co.run(warmup)
     t0 = time.perf_counter()
@@ -189,14 +197,15 @@ def run_reference(args, world, rank):
         return
     from pylabolt_gb300 import workloads  # noqa: F401
     from oracle.clib import build
-    build()
+    real = reference_real(args.storage)
+    build(real=real)
     cores = os.cpu_count()
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     case = workload_case(args, "fp64")
     from oracle.setup import build_state
     from oracle.clib import COracle
     st = build_state(case)
-    co = COracle(st)
+    co = COracle(st, real=real)
     co.initialize()
     co.run(args.warmup)
     # bounded sample: time as many of the K steps as fit in ~90 s
@@ -209,13 +218,14 @@ def run_reference(args, world, rank):
     dt = time.perf_counter() - t0 + one
     nodes = args.nx * args.ny
     mlups = nodes * k / dt / 1e6
+    prec = "FP64" if real == "double" else "FP32 fields (the reference's precision single)"
     sample = (f"{k} of {args.steps} time steps of the full {args.nx}x{args.ny} grid "
-              f"(FP64, 5 unfused sweeps + boundary kernels, OpenMP {cores} threads)")
+              f"({prec}, 5 unfused sweeps + boundary kernels, OpenMP {cores} threads)")
     line = {
         "impl": "reference", "metric": "D2Q9 MLUPS", "value": mlups, "unit": "MLUPS",
         "n_gpus": args.gpus, "steps": k, "warmup": args.warmup,
         "ms_per_step": dt / k * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f64" if real == "double" else "f32", "data": "synthetic",
         "config": {"workload": workload_name(args), "nx": args.nx, "ny": args.ny,
                    "collision": args.collision},
         "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": cores, "kind": "port",
@@ -328,13 +338,16 @@ def run_gb300(args, world, rank, local):
     if rank == 0 and not args.no_cpu_baseline:
         try:
             from oracle.clib import build
-            build()
+            real = reference_real(args.storage)
+            build(real=real)
             cpu_case = workload_case(args, "fp64")
-            mlups_cpu, n_cpu, dt_cpu = cpu_measure(cpu_case, steps_budget_s=15.0, max_steps=200)
+            mlups_cpu, n_cpu, dt_cpu = cpu_measure(cpu_case, steps_budget_s=15.0, max_steps=200,
+                                                   real=real)
+            prec = "FP64" if real == "double" else "FP32 fields, the reference's precision single"
             cpu = {"value": mlups_cpu, "unit": "MLUPS", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"{n_cpu} full time steps of the same {args.nx}x{args.ny} case "
                              f"in {dt_cpu:.1f} s (C restatement of the reference CPU kernels, "
-                             f"FP64, OpenMP)"}
+                             f"{prec}, OpenMP)"}
         except Exception as e:  # reported, never substituted
             cpu = {"value": None, "unit": "MLUPS", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {e}"}

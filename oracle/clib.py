@@ -15,6 +15,7 @@ from .lbm_np import M_MRT, M_INV
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "liblbm_oracle.so")
+LIB_PATH_F32 = os.path.join(BUILD_DIR, "liblbm_oracle_f32.so")
 SRC = os.path.join(HERE, "lbm_oracle.c")
 
 BC_CODES = {"bounce_back": 0, "fixed_velocity": 1, "fixed_pressure": 2,
@@ -22,17 +23,21 @@ BC_CODES = {"bounce_back": 0, "fixed_velocity": 1, "fixed_pressure": 2,
 FORCING_CODES = {None: 0, "guo_linear": 1, "guo_second_order": 2}
 
 
-def build(force=False):
-    """Compile the C oracle (no fused multiply-add, OpenMP over nodes)."""
-    if (not force and os.path.exists(LIB_PATH)
-            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC)):
-        return LIB_PATH
+def build(force=False, real="double"):
+    """Compile the C oracle (no fused multiply-add, OpenMP over nodes).
+    real="float" builds the single-precision variant (float32 fields, the
+    "precision": "single" case) used as a timed CPU baseline."""
+    path = LIB_PATH if real == "double" else LIB_PATH_F32
+    if (not force and os.path.exists(path)
+            and os.path.getmtime(path) >= os.path.getmtime(SRC)):
+        return path
     os.makedirs(BUILD_DIR, exist_ok=True)
-    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    tmp = path + f".tmp{os.getpid()}"
     subprocess.check_call(["gcc", "-O2", "-fno-fast-math", "-ffp-contract=off",
-                           "-fopenmp", "-fPIC", "-shared", SRC, "-o", tmp, "-lm"])
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+                           "-fopenmp", "-fPIC", "-shared", f"-DOR_REAL={real}", SRC,
+                           "-o", tmp, "-lm"])
+    os.replace(tmp, path)
+    return path
 
 
 class OrParams(ctypes.Structure):
@@ -59,18 +64,26 @@ def _ptr(a):
 
 
 class COracle:
-    """Holds a reference-layout state and advances it with the C oracle."""
+    """Holds a reference-layout state and advances it with the C oracle.
+    real="float" runs the single-precision build on float32 copies of the
+    state's fields (``self.f``); the default runs on the state itself."""
 
-    def __init__(self, st):
-        self.lib = ctypes.CDLL(build())
+    def __init__(self, st, real="double"):
+        self.lib = ctypes.CDLL(build(real=real))
         self.st = st
+        self.real = real
+        dt = np.float64 if real == "double" else np.float32
+        self.f = {name: np.ascontiguousarray(getattr(st, name), dtype=dt) if real != "double"
+                  else getattr(st, name)
+                  for name in ("density", "velocity", "force", "pop", "pop_new")}
         p = OrParams()
         p.nxp, p.nyp = st.nxp, st.nyp
         p.collision = 1 if st.collision == "MRT" else 0
         p.forcing = FORCING_CODES[st.forcing]
         p.x_periodic, p.y_periodic = int(st.x_periodic), int(st.y_periodic)
         p.periodic_selfcopy = int(st.periodic_mode == "selfcopy")
-        p.omega, p.inv_cs_2, p.inv_cs_4, p.eps = st.omega, INV_CS_2, INV_CS_4, EPS64
+        eps = EPS64 if real == "double" else float(np.finfo(np.float32).eps)
+        p.omega, p.inv_cs_2, p.inv_cs_4, p.eps = st.omega, INV_CS_2, INV_CS_4, eps
         p.gravity[:] = list(st.gravity)
         p.w[:] = list(W)
         if st.mrt_rates is not None:
@@ -102,32 +115,32 @@ class COracle:
         self.els = (OrElement * max(1, self.nel))(*els)
         self.nodes = np.ascontiguousarray(
             np.concatenate(nodes) if nodes else np.zeros(1, np.int64)).astype(np.int64)
-        self.body = (np.ascontiguousarray(st.body_force)
+        self.body = (np.ascontiguousarray(st.body_force, dtype=dt)
                      if st.body_force is not None else None)
-        self.density_old = np.zeros(st.size)
-        self.velocity_old = np.zeros((st.size, 2))
+        self.density_old = np.zeros(st.size, dtype=dt)
+        self.velocity_old = np.zeros((st.size, 2), dtype=dt)
 
     def initialize(self):
-        st = self.st
+        f = self.f
         self.lib.or_initialize(ctypes.byref(self.p), _ptr(self.idx),
-                               ctypes.c_int64(self.idx.size), _ptr(st.density),
-                               _ptr(st.velocity), _ptr(st.pop), _ptr(st.pop_new))
+                               ctypes.c_int64(self.idx.size), _ptr(f["density"]),
+                               _ptr(f["velocity"]), _ptr(f["pop"]), _ptr(f["pop_new"]))
 
     def run(self, nsteps):
-        st = self.st
+        f = self.f
         self.lib.or_run(ctypes.byref(self.p), _ptr(self.idx),
                         ctypes.c_int64(self.idx.size), _ptr(self.solid),
-                        _ptr(st.density), _ptr(st.velocity), _ptr(st.force),
-                        _ptr(st.pop), _ptr(st.pop_new),
+                        _ptr(f["density"]), _ptr(f["velocity"]), _ptr(f["force"]),
+                        _ptr(f["pop"]), _ptr(f["pop_new"]),
                         _ptr(self.body) if self.body is not None else None,
                         self.els, ctypes.c_int32(self.nel), _ptr(self.nodes),
                         ctypes.c_int64(nsteps))
 
     def residue(self):
         """Residuals (res_rho, res_ux, res_uy) -- pylabolt/utils/residues.py:171-222."""
-        st = self.st
+        f = self.f
         out = np.zeros(6)
         self.lib.or_residue(_ptr(self.idx), ctypes.c_int64(self.idx.size),
-                            _ptr(st.density), _ptr(st.velocity),
+                            _ptr(f["density"]), _ptr(f["velocity"]),
                             _ptr(self.density_old), _ptr(self.velocity_old), _ptr(out))
         return np.sqrt(out[0::2] / (out[1::2] + EPS64))

@@ -2,8 +2,9 @@
  * C restatement of the pylabolt fluidLB CPU kernels -- TEST INFRASTRUCTURE.
  *
  * Used by the tests as the FP64 oracle for cases too large for the NumPy
- * restatement, and by bench.py as the timed CPU baseline.  It is never linked
- * into or called by the product library.
+ * restatement, and by bench.py as the timed CPU baseline (FP64, or the FP32
+ * build for single-precision workloads).  It is never linked into or called
+ * by the product library.
  *
  * It keeps the reference's structure: padded AoS populations [node][9], node
  * index x*(Ny+2)+y, one parallel sweep per reference kernel (OpenMP over nodes,
@@ -25,6 +26,18 @@
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
+
+/* Type of the fields and of the per-node arithmetic: double for the FP64
+ * oracle; float (-DOR_REAL=float) for the "precision": "single" case, whose
+ * state.fields arrays are float32 (pylabolt/base/control.py:36-40,
+ * pylabolt/base/fields.py:64-92), timed as the CPU baseline of
+ * single-precision workloads.  As in the reference's Numba kernels on float32
+ * arrays, double-precision constants promote the expressions they appear in;
+ * the residue sums stay in double. */
+#ifndef OR_REAL
+#define OR_REAL double
+#endif
+typedef OR_REAL real;
 
 static const int CX[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
 static const int CY[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
@@ -54,15 +67,15 @@ typedef struct {
 } OrElement;
 
 static void compute_moments(const OrParams *p, const int64_t *idx, int64_t n,
-                            const double *pop_new, double *density,
-                            double *velocity, double *force,
-                            const double *body_force) {
+                            const real *pop_new, real *density,
+                            real *velocity, real *force,
+                            const real *body_force) {
     int64_t t;
 #pragma omp parallel for schedule(static)
     for (t = 0; t < n; ++t) {
         int64_t ind = idx[t];
-        const double *f = pop_new + 9 * ind;
-        double s = 0.;
+        const real *f = pop_new + 9 * ind;
+        real s = 0.;
         for (int k = 0; k < 9; ++k) s += f[k];
         density[ind] = s;
     }
@@ -73,7 +86,7 @@ static void compute_moments(const OrParams *p, const int64_t *idx, int64_t n,
             force[2 * ind] = body_force[2 * ind];
             force[2 * ind + 1] = body_force[2 * ind + 1];
         } else {
-            double r = density[ind];
+            real r = density[ind];
             force[2 * ind] = r * p->gravity[0];
             force[2 * ind + 1] = r * p->gravity[1];
         }
@@ -81,52 +94,52 @@ static void compute_moments(const OrParams *p, const int64_t *idx, int64_t n,
 #pragma omp parallel for schedule(static)
     for (t = 0; t < n; ++t) {
         int64_t ind = idx[t];
-        const double *f = pop_new + 9 * ind;
-        double sx = 0., sy = 0.;
+        const real *f = pop_new + 9 * ind;
+        real sx = 0., sy = 0.;
         for (int k = 0; k < 9; ++k) {
-            sx += (double)CX[k] * f[k];
-            sy += (double)CY[k] * f[k];
+            sx += (real)CX[k] * f[k];
+            sy += (real)CY[k] * f[k];
         }
-        double inv_density = 1 / (density[ind] + p->eps);
+        real inv_density = 1 / (density[ind] + p->eps);
         velocity[2 * ind] = sx * inv_density + 0.5 * force[2 * ind] * inv_density;
         velocity[2 * ind + 1] = sy * inv_density + 0.5 * force[2 * ind + 1] * inv_density;
     }
 }
 
-static inline double feq_k(const OrParams *p, int k, double rho, double ux,
-                           double uy, double u2) {
-    double cu = (double)CX[k] * ux + (double)CY[k] * uy;
+static inline real feq_k(const OrParams *p, int k, real rho, real ux,
+                           real uy, real u2) {
+    real cu = (real)CX[k] * ux + (real)CY[k] * uy;
     return p->w[k] * rho *
            (1 + p->inv_cs_2 * cu + 0.5 * p->inv_cs_4 * cu * cu - 0.5 * p->inv_cs_2 * u2);
 }
 
-static inline double guo_k(const OrParams *p, int k, double ux, double uy,
-                           double fx, double fy) {
+static inline real guo_k(const OrParams *p, int k, real ux, real uy,
+                           real fx, real fy) {
     if (p->forcing == 1)
-        return p->w[k] * ((double)CX[k] * fx + (double)CY[k] * fy) * p->inv_cs_2;
-    double cu = (double)CX[k] * ux + (double)CY[k] * uy;
-    double const_x = ((double)CX[k] - ux) * p->inv_cs_2 + cu * (double)CX[k] * p->inv_cs_4;
-    double const_y = ((double)CY[k] - uy) * p->inv_cs_2 + cu * (double)CY[k] * p->inv_cs_4;
+        return p->w[k] * ((real)CX[k] * fx + (real)CY[k] * fy) * p->inv_cs_2;
+    real cu = (real)CX[k] * ux + (real)CY[k] * uy;
+    real const_x = ((real)CX[k] - ux) * p->inv_cs_2 + cu * (real)CX[k] * p->inv_cs_4;
+    real const_y = ((real)CY[k] - uy) * p->inv_cs_2 + cu * (real)CY[k] * p->inv_cs_4;
     return p->w[k] * (const_x * fx + const_y * fy);
 }
 
 static void collide(const OrParams *p, const int64_t *idx, int64_t n,
-                    const double *density, const double *velocity,
-                    const double *force, double *pop, const double *pop_new) {
+                    const real *density, const real *velocity,
+                    const real *force, real *pop, const real *pop_new) {
     int64_t t;
-    const double omega = p->omega;
+    const real omega = p->omega;
 #pragma omp parallel for schedule(static)
     for (t = 0; t < n; ++t) {
         int64_t ind = idx[t];
-        double rho = density[ind];
-        double ux = velocity[2 * ind], uy = velocity[2 * ind + 1];
-        double fx = force[2 * ind], fy = force[2 * ind + 1];
-        double u2 = ux * ux + uy * uy;
-        const double *fn = pop_new + 9 * ind;
-        double *fo = pop + 9 * ind;
+        real rho = density[ind];
+        real ux = velocity[2 * ind], uy = velocity[2 * ind + 1];
+        real fx = force[2 * ind], fy = force[2 * ind + 1];
+        real u2 = ux * ux + uy * uy;
+        const real *fn = pop_new + 9 * ind;
+        real *fo = pop + 9 * ind;
         if (p->collision == 0) {
             for (int k = 0; k < 9; ++k) {
-                double pop_eq = feq_k(p, k, rho, ux, uy, u2);
+                real pop_eq = feq_k(p, k, rho, ux, uy, u2);
                 if (p->forcing == 0)
                     fo[k] = (1 - omega) * fn[k] + omega * pop_eq;
                 else
@@ -134,13 +147,13 @@ static void collide(const OrParams *p, const int64_t *idx, int64_t n,
                             (1 - 0.5 * omega) * guo_k(p, k, ux, uy, fx, fy);
             }
         } else {
-            double m[9], meq[9], mf[9], fe[9], fb[9], ms[9];
+            real m[9], meq[9], mf[9], fe[9], fb[9], ms[9];
             for (int k = 0; k < 9; ++k) {
                 fe[k] = feq_k(p, k, rho, ux, uy, u2);
                 fb[k] = p->forcing ? guo_k(p, k, ux, uy, fx, fy) : 0.0;
             }
             for (int a = 0; a < 9; ++a) {
-                double s0 = 0, s1 = 0, s2 = 0;
+                real s0 = 0, s1 = 0, s2 = 0;
                 for (int k = 0; k < 9; ++k) {
                     s0 += p->m[9 * a + k] * fn[k];
                     s1 += p->m[9 * a + k] * fe[k];
@@ -151,7 +164,7 @@ static void collide(const OrParams *p, const int64_t *idx, int64_t n,
             for (int a = 0; a < 9; ++a)
                 ms[a] = m[a] - p->mrt_s[a] * (m[a] - meq[a]) + (1 - 0.5 * p->mrt_s[a]) * mf[a];
             for (int k = 0; k < 9; ++k) {
-                double s = 0;
+                real s = 0;
                 for (int a = 0; a < 9; ++a) s += p->minv[9 * k + a] * ms[a];
                 fo[k] = s;
             }
@@ -159,7 +172,7 @@ static void collide(const OrParams *p, const int64_t *idx, int64_t n,
     }
 }
 
-static void halo(const OrParams *p, double *pop) {
+static void halo(const OrParams *p, real *pop) {
     const int64_t nxp = p->nxp, nyp = p->nyp;
     if (p->x_periodic) {
         int64_t sl = p->periodic_selfcopy ? 1 : nxp - 2;
@@ -182,14 +195,14 @@ static void halo(const OrParams *p, double *pop) {
 }
 
 static void stream(const OrParams *p, const int64_t *idx, int64_t n,
-                   const uint8_t *solid, const double *density,
-                   const double *velocity, const double *pop, double *pop_new) {
+                   const uint8_t *solid, const real *density,
+                   const real *velocity, const real *pop, real *pop_new) {
     int64_t t;
     const int64_t nyp = p->nyp;
 #pragma omp parallel for schedule(static)
     for (t = 0; t < n; ++t) {
         int64_t ind = idx[t];
-        double density_local = density[ind];
+        real density_local = density[ind];
         pop_new[9 * ind] = pop[9 * ind];
         for (int k = 1; k < 9; ++k) {
             int64_t nb = ind - CX[k] * nyp - CY[k];
@@ -197,9 +210,9 @@ static void stream(const OrParams *p, const int64_t *idx, int64_t n,
                 pop_new[9 * ind + k] = pop[9 * nb + k];
             } else {
                 int ki = INVD[k];
-                double temp = 2 * p->w[ki] * density_local * p->inv_cs_2 *
-                              ((double)CX[ki] * velocity[2 * nb] +
-                               (double)CY[ki] * velocity[2 * nb + 1]);
+                real temp = 2 * p->w[ki] * density_local * p->inv_cs_2 *
+                              ((real)CX[ki] * velocity[2 * nb] +
+                               (real)CY[ki] * velocity[2 * nb + 1]);
                 pop_new[9 * ind + k] = pop[9 * ind + ki] - temp;
             }
         }
@@ -208,8 +221,8 @@ static void stream(const OrParams *p, const int64_t *idx, int64_t n,
 
 static void boundaries(const OrParams *p, const OrElement *el, int32_t nel,
                        const int64_t *nodes, const uint8_t *solid,
-                       const double *density, const double *velocity,
-                       const double *pop, double *pop_new) {
+                       const real *density, const real *velocity,
+                       const real *pop, real *pop_new) {
     const int64_t nyp = p->nyp, nxp = p->nxp;
     for (int32_t e = 0; e < nel; ++e) {
         const OrElement *E = el + e;
@@ -222,23 +235,23 @@ static void boundaries(const OrParams *p, const OrElement *el, int32_t nel,
                 for (int k = 0; k < 3; ++k)
                     pop_new[9 * ind + E->inv_list[k]] = pop[9 * ind + E->out_list[k]];
             } else if (E->type == 1) {
-                double density_local = density[ind];
+                real density_local = density[ind];
                 for (int k = 0; k < 3; ++k) {
                     int o = E->out_list[k], i = E->inv_list[k];
-                    double temp = 2 * p->w[o] * density_local * p->inv_cs_2 *
-                                  ((double)CX[o] * E->value[0] + (double)CY[o] * E->value[1]);
+                    real temp = 2 * p->w[o] * density_local * p->inv_cs_2 *
+                                  ((real)CX[o] * E->value[0] + (real)CY[o] * E->value[1]);
                     pop_new[9 * ind + i] = pop[9 * ind + o] - temp;
                 }
             } else if (E->type == 2) {
                 int64_t nrm = ind + E->normal[0] * nyp + E->normal[1];
-                double ux = velocity[2 * ind], uy = velocity[2 * ind + 1];
-                double uex = ux + 0.5 * (ux - velocity[2 * nrm]);
-                double uey = uy + 0.5 * (uy - velocity[2 * nrm + 1]);
-                double u2 = uex * uex + uey * uey;
+                real ux = velocity[2 * ind], uy = velocity[2 * ind + 1];
+                real uex = ux + 0.5 * (ux - velocity[2 * nrm]);
+                real uey = uy + 0.5 * (uy - velocity[2 * nrm + 1]);
+                real u2 = uex * uex + uey * uey;
                 for (int k = 0; k < 3; ++k) {
                     int o = E->out_list[k], i = E->inv_list[k];
-                    double cu = (double)CX[o] * uex + (double)CY[o] * uey;
-                    double temp = 2 * p->w[o] * E->value[0] *
+                    real cu = (real)CX[o] * uex + (real)CY[o] * uey;
+                    real temp = 2 * p->w[o] * E->value[0] *
                                   (1 + 0.5 * p->inv_cs_4 * cu * cu - 0.5 * p->inv_cs_2 * u2);
                     pop_new[9 * ind + i] = -pop[9 * ind + o] + temp;
                 }
@@ -266,16 +279,16 @@ static void boundaries(const OrParams *p, const OrElement *el, int32_t nel,
 
 /* Initial equilibrium -- pylabolt/parallel/cpu/equilibrium_kernels.py:38-78 */
 void or_initialize(const OrParams *p, const int64_t *idx, int64_t n,
-                   const double *density, const double *velocity, double *pop,
-                   double *pop_new) {
+                   const real *density, const real *velocity, real *pop,
+                   real *pop_new) {
     int64_t t;
 #pragma omp parallel for schedule(static)
     for (t = 0; t < n; ++t) {
         int64_t ind = idx[t];
-        double ux = velocity[2 * ind], uy = velocity[2 * ind + 1];
-        double u2 = ux * ux + uy * uy;
+        real ux = velocity[2 * ind], uy = velocity[2 * ind + 1];
+        real u2 = ux * ux + uy * uy;
         for (int k = 0; k < 9; ++k) {
-            double v = feq_k(p, k, density[ind], ux, uy, u2);
+            real v = feq_k(p, k, density[ind], ux, uy, u2);
             pop[9 * ind + k] = v;
             pop_new[9 * ind + k] = v;
         }
@@ -284,9 +297,9 @@ void or_initialize(const OrParams *p, const int64_t *idx, int64_t n,
 
 /* nsteps of Solver.single_time_step (pylabolt/solvers/fluidLB.py:206-253). */
 void or_run(const OrParams *p, const int64_t *idx, int64_t n,
-            const uint8_t *solid, double *density, double *velocity,
-            double *force, double *pop, double *pop_new,
-            const double *body_force, const OrElement *el, int32_t nel,
+            const uint8_t *solid, real *density, real *velocity,
+            real *force, real *pop, real *pop_new,
+            const real *body_force, const OrElement *el, int32_t nel,
             const int64_t *nodes, int64_t nsteps) {
     for (int64_t s = 0; s < nsteps; ++s) {
         compute_moments(p, idx, n, pop_new, density, velocity, force, body_force);
@@ -299,19 +312,19 @@ void or_run(const OrParams *p, const int64_t *idx, int64_t n,
 
 /* Residue sums in node order; updates the old fields.
  * out = {num_rho, den_rho, num_ux, den_ux, num_uy, den_uy}. */
-void or_residue(const int64_t *idx, int64_t n, const double *density,
-                const double *velocity, double *density_old,
-                double *velocity_old, double *out) {
+void or_residue(const int64_t *idx, int64_t n, const real *density,
+                const real *velocity, real *density_old,
+                real *velocity_old, double *out) {
     double s[6] = {0, 0, 0, 0, 0, 0};
     for (int64_t t = 0; t < n; ++t) {
         int64_t ind = idx[t];
-        double d = density[ind] - density_old[ind];
+        double d = (double)density[ind] - (double)density_old[ind];
         s[0] += d * d;
-        s[1] += density_old[ind] * density_old[ind];
+        s[1] += (double)density_old[ind] * (double)density_old[ind];
         density_old[ind] = density[ind];
         for (int c = 0; c < 2; ++c) {
             double o = velocity_old[2 * ind + c];
-            double v = velocity[2 * ind + c] - o;
+            double v = (double)velocity[2 * ind + c] - o;
             s[2 + 2 * c] += v * v;
             s[3 + 2 * c] += o * o;
             velocity_old[2 * ind + c] = velocity[2 * ind + c];

@@ -182,7 +182,7 @@ struct Kernels {
 
   template <int COLL, int FORC>
   static cudaError_t step_t(const StepArgs& a, Variant v, int sms, cudaStream_t s) {
-    const dim3 grid = step_grid(a.g, v, sms, sizeof(S));
+    const dim3 grid = step_grid(a.g, v, sms, sizeof(S), (a.flags & F_RESIDUAL) != 0);
     if (a.aa) {   // AA layout: the scalar kernel (capped for shifted storage), one phase
       constexpr int AC = Store<S>::shifted ? (COLL == 0 ? 1 : 2) : 0;
       if constexpr (Store<S>::shifted) {

@@ -527,7 +527,7 @@ struct LbmHandle {
   }
 
   long long nparts_of(lbm::Variant v) const {
-    const dim3 gr = lbm::step_grid(g, v, sms, ks->elem_bytes);
+    const dim3 gr = lbm::step_grid(g, v, sms, ks->elem_bytes, true);   // residual launches
     return (long long)gr.x * gr.y;
   }
 

@@ -271,16 +271,16 @@ cudaError_t finish_reduce(const double* partials, long long nrows, double* scrat
 // Shared memory of one stage of the kind-2 kernel (nine halo-padded row windows).
 inline int tile_stage_bytes() { return 9 * (kTileBytes + 2 * kTmaHaloBytes); }
 // Number of SMs of the current device (cached by the caller's handle).
-// grid of the fused step for variant v (`sms` multiprocessors).  Kind 2 is
-// persistent: as many blocks as are sure to be resident at once -- shared
-// memory per block (stages, the static barriers and residual rows, and the
-// 1 KB the runtime reserves) and the 1024 threads per SM its launch bounds
-// guarantee registers for.
-inline dim3 step_grid(const Geom& g, Variant v, int sms, int elem_bytes) {
+// grid of the fused step for variant v (`sms` multiprocessors; res: a
+// residual launch).  Kind 2 is persistent: as many blocks as are sure to be
+// resident at once -- shared memory per block (stages, the static barriers,
+// the residual rows of a residual launch, and the 1 KB the runtime reserves)
+// and the 1024 threads per SM its launch bounds guarantee registers for.
+inline dim3 step_grid(const Geom& g, Variant v, int sms, int elem_bytes, bool res) {
   if (v.kind == 2) {
     const int tw = kTileBytes / elem_bytes;
     const long long tiles = (long long)g.ny * ((g.nx + tw - 1) / tw);
-    const int smem = v.stages * tile_stage_bytes() + 8 * kMaxTileStages + 32 * 8 * 8 + 1024;
+    const int smem = v.stages * tile_stage_bytes() + 2 * 8 * kMaxTileStages + (res ? 16 * 8 * 8 : 0) + 1024;
     int per_sm = kSmemPerSM / smem;
     if (per_sm * v.block > 1024) per_sm = 1024 / v.block;   // 64 registers a thread
     if (per_sm < 1) per_sm = 1;

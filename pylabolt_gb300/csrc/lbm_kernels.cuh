@@ -687,7 +687,7 @@ __device__ __forceinline__ R warp_sum8(const R v[8]) {
 
 template <class T>
 __device__ __forceinline__ void block_residual(const StepArgs& a, T red[7]) {
-  __shared__ double sh[32][8];
+  __shared__ double sh[16][8];   // one row per warp: blocks of at most 512 threads
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const T v[8] = {red[0], red[1], red[2], red[3], red[4], red[5], red[6], T(0)};
   const T s = warp_sum8<T>(v);

@@ -89,9 +89,11 @@ def test_tile_shared_words_and_blocks(eb, ppt):
             # first word, low half of the second
             got = [2 * wi, 2 * wi + 1] if CX[k] == 0 else [2 * words[0] + 1, 2 * words[1]]
             assert got == [2 * j + d - CX[k] + H for d in (0, 1)]
-    for stages in (1, 2, 3, 4):
+    for stages, res in ((1, False), (2, True), (3, False), (3, True), (4, False)):
         stage = 9 * (TW + 2 * H) * eb
-        smem = stages * stage + 8 * 8 + 32 * 8 * 8 + 1024
+        # stages, the full/empty barriers, the residual rows (16 warps x 8
+        # doubles) of a residual launch, the runtime's 1 KB per block
+        smem = stages * stage + 2 * 8 * 8 + (16 * 8 * 8 if res else 0) + 1024
         per_sm = max(min(SMEM_PER_SM // smem, 1024 // block), 1)
         assert stages * stage <= 227 * 1024
         assert per_sm * smem <= SMEM_PER_SM or per_sm == 1

@@ -118,10 +118,16 @@ struct Kernels {
     return cudaGetLastError();
   }
 
-  // The node-pair kernel (stages = register cap: 0 none, 1 40, 2 64, 3 32).
+  // The node-pair kernel (stages = register cap: 0 none, 1 40, 2 64, 3 32);
+  // with moving obstacles (rho_dyn_out) the 40-register shape only.
   template <int COLL, int FORC, bool RES>
   static cudaError_t pair(const StepArgs& a, Variant v, dim3 grid, cudaStream_t s) {
     if constexpr (Store<S>::shifted) {
+      if (a.rho_dyn_out) {
+        if (v.stages != 1) return cudaErrorInvalidValue;
+        step_pair_kernel<S, COLL, FORC, 1, RES, true><<<grid, v.block, 0, s>>>(a);
+        return cudaGetLastError();
+      }
       switch (v.stages) {
         case 0: step_pair_kernel<S, COLL, FORC, 0, RES><<<grid, v.block, 0, s>>>(a); break;
         case 1: step_pair_kernel<S, COLL, FORC, 1, RES><<<grid, v.block, 0, s>>>(a); break;
@@ -206,8 +212,8 @@ struct Kernels {
       return cudaGetLastError();
     }
     if constexpr (Store<S>::shifted) {
-      if (v.kind == 3) {   // node pairs (not for moving obstacles: class-4 nodes)
-        if (v.vec != 2 || v.block > 256 || a.rho_dyn_out) return cudaErrorInvalidValue;
+      if (v.kind == 3) {   // node pairs (moving obstacles: the 40-register shape)
+        if (v.vec != 2 || v.block > 256) return cudaErrorInvalidValue;
         if (a.flags & F_RESIDUAL) return pair<COLL, FORC, true>(a, v, grid, s);
         return pair<COLL, FORC, false>(a, v, grid, s);
       }

@@ -324,8 +324,8 @@ struct LbmHandle {
       for (int i = 0; i < ks->nvariants && rc == LBM_OK; ++i) {
         const lbm::Variant v = ks->variants[i];
         // every kernel has a residual instantiation; moving obstacles take
-        // the scalar one
-        if (v.kind != 0 && mov.n) continue;
+        // the scalar one or the 40-register pairs
+        if (mov.n && !mov_ok(v)) continue;
         if ((rc = launch_v(lbm::F_RESIDUAL, v, false))) break;
         cudaEventRecord(e0, stream);
         for (int r = 0; r < 4 && rc == LBM_OK; ++r) rc = launch_v(lbm::F_RESIDUAL, v, false);
@@ -512,6 +512,14 @@ struct LbmHandle {
     return LBM_OK;
   }
 
+  // Kernels that handle moving obstacles (class-4 links on the per-node path,
+  // the densities their bounce-back reads): the scalar kernel, and the
+  // node-pair kernel's 40-register shape, whose flagged segments take the
+  // scalar body.
+  bool mov_ok(lbm::Variant v) const {
+    return v.kind == 0 || (v.kind == 3 && v.vec == 2 && v.stages == 1);
+  }
+
   // The node-pair tile kernel in the AA layout: shifted storage, two pairs
   // of a tile per thread, 1 to kMaxTileStages stages, no moving obstacles.
   bool aa_tile_ok(lbm::Variant v) const {
@@ -559,8 +567,9 @@ struct LbmHandle {
         for (int i = 0; i < ks->nvariants; ++i)
           if (ks->variants[i].kind == kind && ks->variants[i].vec == vec &&
               ks->variants[i].block == blk && ks->variants[i].stages == st) {
-            if (mov.n && kind != 0)
-              return fail(LBM_ERR_ARG, "LBM_VARIANT: moving obstacles need the scalar kernel (kind 0)");
+            if (mov.n && !mov_ok(ks->variants[i]))
+              return fail(LBM_ERR_ARG, "LBM_VARIANT: moving obstacles need the scalar kernel (kind 0) "
+                                       "or the node-pair kernel with a 40-register cap (3,2,block,1)");
             variant = ks->variants[i];
             return LBM_OK;
           }
@@ -585,7 +594,7 @@ struct LbmHandle {
     int rc = LBM_OK;
     for (int i = 0; i < ks->nvariants && rc == LBM_OK; ++i) {
       const lbm::Variant v = ks->variants[i];
-      if (mov.n && v.kind != 0) {   // class-4 links: the scalar kernel only
+      if (mov.n && !mov_ok(v)) {   // class-4 links: the scalar kernel or 40-register pairs
         tune_ms[i] = 1e30;
         continue;
       }
@@ -2003,7 +2012,7 @@ bool valid_variant(const LbmHandle* h, const int32_t v[4], lbm::Variant* out) {
   for (int i = 0; i < h->ks->nvariants; ++i) {
     const lbm::Variant& c = h->ks->variants[i];
     if (c.kind == w.kind && c.vec == w.vec && c.block == w.block && c.stages == w.stages) {
-      if (h->mov.n && c.kind != 0) return false;
+      if (h->mov.n && !h->mov_ok(c)) return false;
       *out = c;
       return true;
     }

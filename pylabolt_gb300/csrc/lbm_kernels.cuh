@@ -1016,16 +1016,19 @@ __device__ __forceinline__ void pair_finish(const StepArgs& a, long long n, int 
   pair_outputs<RES>(a, n, rho0, ux0, uy0, rho1, ux1, uy1, red, o2);
 }
 
-// One pair of the node-pair kernel (row y, nodes x0 and x0 + 1).
-template <class S, int COLL, int FORC, bool RES>
+// One pair of the node-pair kernel (row y, nodes x0 and x0 + 1).  MOV: the
+// case has moving obstacles; their nodes and the segments around them are
+// flagged, so only the per-node path sees them (and records the densities
+// their bounce-back reads).
+template <class S, int COLL, int FORC, bool RES, bool MOV = false>
 __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, float red[7]) {
   using IO = PairIO<S>;
   using W = typename IO::W;
   const Geom& g = a.g;
   const int seg = y * g.nseg + (x0 >> 5);
   if (g.segflag[seg] != 0) {
-    step_node<S, COLL, FORC, false, RES>(a, x0, y, red);
-    if (x0 + 1 < g.nx) step_node<S, COLL, FORC, false, RES>(a, x0 + 1, y, red);
+    step_node<S, COLL, FORC, MOV, RES>(a, x0, y, red);
+    if (x0 + 1 < g.nx) step_node<S, COLL, FORC, MOV, RES>(a, x0 + 1, y, red);
     return;
   }
   // both nodes are bulk nodes: every source is inside the grid
@@ -1060,15 +1063,15 @@ __device__ __forceinline__ void pair_step(const StepArgs& a, int x0, int y, floa
 
 // CAP = 1 asks for 6 resident blocks of 256 threads (at most 40 registers),
 // CAP = 2 for 4 (at most 64), CAP = 3 for 7 (32, with a few spills).  RES: the
-// residual instantiation.  (Two rows per
-// thread, one after the other, ran no faster: 131.8 against 131.5 GLUPS in
-// FP16, 87.6 against 91.0 in FP32.)
-template <class S, int COLL, int FORC, int CAP, bool RES>
+// residual instantiation; MOV: the moving-obstacle one (CAP = 1 only).  (Two
+// rows per thread, one after the other, ran no faster: 131.8 against 131.5
+// GLUPS in FP16, 87.6 against 91.0 in FP32.)
+template <class S, int COLL, int FORC, int CAP, bool RES, bool MOV = false>
 __global__ void __launch_bounds__(256, CAP == 1 ? 6 : (CAP == 2 ? 4 : (CAP == 3 ? 7 : 1)))
     step_pair_kernel(const StepArgs a) {
   const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
   float red[7] = {0, 0, 0, 0, 0, 0, 0};
-  if (x0 < a.g.nx) pair_step<S, COLL, FORC, RES>(a, x0, blockIdx.y, red);
+  if (x0 < a.g.nx) pair_step<S, COLL, FORC, RES, MOV>(a, x0, blockIdx.y, red);
   if (RES) block_residual<float>(a, red);
 }
 

@@ -174,3 +174,52 @@ def test_residual_steps_do_not_change_the_moving_run(storage):
         else:
             assert np.abs(ua - ub).max() <= 1e-5 * np.abs(ub).max()
             assert np.abs(ra - rb).max() <= 1e-6
+
+
+def _moving_channel(kind="fixed_velocity"):
+    """A 512 x 128 channel (pressure-driven) with a cylinder of radius 12
+    that translates and rotates (or moves under its forces): wide enough for
+    whole bulk row segments around it."""
+    from pylabolt_gb300 import workloads
+    c = workloads.cylinder(nx=512, ny=128, radius=12.0, center=(160, 65))
+    c["obstacle_dict"]["options"] = {"compute_force_torque": True, "move_obstacles": True}
+    c["obstacle_dict"]["cylinder"].update({"static": False, "solid_motion_dict": {
+        "type": kind, "degree_of_freedom": "both",
+        "linear_velocity": [0.03, 0.01] if kind == "fixed_velocity" else [0.0, 0.0],
+        "angular_velocity": 0.005 if kind == "fixed_velocity" else 0.0}})
+    if kind == "calculated":
+        c["obstacle_dict"]["cylinder"]["density"] = 1.5
+    return Case(c)
+
+
+@pytest.mark.parametrize("kind", ["fixed_velocity", "calculated"])
+def test_moving_obstacles_on_the_node_pair_kernel(kind, monkeypatch):
+    """The node-pair kernel serves cases with moving obstacles: bulk pairs on
+    the fast path, the flagged segments around the obstacle on the per-node
+    moving-obstacle path.  Against the scalar kernel, FP32, with residual and
+    moment steps: the same obstacle track and fields within FP32 rounding."""
+    case = _moving_channel(kind)
+    out = []
+    for v in ("0,1,128,1", "3,2,128,1"):
+        monkeypatch.setenv("LBM_VARIANT", v)
+        with FluidLBM(case, storage="fp32_shifted") as s:
+            s.initialize()
+            res = []
+            for _ in range(4):
+                s.step(40)
+                s.step(10, residual=True)
+                res.append(s.residual())
+            s.step(1, moments=True)
+            assert s.kernel_variant == tuple(int(i) for i in v.split(","))
+            rho, u = s.moments()
+            out.append((u, s.moving_obstacles()[0], np.array(res), s.node_flags()))
+    (u0, o0, r0, f0), (u1, o1, r1, f1) = out
+    fluid = ~case.solid
+    assert np.abs(u1 - u0)[fluid].max() <= 1e-5 * np.abs(u0[fluid]).max()
+    if kind == "fixed_velocity":
+        assert o1["center"][0] == o0["center"][0] and o1["center"][1] == o0["center"][1]
+        assert np.array_equal(f1, f0)
+    else:
+        assert np.allclose(o1["center"], o0["center"], rtol=0, atol=1e-6)
+    np.testing.assert_allclose(o1["force"], o0["force"], rtol=1e-4, atol=1e-9)
+    np.testing.assert_allclose(r1, r0, rtol=1e-4)

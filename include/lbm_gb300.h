@@ -247,15 +247,17 @@ int lbm_set_force_links(LbmHandle* h, const LbmForceLink* links, int64_t nlinks,
  * gives the t = 0 values (pop = pop_new = f_eq, fluidLB.py:323-335). */
 int lbm_forces(LbmHandle* h, double* out);
 
-/* A circular obstacle that moves (extension: the reference's moving-obstacle
+/* A circular or elliptic obstacle that moves (extension: the reference's moving-obstacle
  * path cannot run, pylabolt/base/obstacle_operator.py:47-73 calls an undefined
  * reconstruct_obstacles).  Each step, before the fused step:
  *   1. motion (update_position_velocity, pylabolt/parallel/cpu/
  *      obstacle_kernels.py:386-460, from the last step's force / torque):
  *      calculated: omega += T/I (rotation), v += F/m + g (translation);
  *      angle += omega_old + T/(2I); center += v_old + (F/m + g)/2;
- *   2. re-rasterisation: (x-cx)^2 + (y-cy)^2 <= r^2 is solid, with velocity
- *      v + omega x r and the obstacle's density; nodes it leaves become fluid
+ *   2. re-rasterisation: (x-cx)^2 + (y-cy)^2 <= r^2 is solid (an ellipse:
+ *      its semi-axes at the angle reached, construct_ellipse, obstacle_kernels.py:
+ *      192-241), with velocity v + omega x r and the obstacle's density;
+ *      nodes it leaves become fluid
  *      and are refilled with f_eq(mean rho of their fluid neighbours, the
  *      wall velocity they had);
  *   3. fluid nodes next to it pull moving-solid bounce-back
@@ -288,8 +290,8 @@ typedef struct {
 
 /* Registers the moving obstacles (at most 32) and the gravity of their
  * motion; call after lbm_create.  lbm_init_fields must follow before the next
- * step (it places them).  Only the scalar step kernel serves a case with
- * moving obstacles. */
+ * step (it places them).  The scalar step kernel or the node-pair kernel's
+ * 40-register shape serves a case with moving obstacles. */
 int lbm_set_moving_obstacles(LbmHandle* h, const LbmMovingObstacle* obs, int n,
                              const double gravity[2]);
 

@@ -920,8 +920,11 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   if (aa) h->pop_raw[1] = h->pop_raw[0];
   h->aa = aa;
   for (int i = 0; i < 2; ++i) h->pop[i] = static_cast<char*>(h->pop_raw[i]) + pitch * eb;
-  for (int i = 0; i < 3; ++i)
-    if ((rc = h->alloc(&h->mom[i], plane * cb))) return bail(rc);
+  // rho, ux, uy: three consecutive planes of one allocation (u is read back
+  // as a two-component array from ux)
+  if ((rc = h->alloc(&h->mom[0], 3 * plane * cb))) return bail(rc);
+  h->mom[1] = static_cast<char*>(h->mom[0]) + plane * cb;
+  h->mom[2] = static_cast<char*>(h->mom[0]) + 2 * plane * cb;
   e = cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, c.device);
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("device attribute: ") + cudaGetErrorString(e)));
   {
@@ -1067,10 +1070,11 @@ static int fields_to_stage(LbmHandle* h, const HT* rho, const HT* u, int layout,
   int rc = h->ensure_stage(hn + 3 * plane);
   if (rc) return rc;
   h->initialized = false;   // until the new state is complete
-  double* ds = h->stage + hn;   // device order: rho [plane], u [2][plane]
+  // device order: rho [plane], u [2][plane]; the transposes write every
+  // inner node, the only ones the equilibrium kernel reads
+  double* ds = h->stage + hn;
   HT* hs = reinterpret_cast<HT*>(h->stage);   // host order: rho [nh], u [nh][2]
   const int nx = h->cfg.nx;
-  LBM_CUDA(cudaMemsetAsync(ds, 0, 3 * plane * sizeof(double), h->stream));
   if (direct) {   // transposed straight from the caller's pinned buffers
     LBM_CUDA(lbm::reorder_cols(h->g, rd, ds, 1, layout, 1, 0, nx, h->stream));
     LBM_CUDA(lbm::reorder_cols(h->g, ud, ds + plane, 2, layout, 1, 0, nx, h->stream));
@@ -1480,6 +1484,25 @@ int lbm_adjoint_backward(LbmHandle* h, const double* grad_u, double* grad_force,
 extern "C++" {
 // Moments of the last recorded step into caller fields in host order
 // (HT = double, or float for single-precision cases, rounded to nearest).
+// The device keeps them as three consecutive planes in the compute type
+// (FP64, or FP32 for shifted storage); they are transposed straight from
+// there, widened or rounded on the way.
+template <class HT, class CT>
+static cudaError_t moments_cols(const LbmHandle* h, const CT* mom, HT* rho, HT* u, int layout,
+                                int x0, int x1) {
+  const long long plane = h->g.plane;
+  cudaError_t e = lbm::reorder_cols(h->g, mom, rho, 1, layout, 0, x0, x1, h->stream);
+  if (e != cudaSuccess) return e;
+  return lbm::reorder_cols(h->g, mom + plane, u, 2, layout, 0, x0, x1, h->stream);
+}
+
+template <class HT>
+static cudaError_t moments_cols(const LbmHandle* h, HT* rho, HT* u, int layout, int x0, int x1) {
+  if (h->ks->compute_bytes == sizeof(float))
+    return moments_cols(h, static_cast<const float*>(h->mom[0]), rho, u, layout, x0, x1);
+  return moments_cols(h, static_cast<const double*>(h->mom[0]), rho, u, layout, x0, x1);
+}
+
 template <class HT>
 static int get_moments(LbmHandle* h, HT* rho, HT* u, int layout, const char* name) {
   if (!h || !rho || !u) return fail(LBM_ERR_ARG, std::string(name) + ": null argument");
@@ -1488,25 +1511,18 @@ static int get_moments(LbmHandle* h, HT* rho, HT* u, int layout, const char* nam
   if (!h->has_moments)
     return fail(LBM_ERR_STATE, std::string(name) + ": no moments recorded (use LBM_STEP_MOMENTS)");
   LBM_CUDA(cudaSetDevice(h->cfg.device));
-  const long long nh = h->host_nodes(layout), plane = h->g.plane;
+  const long long nh = h->host_nodes(layout);
   const int nx = h->cfg.nx;
   HT* rd = layout == LBM_LAYOUT_INNER ? h->host_direct(rho) : nullptr;
   HT* ud = layout == LBM_LAYOUT_INNER ? h->host_direct(u) : nullptr;
   if (rd && ud) {   // transposed straight into the caller's pinned buffers
-    int rc = h->ensure_stage(3 * plane);
-    if (rc) return rc;
-    double* ds = h->stage;
-    LBM_CUDA(h->ks->moments_to_f64(h->g, h->mom[0], h->mom[1], h->mom[2], ds, h->stream));
-    LBM_CUDA(lbm::reorder_cols(h->g, ds, rd, 1, layout, 0, 0, nx, h->stream));
-    LBM_CUDA(lbm::reorder_cols(h->g, ds + plane, ud, 2, layout, 0, 0, nx, h->stream));
+    LBM_CUDA(moments_cols(h, rd, ud, layout, 0, nx));
     return h->wait();
   }
-  const long long hn = (3 * nh * (long long)sizeof(HT) + 7) / 8;   // host-order part, in doubles
-  int rc = h->ensure_stage(hn + 3 * plane);
+  const long long hn = (3 * nh * (long long)sizeof(HT) + 7) / 8;   // host-order stage, in doubles
+  int rc = h->ensure_stage(hn);
   if (rc) return rc;
   HT* hs = reinterpret_cast<HT*>(h->stage);
-  double* ds = h->stage + hn;
-  LBM_CUDA(h->ks->moments_to_f64(h->g, h->mom[0], h->mom[1], h->mom[2], ds, h->stream));
   if (layout == LBM_LAYOUT_INNER) {
     // column chunks: chunk c goes to the host on the transfer stream while
     // the handle's stream transposes chunk c + 1
@@ -1516,8 +1532,7 @@ static int get_moments(LbmHandle* h, HT* rho, HT* u, int layout, const char* nam
     for (int c = 0; c < NC; ++c) {
       const int x0 = h->xfer_col(c), x1 = h->xfer_col(c + 1);
       if (x0 >= x1) continue;
-      LBM_CUDA(lbm::reorder_cols(h->g, ds, hs, 1, layout, 0, x0, x1, h->stream));
-      LBM_CUDA(lbm::reorder_cols(h->g, ds + plane, hs + nh, 2, layout, 0, x0, x1, h->stream));
+      LBM_CUDA(moments_cols(h, hs, hs + nh, layout, x0, x1));
       LBM_CUDA(cudaEventRecord(h->xev[c], h->stream));
       LBM_CUDA(cudaStreamWaitEvent(h->xfer, h->xev[c], 0));
       LBM_CUDA(cudaMemcpyAsync(rho + x0 * ny, hs + x0 * ny, (x1 - x0) * ny * sizeof(HT),
@@ -1530,8 +1545,7 @@ static int get_moments(LbmHandle* h, HT* rho, HT* u, int layout, const char* nam
     return h->wait();
   }
   LBM_CUDA(cudaMemsetAsync(hs, 0, 3 * nh * sizeof(HT), h->stream));   // ghosts of the padded layout
-  LBM_CUDA(lbm::reorder_cols(h->g, ds, hs, 1, layout, 0, 0, nx, h->stream));
-  LBM_CUDA(lbm::reorder_cols(h->g, ds + plane, hs + nh, 2, layout, 0, 0, nx, h->stream));
+  LBM_CUDA(moments_cols(h, hs, hs + nh, layout, 0, nx));
   LBM_CUDA(cudaMemcpyAsync(rho, hs, nh * sizeof(HT), cudaMemcpyDefault, h->stream));
   LBM_CUDA(cudaMemcpyAsync(u, hs + nh, 2 * nh * sizeof(HT), cudaMemcpyDefault, h->stream));
   return h->wait();

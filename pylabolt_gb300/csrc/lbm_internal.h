@@ -305,6 +305,8 @@ cudaError_t reorder_cols(const Geom& g, const float* in, double* out, int ncomp,
                          int layout, int to_device, int x_lo, int x_hi, cudaStream_t s);
 cudaError_t reorder_cols(const Geom& g, const double* in, float* out, int ncomp,
                          int layout, int to_device, int x_lo, int x_hi, cudaStream_t s);
+cudaError_t reorder_cols(const Geom& g, const float* in, float* out, int ncomp,
+                         int layout, int to_device, int x_lo, int x_hi, cudaStream_t s);
 
 // Launches the bounded-wait self-test kernel (one mbarrier nobody arrives
 // at): *err (device-visible) gets kErrWaitTimeout after limit_s, *waited_ns

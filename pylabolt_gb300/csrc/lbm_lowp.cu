@@ -134,4 +134,9 @@ cudaError_t reorder_cols(const Geom& g, const double* in, float* out, int ncomp,
   return reorder_launch(g, in, out, ncomp, layout, to_device, x_lo, x_hi, s);
 }
 
+cudaError_t reorder_cols(const Geom& g, const float* in, float* out, int ncomp,
+                         int layout, int to_device, int x_lo, int x_hi, cudaStream_t s) {
+  return reorder_launch(g, in, out, ncomp, layout, to_device, x_lo, x_hi, s);
+}
+
 }  // namespace lbm

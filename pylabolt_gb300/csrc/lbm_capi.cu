@@ -80,8 +80,9 @@ struct LbmHandle {
   float* omega_seg = nullptr;  // optional per-segment relaxation rate
   double* partials = nullptr;
   double* red = nullptr;       // device [16]: residual sums, conservation sums
-  double* scratch = nullptr;   // device [kFinishBlocks*8]: first reduction stage
+  double* scratch = nullptr;   // device [kFinishScratch]: block sums and the last-block counter
   double* host_red = nullptr;  // pinned  [16]
+  double* host_red_dev = nullptr;   // host_red as the device addresses it
   double* stage = nullptr;     // device FP64 staging
   size_t stage_elems = 0;
   int cur = 0;                 // AA layout: both pop[] are one buffer; cur 0 = next step even
@@ -962,10 +963,15 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
   }
   if ((rc = h->alloc(reinterpret_cast<void**>(&h->partials), maxparts * 8 * sizeof(double))) ||
       (rc = h->alloc(reinterpret_cast<void**>(&h->red), 16 * sizeof(double))) ||
-      (rc = h->alloc(reinterpret_cast<void**>(&h->scratch), lbm::kFinishBlocks * 8 * sizeof(double))))
+      (rc = h->alloc(reinterpret_cast<void**>(&h->scratch), lbm::kFinishScratch * sizeof(double))))
     return bail(rc);
   e = cudaMallocHost(reinterpret_cast<void**>(&h->host_red), 16 * sizeof(double));
   if (e != cudaSuccess) return bail(fail(LBM_ERR_ALLOC, std::string("cudaMallocHost: ") + cudaGetErrorString(e)));
+  // the reductions write their results straight into it
+  e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&h->host_red_dev), h->host_red, 0);
+  if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaHostGetDevicePointer: ") + cudaGetErrorString(e)));
+  if ((e = cudaMemsetAsync(h->scratch, 0, lbm::kFinishScratch * sizeof(double), h->stream)) != cudaSuccess)
+    return bail(fail(LBM_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
   g.cls = (const uint8_t*)d_cls;
   g.segflag = (const uint8_t*)d_seg;
   g.seglist = (const int*)d_seglist;
@@ -1273,8 +1279,7 @@ int lbm_step_ex(LbmHandle* h, int64_t nsteps, int flags) {
   if (flags & LBM_STEP_MOMENTS) h->has_moments = true;
   if (flags & LBM_STEP_RESIDUAL) {
     const lbm::Variant rv = h->res_tuned ? h->res_variant : h->variant;
-    LBM_CUDA(lbm::finish_reduce(h->partials, h->nparts_of(rv), h->scratch, h->red, h->stream));
-    LBM_CUDA(cudaMemcpyAsync(h->host_red, h->red, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    LBM_CUDA(lbm::finish_reduce(h->partials, h->nparts_of(rv), h->scratch, h->host_red_dev, h->stream));
     h->has_residual = true;
   }
   return LBM_OK;
@@ -1580,8 +1585,7 @@ int lbm_conservation(LbmHandle* h, double out[3]) {
   if (!h->initialized) return fail(LBM_ERR_STATE, "lbm_conservation: not initialised");
   LBM_CUDA(cudaSetDevice(h->cfg.device));
   LBM_CUDA(h->ks->conservation(h->g, h->p, h->pop[h->cur], h->partials, h->aa_state(), h->stream));
-  LBM_CUDA(lbm::finish_reduce(h->partials, h->g.ny, h->scratch, h->red + 8, h->stream));
-  LBM_CUDA(cudaMemcpyAsync(h->host_red + 8, h->red + 8, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  LBM_CUDA(lbm::finish_reduce(h->partials, h->g.ny, h->scratch, h->host_red_dev + 8, h->stream));
   int rc = h->wait();
   if (rc) return rc;
   for (int c = 0; c < 3; ++c) out[c] = h->host_red[8 + c];

@@ -264,8 +264,11 @@ const KernelSet& kernels_fp32();
 const KernelSet& kernels_fp16();
 
 // Deterministic reduction of `nrows` rows of 8 doubles into out8 (fixed
-// order); `scratch` holds kFinishBlocks rows.
+// order; out8 may be mapped host memory), one launch: `scratch` holds
+// kFinishBlocks rows and, after them, a zeroed counter (kFinishScratch
+// doubles in all) that tells the last block to finish to sum the rows.
 constexpr int kFinishBlocks = 128;
+constexpr int kFinishScratch = kFinishBlocks * 8 + 8;
 cudaError_t finish_reduce(const double* partials, long long nrows, double* scratch,
                           double* out8, cudaStream_t s);
 // Shared memory of one stage of the kind-2 kernel (nine halo-padded row windows).

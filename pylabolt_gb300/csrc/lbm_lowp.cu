@@ -9,8 +9,11 @@ namespace lbm {
 // rows t, t+256, ... of the range, then a shared-memory tree), and one block
 // sums those kFinishBlocks rows the same way.
 __global__ void finish_reduce_kernel(const double* __restrict__ partials,
-                                     long long nrows, double* out) {
+                                     long long nrows, double* scratch, unsigned* counter,
+                                     double* out8) {
   __shared__ double sh[8][256];
+  __shared__ bool last;
+  // stage 1: block b sums the rows of its contiguous slice into scratch row b
   const long long per = (nrows + gridDim.x - 1) / gridDim.x;
   const long long r0 = blockIdx.x * per;
   const long long r1 = r0 + per < nrows ? r0 + per : nrows;
@@ -27,13 +30,36 @@ __global__ void finish_reduce_kernel(const double* __restrict__ partials,
       for (int c = 0; c < 8; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x < 8) out[blockIdx.x * 8 + threadIdx.x] = sh[threadIdx.x][0];
+  if (threadIdx.x < 8) scratch[blockIdx.x * 8 + threadIdx.x] = sh[threadIdx.x][0];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  // stage 2, in the last block to finish: the scratch rows in row order
+  __threadfence();
+#pragma unroll
+  for (int c = 0; c < 8; ++c) s[c] = 0;
+  for (int r = threadIdx.x; r < (int)gridDim.x; r += blockDim.x)
+#pragma unroll
+    for (int c = 0; c < 8; ++c) s[c] += __ldcg(scratch + r * 8 + c);
+#pragma unroll
+  for (int c = 0; c < 8; ++c) sh[c][threadIdx.x] = s[c];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+#pragma unroll
+      for (int c = 0; c < 8; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x < 8) out8[threadIdx.x] = sh[threadIdx.x][0];
+  if (threadIdx.x == 0) *counter = 0u;   // ready for the next reduction
 }
 
 cudaError_t finish_reduce(const double* partials, long long nrows, double* scratch,
                           double* out8, cudaStream_t s) {
-  finish_reduce_kernel<<<kFinishBlocks, 256, 0, s>>>(partials, nrows, scratch);
-  finish_reduce_kernel<<<1, 256, 0, s>>>(scratch, kFinishBlocks, out8);
+  unsigned* counter = reinterpret_cast<unsigned*>(scratch + kFinishBlocks * 8);
+  finish_reduce_kernel<<<kFinishBlocks, 256, 0, s>>>(partials, nrows, scratch, counter, out8);
   return cudaGetLastError();
 }
 

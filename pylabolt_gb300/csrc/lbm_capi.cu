@@ -748,7 +748,8 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
                              : c.precision == LBM_FP32_SHIFTED ? &lbm::kernels_fp32()
                                                                 : &lbm::kernels_fp16();
   const int nx = c.nx, ny = c.ny;
-  // rows are whole TMA tiles (4096 B) for shifted storage, 512 B for FP64.
+  // rows are multiples of 4096 B for shifted storage (whole 2048-byte tiles
+  // of the tile kernel), 512 B for FP64.
   // AA layout (scalar kernel only): 128-byte rows with at least one padding
   // column, which receives the pushes across the x edges.
   const int align = (aa ? 128 : c.precision == LBM_FP64 ? 512 : lbm::kTmaRowBytes) / ks->elem_bytes;

@@ -1,6 +1,8 @@
 // Auxiliary kernels of one storage precision (conversions, conservation sums)
 // and the KernelSet that bundles them with the fused step kernel.
 #pragma once
+#include <utility>
+
 #include "lbm_adjoint.cuh"
 #include "lbm_force.cuh"
 #include "lbm_moving.cuh"
@@ -313,6 +315,9 @@ struct Kernels {
       // kind 0: {threads, register cap: 0 none, 1 32, 2 40};
       // kind 3: node pairs {2 nodes per thread, threads, register cap: 0 none,
       // 1 40, 2 64, 3 32}
+      // The first candidate runs the untuned first step and is kept with
+      // LBM_TUNE=0: the one that measured fastest for the storage at
+      // 8192x2048 (FP32 node pairs, FP16 node-pair tiles).
       constexpr int TP = kTileBytes / (2 * sizeof(S));
       const Variant vs[] = {{2, 2, TP / 2, 2}, {2, 2, TP / 2, 3}, {2, 2, TP, 2},
                             {2, 2, TP / 4, 2}, {0, 1, 128, 0}, {0, 1, 256, 0}, {0, 1, 128, 1},
@@ -320,6 +325,7 @@ struct Kernels {
                             {3, 2, 256, 0}, {3, 2, 128, 1}, {3, 2, 256, 2}, {3, 2, 128, 3}};
       k.nvariants = 15;
       for (int i = 0; i < 15; ++i) k.variants[i] = vs[i];
+      if (sizeof(S) == 4) std::swap(k.variants[0], k.variants[12]);
     } else {
       const Variant vs[] = {{0, 1, 128, 0}, {0, 1, 256, 0}, {0, 1, 512, 0}};
       k.nvariants = 3;

@@ -239,10 +239,12 @@ struct Kernels {
   }
   static cudaError_t init(const Geom& g, const Params& p, const double* rho,
                           const double* u, void* f, void* mr, void* mx, void* my,
-                          cudaStream_t s) {
-    init_kernel<S><<<node_grid(g), kStepBlock, 0, s>>>(
+                          int x_lo, int x_hi, cudaStream_t s) {
+    if (x_lo < 0 || x_hi > g.nx || x_lo >= x_hi) return cudaErrorInvalidValue;
+    const dim3 grid((x_hi - x_lo + kStepBlock - 1) / kStepBlock, g.ny);
+    init_kernel<S><<<grid, kStepBlock, 0, s>>>(
         g, p, rho, u, static_cast<S*>(f), static_cast<T*>(mr),
-        static_cast<T*>(mx), static_cast<T*>(my));
+        static_cast<T*>(mx), static_cast<T*>(my), x_lo, x_hi);
     return cudaGetLastError();
   }
   static cudaError_t convert(const Geom& g, const Params& p, void* f,

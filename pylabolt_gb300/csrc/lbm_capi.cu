@@ -1066,9 +1066,13 @@ int lbm_destroy(LbmHandle* h) {
 extern "C++" {
 // Caller fields in host order (HT = double, or float for single-precision
 // cases) to the FP64 device-order stage *ds: rho [plane], u [2][plane].
+// *inited: the equilibrium was written chunk by chunk as the columns
+// arrived (inner layout, staged, no moving obstacles).
 template <class HT>
-static int fields_to_stage(LbmHandle* h, const HT* rho, const HT* u, int layout, double** ds_out) {
+static int fields_to_stage(LbmHandle* h, const HT* rho, const HT* u, int layout, double** ds_out,
+                           bool* inited) {
   const long long nh = h->host_nodes(layout), plane = h->g.plane;
+  *inited = false;
   const HT* rd = h->host_direct(rho);
   const HT* ud = h->host_direct(u);
   const bool direct = rd && ud;
@@ -1082,7 +1086,20 @@ static int fields_to_stage(LbmHandle* h, const HT* rho, const HT* u, int layout,
   double* ds = h->stage + hn;
   HT* hs = reinterpret_cast<HT*>(h->stage);   // host order: rho [nh], u [nh][2]
   const int nx = h->cfg.nx;
+  // the previous residual step's fields restart from zero; they do not
+  // depend on the new fields, so they clear while those are copied
+  auto clear_old = [&]() -> int {
+    for (int i = 0; i < 6; ++i)
+      if (h->old[i]) LBM_CUDA(cudaMemsetAsync(h->old[i], 0, plane * h->ks->compute_bytes, h->stream));
+    h->old_cur = 0;
+    return LBM_OK;
+  };
+  if (h->aa) h->cur = 0;   // AA: the first step is an even phase
+  // with no moving obstacles the classes are static, so the equilibrium of a
+  // chunk of columns can be written as soon as the chunk is transposed
+  const bool chunk_init = !h->mov.n;
   if (direct) {   // transposed straight from the caller's pinned buffers
+    if ((rc = clear_old())) return rc;
     LBM_CUDA(lbm::reorder_cols(h->g, rd, ds, 1, layout, 1, 0, nx, h->stream));
     LBM_CUDA(lbm::reorder_cols(h->g, ud, ds + plane, 2, layout, 1, 0, nx, h->stream));
   } else if (layout == LBM_LAYOUT_INNER) {
@@ -1094,6 +1111,7 @@ static int fields_to_stage(LbmHandle* h, const HT* rho, const HT* u, int layout,
     constexpr int NC = LbmHandle::kXferChunks;
     LBM_CUDA(cudaEventRecord(h->xev[NC], h->stream));
     LBM_CUDA(cudaStreamWaitEvent(h->xfer, h->xev[NC], 0));
+    if ((rc = clear_old())) return rc;   // after the event: the copies need not wait
     for (int c = 0; c < NC; ++c) {
       const int x0 = h->xfer_col(c), x1 = h->xfer_col(c + 1);
       if (x0 >= x1) continue;
@@ -1105,8 +1123,13 @@ static int fields_to_stage(LbmHandle* h, const HT* rho, const HT* u, int layout,
       LBM_CUDA(cudaStreamWaitEvent(h->stream, h->xev[c], 0));
       LBM_CUDA(lbm::reorder_cols(h->g, hs, ds, 1, layout, 1, x0, x1, h->stream));
       LBM_CUDA(lbm::reorder_cols(h->g, hs + nh, ds + plane, 2, layout, 1, x0, x1, h->stream));
+      if (chunk_init)
+        LBM_CUDA(h->ks->init(h->g, h->p, ds, ds + plane, h->pop[h->cur], h->mom[0], h->mom[1],
+                             h->mom[2], x0, x1, h->stream));
     }
+    *inited = chunk_init;
   } else {
+    if ((rc = clear_old())) return rc;
     LBM_CUDA(cudaMemcpyAsync(hs, rho, nh * sizeof(HT), cudaMemcpyDefault, h->stream));
     LBM_CUDA(cudaMemcpyAsync(hs + nh, u, 2 * nh * sizeof(HT), cudaMemcpyDefault, h->stream));
     LBM_CUDA(lbm::reorder_cols(h->g, hs, ds, 1, layout, 1, 0, nx, h->stream));
@@ -1118,7 +1141,7 @@ static int fields_to_stage(LbmHandle* h, const HT* rho, const HT* u, int layout,
 
 }  // extern "C++"
 
-static int init_from_stage(LbmHandle* h, double* ds);
+static int init_from_stage(LbmHandle* h, double* ds, bool inited);
 
 extern "C++" {
 template <class HT>
@@ -1128,8 +1151,9 @@ static int init_fields(LbmHandle* h, const HT* rho, const HT* u, int layout, con
     return fail(LBM_ERR_ARG, std::string(name) + ": unknown layout");
   LBM_CUDA(cudaSetDevice(h->cfg.device));
   double* ds = nullptr;
-  int rc = fields_to_stage(h, rho, u, layout, &ds);
-  return rc ? rc : init_from_stage(h, ds);
+  bool inited = false;
+  int rc = fields_to_stage(h, rho, u, layout, &ds, &inited);
+  return rc ? rc : init_from_stage(h, ds, inited);
 }
 
 }  // extern "C++"
@@ -1143,7 +1167,7 @@ int lbm_init_fields_f32(LbmHandle* h, const float* rho, const float* u, int layo
 }
 
 // Equilibrium populations from the staged fields, then the step state reset.
-static int init_from_stage(LbmHandle* h, double* ds) {
+static int init_from_stage(LbmHandle* h, double* ds, bool inited) {
   const long long plane = h->g.plane;
   int rc;
   if (h->mov.n) {   // static classes back before f_eq is written (a run may have moved obstacles)
@@ -1152,12 +1176,9 @@ static int init_from_stage(LbmHandle* h, double* ds) {
     LBM_CUDA(cudaMemcpyAsync(const_cast<uint8_t*>(h->g.segflag), h->mov.seg_static,
                              (size_t)h->g.ny * h->g.nseg, cudaMemcpyDeviceToDevice, h->stream));
   }
-  if (h->aa) h->cur = 0;   // AA: the first step is an even phase
-  LBM_CUDA(h->ks->init(h->g, h->p, ds, ds + plane, h->pop[h->cur], h->mom[0], h->mom[1],
-                       h->mom[2], h->stream));
-  for (int i = 0; i < 6; ++i)
-    if (h->old[i]) LBM_CUDA(cudaMemsetAsync(h->old[i], 0, plane * h->ks->compute_bytes, h->stream));
-  h->old_cur = 0;
+  if (!inited)
+    LBM_CUDA(h->ks->init(h->g, h->p, ds, ds + plane, h->pop[h->cur], h->mom[0], h->mom[1],
+                         h->mom[2], 0, h->cfg.nx, h->stream));
   if (h->mov.n) {
     // registered obstacle state, static classes, then the obstacles placed,
     // their nodes classified and the t = 0 momentum exchange (the reference

@@ -233,7 +233,7 @@ struct KernelSet {
   // rho/u on every node.  rho [plane], u [2][plane], FP64, device order.
   cudaError_t (*init)(const Geom& g, const Params& p, const double* rho,
                       const double* u, void* f, void* mr, void* mx, void* my,
-                      cudaStream_t s);
+                      int x_lo, int x_hi, cudaStream_t s);
   // storage <-> FP64 [9][plane] (dir 0: to FP64, 1: from FP64); solids 0.
   // aa_state (dir 0): where the post-collision values sit (aa_post_index).
   cudaError_t (*convert)(const Geom& g, const Params& p, void* f, double* f64,

@@ -1464,16 +1464,17 @@ __global__ void __launch_bounds__(kTileBytes / (2 * PPT * sizeof(S)), 2048 * PPT
 
 // ---------------------------------------------------------------------------
 // Initial equilibrium -- equilibrium_kernels.py:38-78.  rho/u are FP64 device
-// arrays in device order; moments (compute type) receive rho/u on every node.
+// arrays in device order; moments (compute type) receive rho/u on every node
+// of the columns x_lo <= x < x_hi.
 template <class S>
 __global__ void init_kernel(const Geom g, const Params p, const double* __restrict__ rho,
                             const double* __restrict__ u, S* __restrict__ f,
                             typename Store<S>::T* mr, typename Store<S>::T* mx,
-                            typename Store<S>::T* my) {
+                            typename Store<S>::T* my, int x_lo, int x_hi) {
   using T = typename Store<S>::T;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int x = x_lo + blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
-  if (x >= g.nx) return;
+  if (x >= x_hi) return;
   const long long n = g.node(x, y);
   const double r = rho[n], ux = u[n], uy = u[g.plane + n];
   mr[n] = T(r);

@@ -78,9 +78,11 @@ typedef struct LbmHandle LbmHandle;
                           write each node's own slots (swapped), odd steps pull
                           from and push to the neighbours' slots.  Half the
                           population memory.  Not with moving obstacles, the
-                          adjoint or zero_gradient links; the scalar kernel
-                          only, its launch shape fixed (no autotuner trials:
-                          they would advance the state). */
+                          adjoint or zero_gradient links.  Its launch shape
+                          is fixed per storage (no autotuner trials: they
+                          would advance the state): the scalar kernel for
+                          FP64, node pairs for FP32, node-pair tiles for
+                          FP16. */
 
 /* flags of lbm_step_ex: what the last step of the call records */
 #define LBM_STEP_MOMENTS 1   /* keep rho/u of that step for lbm_get_moments */

@@ -169,17 +169,23 @@ struct Kernels {
     if constexpr (Store<S>::shifted) {
       const int smem = v.stages * tile_stage_bytes();
       constexpr int TP = kTileBytes / (2 * sizeof(S));   // pairs of a tile
-      static int configured[3] = {0, 0, 0};   // bytes the attribute was last raised to
+      // bytes the attribute was last raised to, per device (function
+      // attributes belong to each device's copy of the kernel)
+      constexpr int kDevices = 64;
+      static int configured[kDevices][3] = {};
       if (v.block == TP / 2 || (MODE == 0 && (v.block == TP || v.block == TP / 4))) {
         const int i = v.block == TP ? 0 : (v.block == TP / 2 ? 1 : 2);
         const auto kern = MODE != 0 ? step_tile_pair_kernel<S, COLL, FORC, RES, 2, MODE>
                           : i == 0  ? step_tile_pair_kernel<S, COLL, FORC, RES, 1, MODE>
                           : i == 1  ? step_tile_pair_kernel<S, COLL, FORC, RES, 2, MODE>
                                     : step_tile_pair_kernel<S, COLL, FORC, RES, 4, MODE>;
-        if (smem > configured[i]) {
-          cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        if (dev < 0 || dev >= kDevices || smem > configured[dev][i]) {
+          e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
           if (e != cudaSuccess) return e;
-          configured[i] = smem;
+          if (dev >= 0 && dev < kDevices) configured[dev][i] = smem;
         }
         kern<<<grid, v.block, smem, s>>>(a, v.stages);
         return cudaGetLastError();

@@ -291,8 +291,10 @@ inline dim3 step_grid(const Geom& g, Variant v, int sms, int elem_bytes, bool re
     if (blocks > tiles) blocks = tiles;
     return dim3((unsigned)blocks, 1);
   }
+  // blocks cover the nodes x < nx of a row, not its padding (the AA layout's
+  // rows carry at least one padding column: a whole block more at nx = 8192)
   const long long per_block = (long long)v.block * v.vec;
-  return dim3((unsigned)((g.pitch + per_block - 1) / per_block), (unsigned)g.ny);
+  return dim3((unsigned)((g.nx + per_block - 1) / per_block), (unsigned)g.ny);
 }
 // Host-order <-> device-order copies of node data with `ncomp`
 // components: host AoS [node][ncomp] in inner (ind = x*ny+y) or padded

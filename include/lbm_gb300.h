@@ -186,6 +186,14 @@ int lbm_get_moments_f32(LbmHandle* h, float* rho, float* u, int layout);
  * pass met a non-finite rho or u. */
 int lbm_residual(LbmHandle* h, double out[3]);
 
+/* The same residuals for the residual step that ended at time step t (t as
+ * lbm_time reports it), which must be one of the last eight residual steps
+ * since initialisation (LBM_ERR_STATE otherwise).  Waits for that step only,
+ * not for the steps queued after it: a host loop can read step t's residual
+ * while step t+1 runs, as the reference's run loop logs each step's residues
+ * (pylabolt/solvers/fluidLB.py:364-375). */
+int lbm_residual_at(LbmHandle* h, int64_t t, double out[3]);
+
 /* FP64 sums over fluid nodes of the stored post-collision populations:
  * {sum f, sum cx f, sum cy f} (mass and momentum diagnostics; extension). */
 int lbm_conservation(LbmHandle* h, double out[3]);

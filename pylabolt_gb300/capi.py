@@ -83,7 +83,8 @@ _LIB = None
 
 # every symbol include/lbm_gb300.h declares
 EXPORTS = ["lbm_create", "lbm_init_fields", "lbm_init_fields_f32", "lbm_set_body_force", "lbm_step",
-           "lbm_step_ex", "lbm_get_moments", "lbm_get_moments_f32", "lbm_residual", "lbm_conservation",
+           "lbm_step_ex", "lbm_get_moments", "lbm_get_moments_f32", "lbm_residual", "lbm_residual_at",
+           "lbm_conservation",
            "lbm_get_populations", "lbm_set_populations", "lbm_time",
            "lbm_kernel_launches", "lbm_kernel_variant", "lbm_tuning", "lbm_device_bytes", "lbm_time_steps",
            "lbm_synchronize", "lbm_last_error", "lbm_destroy", "lbm_conservation_noalloc",
@@ -119,6 +120,7 @@ def load(build=True):
         "lbm_get_moments": [P, P, P, ctypes.c_int],
         "lbm_get_moments_f32": [P, P, P, ctypes.c_int],
         "lbm_residual": [P, dbl],
+        "lbm_residual_at": [P, i64, dbl],
         "lbm_conservation": [P, dbl],
         "lbm_get_populations": [P, P],
         "lbm_set_populations": [P, P],

@@ -49,6 +49,7 @@ constexpr uint64_t kFnvSeed = 14695981039346656037ull;
   } while (0)
 
 constexpr int kGraphChunk = 32;   // steps per captured graph (even)
+constexpr int kResRing = 8;       // residual steps whose sums stay readable
 constexpr int kCX[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
 constexpr int kCY[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
 
@@ -81,8 +82,15 @@ struct LbmHandle {
   double* partials = nullptr;
   double* red = nullptr;       // device [16]: residual sums, conservation sums
   double* scratch = nullptr;   // device [kFinishScratch]: block sums and the last-block counter
-  double* host_red = nullptr;  // pinned  [16]
+  double* host_red = nullptr;  // pinned [16 + 8 kResRing]: sums; residual ring
   double* host_red_dev = nullptr;   // host_red as the device addresses it
+  // The sums of the last kResRing residual steps, each in its own slot of
+  // host_red (8 words from word 16 on), with the event recorded after its
+  // reduction and its time step (-1: empty): a step's residual can be read
+  // while later steps run.
+  cudaEvent_t res_ev[kResRing] = {};
+  int64_t res_t[kResRing] = {-1, -1, -1, -1, -1, -1, -1, -1};
+  int64_t res_seq = 0;
   double* stage = nullptr;     // device FP64 staging
   size_t stage_elems = 0;
   int cur = 0;                 // AA layout: both pop[] are one buffer; cur 0 = next step even
@@ -183,6 +191,8 @@ struct LbmHandle {
       if (e) cudaEventDestroy(e);
     if (xfer) cudaStreamDestroy(xfer);
     for (auto& a : allocs) cudaFree(a.first);
+    for (cudaEvent_t e : res_ev)
+      if (e) cudaEventDestroy(e);
     if (host_red) cudaFreeHost(host_red);
     if (err_host) cudaFreeHost(err_host);
     if (stream) cudaStreamDestroy(stream);
@@ -202,10 +212,17 @@ struct LbmHandle {
     return LBM_OK;
   }
 
-  int wait() {
+  void clear_residuals() {
+    has_residual = false;
+    for (int64_t& v : res_t) v = -1;
+  }
+  double* res_slot(int i) const { return host_red + 16 + 8 * i; }
+
+  // Waits for the handle's stream (or, given one, for an event on it).
+  int wait(cudaEvent_t ev = nullptr) {
     auto t0 = std::chrono::steady_clock::now();
     for (;;) {
-      cudaError_t e = cudaStreamQuery(stream);
+      cudaError_t e = ev ? cudaEventQuery(ev) : cudaStreamQuery(stream);
       if (e == cudaSuccess) {
         if (err_host && *reinterpret_cast<volatile int*>(err_host) != 0) {
           const int code = *reinterpret_cast<volatile int*>(err_host);
@@ -966,11 +983,14 @@ int lbm_create(const LbmConfig* cfg, const uint8_t* node_solid,
       (rc = h->alloc(reinterpret_cast<void**>(&h->red), 16 * sizeof(double))) ||
       (rc = h->alloc(reinterpret_cast<void**>(&h->scratch), lbm::kFinishScratch * sizeof(double))))
     return bail(rc);
-  e = cudaMallocHost(reinterpret_cast<void**>(&h->host_red), 16 * sizeof(double));
+  e = cudaMallocHost(reinterpret_cast<void**>(&h->host_red), (16 + 8 * kResRing) * sizeof(double));
   if (e != cudaSuccess) return bail(fail(LBM_ERR_ALLOC, std::string("cudaMallocHost: ") + cudaGetErrorString(e)));
   // the reductions write their results straight into it
   e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&h->host_red_dev), h->host_red, 0);
   if (e != cudaSuccess) return bail(fail(LBM_ERR_CUDA, std::string("cudaHostGetDevicePointer: ") + cudaGetErrorString(e)));
+  for (cudaEvent_t& ev : h->res_ev)
+    if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
+      return bail(fail(LBM_ERR_CUDA, std::string("cudaEventCreate: ") + cudaGetErrorString(e)));
   if ((e = cudaMemsetAsync(h->scratch, 0, lbm::kFinishScratch * sizeof(double), h->stream)) != cudaSuccess)
     return bail(fail(LBM_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
   g.cls = (const uint8_t*)d_cls;
@@ -1196,7 +1216,7 @@ static int init_from_stage(LbmHandle* h, double* ds, bool inited) {
   h->initialized = true;
   h->nopull = true;
   h->has_moments = true;
-  h->has_residual = false;
+  h->clear_residuals();
   h->t = 0;
   return LBM_OK;
 }
@@ -1301,7 +1321,12 @@ int lbm_step_ex(LbmHandle* h, int64_t nsteps, int flags) {
   if (flags & LBM_STEP_MOMENTS) h->has_moments = true;
   if (flags & LBM_STEP_RESIDUAL) {
     const lbm::Variant rv = h->res_tuned ? h->res_variant : h->variant;
-    LBM_CUDA(lbm::finish_reduce(h->partials, h->nparts_of(rv), h->scratch, h->host_red_dev, h->stream));
+    const int slot = (int)(h->res_seq % kResRing);
+    LBM_CUDA(lbm::finish_reduce(h->partials, h->nparts_of(rv), h->scratch, h->host_red_dev + 16 + 8 * slot,
+                                h->stream));
+    LBM_CUDA(cudaEventRecord(h->res_ev[slot], h->stream));
+    h->res_t[slot] = h->t;
+    h->res_seq += 1;
     h->has_residual = true;
   }
   return LBM_OK;
@@ -1403,6 +1428,7 @@ int lbm_adjoint_forward(LbmHandle* h, int64_t nsteps, int interval) {
   }
   h->nopull = false;
   h->t = nsteps;
+  h->clear_residuals();
   h->launches += nsteps;
   h->has_moments = true;
   A.T = nsteps;
@@ -1588,18 +1614,39 @@ int lbm_get_moments_f32(LbmHandle* h, float* rho, float* u, int layout) {
   return get_moments(h, rho, u, layout, "lbm_get_moments_f32");
 }
 
+namespace {
+// {res_rho, res_ux, res_uy} from one residual step's sums (residues.py:204-222)
+int residual_of(const LbmHandle* h, const double* s, double out[3], const char* who) {
+  for (int c = 0; c < 3; ++c) out[c] = std::sqrt(s[2 * c] / (s[2 * c + 1] + h->cfg.eps));
+  if (s[6] > 0)
+    return fail(LBM_ERR_NONFINITE, std::string(who) + ": " + std::to_string((long long)s[6]) +
+                                       " fluid nodes have non-finite density or velocity");
+  return LBM_OK;
+}
+}  // namespace
+
 int lbm_residual(LbmHandle* h, double out[3]) {
   if (!h || !out) return fail(LBM_ERR_ARG, "lbm_residual: null argument");
   if (!h->has_residual) return fail(LBM_ERR_STATE, "lbm_residual: no residual step recorded (use LBM_STEP_RESIDUAL)");
   LBM_CUDA(cudaSetDevice(h->cfg.device));
   int rc = h->wait();
   if (rc) return rc;
-  const double* s = h->host_red;
-  for (int c = 0; c < 3; ++c) out[c] = std::sqrt(s[2 * c] / (s[2 * c + 1] + h->cfg.eps));
-  if (s[6] > 0)
-    return fail(LBM_ERR_NONFINITE, "lbm_residual: " + std::to_string((long long)s[6]) +
-                                       " fluid nodes have non-finite density or velocity");
-  return LBM_OK;
+  return residual_of(h, h->res_slot((int)((h->res_seq - 1) % kResRing)), out, "lbm_residual");
+}
+
+int lbm_residual_at(LbmHandle* h, int64_t t, double out[3]) {
+  if (!h || !out) return fail(LBM_ERR_ARG, "lbm_residual_at: null argument");
+  int slot = -1;
+  for (int i = 0; i < kResRing; ++i)
+    if (h->res_t[i] == t && t >= 0) slot = i;
+  if (slot < 0)
+    return fail(LBM_ERR_STATE, "lbm_residual_at: time step " + std::to_string((long long)t) +
+                                   " is not one of the last " + std::to_string(kResRing) +
+                                   " residual steps since initialisation");
+  LBM_CUDA(cudaSetDevice(h->cfg.device));
+  int rc = h->wait(h->res_ev[slot]);   // that step only, not the steps queued after it
+  if (rc) return rc;
+  return residual_of(h, h->res_slot(slot), out, "lbm_residual_at");
 }
 
 int lbm_conservation(LbmHandle* h, double out[3]) {
@@ -2156,7 +2203,7 @@ int lbm_load_state(LbmHandle* h, const void* in) {
     h->res_tuned = true;
   }
   h->has_moments = false;
-  h->has_residual = false;
+  h->clear_residuals();
   h->initialized = true;
   return LBM_OK;
 }

@@ -222,9 +222,16 @@ class FluidLBM:
             return rho.reshape(nx, ny), u.reshape(nx, ny, 2)
         return rho, u
 
-    def residual(self):
+    def residual(self, step=None):
+        """{res_rho, res_ux, res_uy} of the last residual step, or of the
+        residual step that ended at time step `step` (one of the last eight):
+        that form waits for that step only, so a loop can read step t's
+        residual while step t + 1 runs."""
         out = (ctypes.c_double * 3)()
-        check(self.lib.lbm_residual(self.h, out))
+        if step is None:
+            check(self.lib.lbm_residual(self.h, out))
+        else:
+            check(self.lib.lbm_residual_at(self.h, int(step), out))
         return np.array(out[:])
 
     def conservation(self):

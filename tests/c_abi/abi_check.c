@@ -55,6 +55,7 @@ int main(void) {
   CHECK(strstr(lbm_last_error(), "lbm_get_moments_f32") != NULL);
   double out[3];
   CHECK(lbm_residual(NULL, out) == LBM_ERR_ARG);
+  CHECK(lbm_residual_at(NULL, 1, out) == LBM_ERR_ARG);
   CHECK(lbm_conservation_noalloc(NULL, NULL, NULL) == LBM_ERR_ARG);
   int64_t nbytes = 0;
   CHECK(lbm_state_size(NULL, &nbytes) == LBM_ERR_ARG);

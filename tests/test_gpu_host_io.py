@@ -141,3 +141,38 @@ def test_single_precision_padded_initial_fields():
         a.step(5)
         b.step(5)
         assert np.array_equal(a.populations(), b.populations())
+
+
+@pytest.mark.parametrize("storage", ["fp64", "fp32_shifted"])
+def test_residual_read_while_the_next_step_runs(storage):
+    """lbm_residual_at(t) gives step t's residual (the one lbm_residual
+    returns right after step t) after later steps have been queued, for the
+    last eight residual steps; older or never-computed steps are refused,
+    and re-initialisation forgets them."""
+    case = Case(workloads.cylinder(nx=300, ny=120, radius=10.0, center=(80, 61)))
+    with FluidLBM(case, storage=storage) as sim:
+        sim.initialize()
+        sync = []
+        for _ in range(12):
+            sim.step(1, residual=True)
+            sync.append(sim.residual())
+    with FluidLBM(case, storage=storage) as sim:
+        sim.initialize()
+        piped = []
+        for t in range(1, 13):
+            sim.step(1, residual=True)
+            if t > 1:
+                piped.append(sim.residual(step=t - 1))
+        piped.append(sim.residual(step=12))
+        for t in range(5, 13):                          # the ring keeps the last eight
+            assert np.array_equal(sim.residual(step=t), sync[t - 1])
+        sim.step(3)                                     # plain steps do not touch the ring
+        assert np.array_equal(sim.residual(step=12), sync[11])
+        for t in (0, 4, 13, 15):
+            with pytest.raises(RuntimeError, match="residual steps"):
+                sim.residual(step=t)
+        sim.initialize()
+        with pytest.raises(RuntimeError, match="residual steps"):
+            sim.residual(step=12)
+    for a, b in zip(piped, sync):
+        assert np.array_equal(a, b)

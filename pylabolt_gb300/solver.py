@@ -90,6 +90,15 @@ class Solver:
     def checkpoint_path(self, t):
         return os.path.join(self.root, "output", "checkpoints", f"state_t{t}.npy")
 
+    def _log_residual(self, t):
+        """The residue line of time step t (SimulationStatusLogger.log_data,
+        pylabolt/solvers/fluidLB.py:370-375), from that step's residual sums:
+        a step with no other output is logged after the next steps have been
+        queued, so the GPU does not wait on the host between them."""
+        r = self.lbm.residual(step=t).astype(self.out.dtype)
+        self.residues = r
+        self.log(log_line(t, res_density=r[:1], res_velocity=r[1:]))
+
     def _checkpoint(self, t):
         if self.checkpoint_interval is None or t % self.checkpoint_interval:
             return
@@ -162,17 +171,22 @@ class Solver:
                 self.out.write_walls(0, self.wall_forces)
         t0 = time.perf_counter()
         t = c.start_time
+        pending = None   # a residual step whose line is logged once the next steps are queued
         while t < c.end_time:
             te = self._next_event(t)
             std, save, bnd, obs = self._events(te)
             self.lbm.step(te - t, moments=save, residual=std)
+            if pending is not None:   # read while the steps just queued run
+                self._log_residual(pending)
+                pending = None
             t = te
             self._checkpoint(t)
             self._update_forces(obs, bnd)
             if std:
-                r = self.lbm.residual().astype(self.out.dtype)
-                self.residues = r
-                self.log(log_line(t, res_density=r[:1], res_velocity=r[1:]))
+                if save or obs or bnd or t >= c.end_time:
+                    self._log_residual(t)
+                else:
+                    pending = t
             if save:
                 rho, u = self.lbm.moments(dtype=self.out.dtype)
                 if c.moving:

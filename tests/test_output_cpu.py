@@ -58,9 +58,9 @@ class GoldenLBM:
         return {"obstacles": self.g[f"force_obstacles_t{self.t}"],
                 "walls": self.g[f"force_walls_t{self.t}"]}
 
-    def residual(self):
+    def residual(self, step=None):
         res = {int(r[0]): r[1:] for r in self.d["residues"]}
-        return np.array(res[self.t])
+        return np.array(res[self.t if step is None else step])
 
     def synchronize(self):
         pass

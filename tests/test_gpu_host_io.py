@@ -143,20 +143,20 @@ def test_single_precision_padded_initial_fields():
         assert np.array_equal(a.populations(), b.populations())
 
 
-@pytest.mark.parametrize("storage", ["fp64", "fp32_shifted"])
-def test_residual_read_while_the_next_step_runs(storage):
+@pytest.mark.parametrize("storage,layout", [("fp64", "ab"), ("fp32_shifted", "ab"), ("fp32_shifted", "aa")])
+def test_residual_read_while_the_next_step_runs(storage, layout):
     """lbm_residual_at(t) gives step t's residual (the one lbm_residual
     returns right after step t) after later steps have been queued, for the
     last eight residual steps; older or never-computed steps are refused,
     and re-initialisation forgets them."""
     case = Case(workloads.cylinder(nx=300, ny=120, radius=10.0, center=(80, 61)))
-    with FluidLBM(case, storage=storage) as sim:
+    with FluidLBM(case, storage=storage, layout=layout) as sim:
         sim.initialize()
         sync = []
         for _ in range(12):
             sim.step(1, residual=True)
             sync.append(sim.residual())
-    with FluidLBM(case, storage=storage) as sim:
+    with FluidLBM(case, storage=storage, layout=layout) as sim:
         sim.initialize()
         piped = []
         for t in range(1, 13):

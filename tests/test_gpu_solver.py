@@ -122,3 +122,30 @@ def test_solver_moving_obstacle_outputs(tmp_path, capsys):
         assert np.array_equal(z["solid"], (X - cx) ** 2 + (Y - 16.0) ** 2 <= 16.0)
         assert np.all(z["solid_id"][z["solid"]] == 0)
         assert np.all(z["fluid_boundary"] <= ~z["solid"])
+
+
+def test_residue_lines_read_while_the_next_steps_run(tmp_path, capsys, monkeypatch):
+    """A status line on every step, field output every 20: the lines of steps
+    with no other output are logged once the next step is queued, and carry
+    the values of a run that reads each residual right after its step (one
+    launch shape for both, so the sums are the same bits)."""
+    from pylabolt_gb300 import workloads
+    from pylabolt_gb300.config import Case
+    from pylabolt_gb300.lbm import FluidLBM
+    monkeypatch.setenv("LBM_VARIANT", "3,2,128,1")
+    c = workloads.cavity(64, re=100.0)
+    c["control_dict"].update({"end_time": 45, "std_out_interval": 1, "save_interval": 20})
+    s = solver.Solver(c, root=str(tmp_path), storage="fp32_shifted")
+    try:
+        s.run()
+    finally:
+        s.close()
+    lines = [l for l in capsys.readouterr().out.splitlines() if l.startswith("time:")]
+    assert [int(l.split()[1]) for l in lines] == list(range(1, 46))
+    dtype = s.out.dtype
+    with FluidLBM(Case(c), storage="fp32_shifted") as sim:
+        sim.initialize()
+        for t, line in enumerate(lines, 1):
+            sim.step(1, residual=True)
+            r = sim.residual().astype(dtype)
+            assert line == output.log_line(t, res_density=r[:1], res_velocity=r[1:]), t

@@ -630,7 +630,7 @@ struct LbmHandle {
         }
       }
     }
-    // second round: the three fastest again, 8 launches each, interleaved
+    // second pass: the three fastest again, 8 launches each, interleaved
     // twice, keeping each one's better mean (one short timing can be off by
     // a clock ramp or a neighbour's burst)
     if (rc == LBM_OK && ks->nvariants > 1) {

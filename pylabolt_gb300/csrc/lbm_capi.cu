@@ -49,6 +49,7 @@ constexpr uint64_t kFnvSeed = 14695981039346656037ull;
   } while (0)
 
 constexpr int kGraphChunk = 32;   // steps per captured graph (even)
+constexpr int kTailGraphs = 4;    // graphs of fewer steps kept (the remainder of a call)
 constexpr int kResRing = 8;       // residual steps whose sums stay readable
 constexpr int kCX[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
 constexpr int kCY[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
@@ -99,6 +100,14 @@ struct LbmHandle {
   int64_t t = 0, launches = 0;
   cudaGraphExec_t gexec = nullptr;
   int gparity = 0;
+  // graphs of 2 .. kGraphChunk - 1 plain steps, by step count and starting
+  // buffer parity, the most recent kTailGraphs kept
+  struct TailGraph {
+    int count = 0, parity = 0;
+    cudaGraphExec_t exec = nullptr;
+  };
+  TailGraph tails[kTailGraphs];
+  int tail_next = 0;
   lbm::Variant variant{0, 1, 256, 0};
   lbm::Variant res_variant{0, 1, 256, 0};   // shape of residual steps (tuned on the first)
   bool res_tuned = false;
@@ -181,7 +190,7 @@ struct LbmHandle {
   }
 
   ~LbmHandle() {
-    if (gexec) cudaGraphExecDestroy(gexec);
+    drop_graphs();
     if (adj.fwd_graph) cudaGraphExecDestroy(adj.fwd_graph);
     if (adj.bwd_graph) cudaGraphExecDestroy(adj.bwd_graph);
     for (cudaEvent_t e : adj.ev)
@@ -711,12 +720,16 @@ struct LbmHandle {
     return LBM_OK;
   }
 
-  int capture_graph() {
+  // Captures `count` plain steps starting from buffer parity `parity` into
+  // an executable graph (nothing runs; cur is left as it was).
+  int capture_steps(int count, int parity, cudaGraphExec_t* out) {
     cudaGraph_t graph = nullptr;
+    *out = nullptr;
     LBM_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     const int c0 = cur;
+    cur = parity;
     int rc = LBM_OK;
-    for (int i = 0; i < kGraphChunk && rc == LBM_OK; ++i) rc = step_full(0);
+    for (int i = 0; i < count && rc == LBM_OK; ++i) rc = step_full(0);
     cudaError_t e = cudaStreamEndCapture(stream, &graph);
     cur = c0;
     if (rc) {
@@ -724,13 +737,73 @@ struct LbmHandle {
       return rc;
     }
     if (e != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&gexec, graph, 0);
+    e = cudaGraphInstantiate(out, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) {
-      gexec = nullptr;
+      *out = nullptr;
       return fail(LBM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     }
-    gparity = c0;
+    return LBM_OK;
+  }
+
+  // The kGraphChunk-step graph, from parity `parity`.
+  int capture_graph(int parity) {
+    const int rc = capture_steps(kGraphChunk, parity, &gexec);
+    if (rc == LBM_OK) gparity = parity;
+    return rc;
+  }
+
+  // The graph of `count` (2 .. kGraphChunk - 1) plain steps from parity
+  // `parity`, captured on first use.
+  int tail_graph(int count, int parity, cudaGraphExec_t* out) {
+    for (const TailGraph& t : tails)
+      if (t.exec && t.count == count && t.parity == parity) {
+        *out = t.exec;
+        return LBM_OK;
+      }
+    TailGraph& t = tails[tail_next];
+    tail_next = (tail_next + 1) % kTailGraphs;
+    if (t.exec) cudaGraphExecDestroy(t.exec);   // freed once a launch in flight ends
+    t = TailGraph{};
+    const int rc = capture_steps(count, parity, &t.exec);
+    if (rc) return rc;
+    t.count = count;
+    t.parity = parity;
+    *out = t.exec;
+    return LBM_OK;
+  }
+
+  // Graphs hold the kernel arguments and buffer parity of their capture.
+  void drop_graphs() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    gexec = nullptr;
+    for (TailGraph& t : tails) {
+      if (t.exec) cudaGraphExecDestroy(t.exec);
+      t = TailGraph{};
+    }
+  }
+
+  // Captures, before a timed call, the graphs an lbm_step(nsteps) from the
+  // present state will launch, following the step loop's choices.
+  int prepare_graphs(int64_t nsteps) {
+    if (std::getenv("LBM_NO_GRAPH") || !tuned || nopull || nsteps < 2) return LBM_OK;
+    int64_t plain = nsteps - 1;   // the last step is launched on its own
+    int c = cur;
+    int rc;
+    while (plain > 0) {
+      if (plain >= kGraphChunk) {
+        if (!gexec && (rc = capture_graph(c))) return rc;
+        if (c == gparity) {
+          plain -= kGraphChunk;
+          continue;
+        }
+      } else if (plain >= 2) {
+        cudaGraphExec_t ex = nullptr;
+        return tail_graph((int)plain, c, &ex);
+      }
+      c ^= 1;
+      --plain;
+    }
     return LBM_OK;
   }
 };
@@ -1265,10 +1338,7 @@ int lbm_set_omega_map(LbmHandle* h, const double* omega) {
   LBM_CUDA(cudaMemcpyAsync(h->omega_seg, seg.data(), seg.size() * sizeof(float), cudaMemcpyHostToDevice,
                            h->stream));
   h->omega_hash = fnv1a(kFnvSeed, seg.data(), seg.size() * sizeof(float));
-  if (h->gexec) {   // graphs captured earlier hold the old argument
-    cudaGraphExecDestroy(h->gexec);
-    h->gexec = nullptr;
-  }
+  h->drop_graphs();   // graphs captured earlier hold the old argument
   return h->wait();
 }
 
@@ -1300,9 +1370,10 @@ int lbm_step_ex(LbmHandle* h, int64_t nsteps, int flags) {
   // tune on the steady (pulling) step, which all later steps use
   if (!h->tuned && !h->nopull && s < nsteps && (rc = h->autotune())) return rc;
   int64_t plain = nsteps - s - (s < nsteps ? 1 : 0);
+  const bool graphs = !std::getenv("LBM_NO_GRAPH");
   while (plain > 0) {
-    if (plain >= kGraphChunk && !std::getenv("LBM_NO_GRAPH")) {
-      if (!h->gexec && (rc = h->capture_graph())) return rc;
+    if (plain >= kGraphChunk && graphs) {
+      if (!h->gexec && (rc = h->capture_graph(h->cur))) return rc;
       if (h->cur == h->gparity) {
         LBM_CUDA(cudaGraphLaunch(h->gexec, h->stream));
         h->t += kGraphChunk;
@@ -1310,6 +1381,15 @@ int lbm_step_ex(LbmHandle* h, int64_t nsteps, int flags) {
         plain -= kGraphChunk;
         continue;
       }
+    } else if (plain >= 2 && graphs) {   // the remainder, as one graph of its own
+      cudaGraphExec_t ex = nullptr;
+      if ((rc = h->tail_graph((int)plain, h->cur, &ex))) return rc;
+      LBM_CUDA(cudaGraphLaunch(ex, h->stream));
+      h->cur ^= (int)(plain & 1);
+      h->t += plain;
+      h->launches += plain;
+      plain = 0;
+      continue;
     }
     if ((rc = one(0))) return rc;
     --plain;
@@ -1880,10 +1960,7 @@ int lbm_set_moving_obstacles(LbmHandle* h, const LbmMovingObstacle* obs, int n,
     }
   h->tuned = false;
   h->res_tuned = false;
-  if (h->gexec) {
-    cudaGraphExecDestroy(h->gexec);
-    h->gexec = nullptr;
-  }
+  h->drop_graphs();
   // the obstacles are placed by lbm_init_fields, which must come next
   h->initialized = false;
   return h->wait();
@@ -1987,7 +2064,13 @@ int lbm_time_steps(LbmHandle* h, int64_t nsteps, double* ms) {
   cudaEvent_t e0, e1;
   LBM_CUDA(cudaEventCreate(&e0));
   LBM_CUDA(cudaEventCreate(&e1));
-  int rc = LBM_OK;
+  // graphs are captured before the timed region (capture runs nothing)
+  int rc = h->initialized ? h->prepare_graphs(nsteps) : LBM_OK;
+  if (rc) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+  }
   cudaError_t e = cudaEventRecord(e0, h->stream);
   if (e == cudaSuccess) {
     rc = lbm_step(h, nsteps);
@@ -2165,10 +2248,7 @@ int lbm_load_state(LbmHandle* h, const void* in) {
   int rc;
   if (H.has_old && (rc = h->ensure_old())) return rc;
   h->initialized = false;   // until the state is complete
-  if (h->gexec) {           // graphs captured earlier hold the old buffer parity
-    cudaGraphExecDestroy(h->gexec);
-    h->gexec = nullptr;
-  }
+  h->drop_graphs();   // graphs captured earlier hold the old buffer parity
   h->cur = h->aa ? H.cur : 0;   // AA: the phase; two buffers: restore into buffer 0
   const char* p = static_cast<const char*>(in) + sizeof H;
   LBM_CUDA(cudaMemcpyAsync(h->pop_raw[h->cur], p, H.pop_bytes, cudaMemcpyHostToDevice, h->stream));

@@ -158,8 +158,9 @@ int lbm_set_omega_map(LbmHandle* h, const double* omega);
 
 /* Advances nsteps time steps, each one Solver.single_time_step
  * (pylabolt/solvers/fluidLB.py:206-253: density, force, velocity, collide,
- * periodic wrap, stream, boundaries) as one fused kernel launch.  Long runs
- * are replayed from a captured CUDA graph (the reference captures one step,
+ * periodic wrap, stream, boundaries) as one fused kernel launch.  Runs of
+ * steps are replayed from captured CUDA graphs: 32-step chunks and the rest
+ * of the call as one graph (the reference captures one step,
  * fluidLB.py:270-287). */
 int lbm_step(LbmHandle* h, int64_t nsteps);
 
